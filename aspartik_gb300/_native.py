@@ -1,0 +1,128 @@
+"""ctypes binding of ``libb3g.so`` (the C ABI in ``include/b3g.h``).
+
+The library is the only compute path: importing this module fails loudly when
+the shared object is missing, and every non-OK status raises ``B3GError`` with
+the library's own message.  There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libb3g.so"
+
+B3G_OK = 0
+B3G_ERR_INVALID_ARGUMENT = 1
+B3G_ERR_OUT_OF_MEMORY = 2
+B3G_ERR_CUDA = 3
+B3G_ERR_TIMEOUT = 4
+B3G_ERR_NUMERIC = 5
+B3G_ERR_STATE = 6
+
+PRECISION_F64 = 0
+PRECISION_F32 = 1
+
+STATUS_NAMES = {
+    0: "OK",
+    1: "INVALID_ARGUMENT",
+    2: "OUT_OF_MEMORY",
+    3: "CUDA",
+    4: "TIMEOUT",
+    5: "NUMERIC",
+    6: "STATE",
+}
+
+
+class B3GError(RuntimeError):
+    """A b3g call returned a non-OK status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"b3g {STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Config(ct.Structure):
+    _fields_ = [
+        ("num_leaves", ct.c_uint32),
+        ("num_patterns", ct.c_uint32),
+        ("num_states", ct.c_uint32),
+        ("num_categories", ct.c_uint32),
+        ("precision", ct.c_uint32),
+        ("scale_ln", ct.c_uint32),
+        ("device", ct.c_int32),
+        ("reserved", ct.c_uint32),
+    ]
+
+
+_u8p = ct.POINTER(ct.c_uint8)
+_u32p = ct.POINTER(ct.c_uint32)
+_f64p = ct.POINTER(ct.c_double)
+_f32p = ct.POINTER(ct.c_float)
+_vp = ct.c_void_p
+
+# name -> (restype, argtypes); every function declared in include/b3g.h
+SIGNATURES = {
+    "b3g_last_error": (ct.c_char_p, []),
+    "b3g_version": (ct.c_char_p, []),
+    "b3g_calculator_create": (ct.c_int, [ct.POINTER(Config), _u8p, ct.POINTER(_vp)]),
+    "b3g_calculator_destroy": (None, [_vp]),
+    "b3g_calculator_num_patterns": (ct.c_uint32, [_vp]),
+    "b3g_calculator_propose": (ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, _f64p]),
+    "b3g_calculator_likelihoods": (ct.c_int, [_vp, _f64p]),
+    "b3g_calculator_accept": (ct.c_int, [_vp]),
+    "b3g_calculator_reject": (ct.c_int, [_vp]),
+    "b3g_calculator_set_weights": (ct.c_int, [_vp, _u32p]),
+    "b3g_calculator_set_eigen": (ct.c_int, [_vp, _f64p, _f64p, _f64p, _f64p, _f64p, ct.c_int]),
+    "b3g_calculator_set_reversible": (ct.c_int, [_vp, _f64p, _f64p, ct.c_int]),
+    "b3g_calculator_set_category_rates": (ct.c_int, [_vp, _f64p]),
+    "b3g_calculator_set_gamma": (ct.c_int, [_vp, ct.c_double]),
+    "b3g_calculator_propose_lengths": (
+        ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
+    "b3g_calculator_log_likelihood": (ct.c_int, [_vp, _f64p]),
+    "b3g_calculator_site_log_likelihoods": (ct.c_int, [_vp, _f64p]),
+    "b3g_calculator_last_timing": (ct.c_int, [_vp, _f32p, _f32p]),
+    "b3g_calculator_timing_totals": (
+        ct.c_int, [_vp, ct.c_int, _f64p, _f64p, ct.POINTER(ct.c_uint64)]),
+    "b3g_calculator_span_begin": (ct.c_int, [_vp]),
+    "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
+}
+
+
+def _load() -> ct.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -m aspartik_gb300.build` "
+            "(the GPU library is the only compute path; there is no fallback)")
+    lib = ct.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def check(status: int) -> None:
+    if status != B3G_OK:
+        raise B3GError(status, lib.b3g_last_error().decode())
+
+
+def as_ptr(arr: np.ndarray, ctype):
+    return arr.ctypes.data_as(ct.POINTER(ctype))
+
+
+def u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def u8(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint8)

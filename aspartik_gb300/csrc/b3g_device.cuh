@@ -1,0 +1,89 @@
+// b3g_device.cuh -- device-side layouts shared by the b3g kernels and the
+// host orchestration.
+//
+// Device store of one calculator (one chain), all resident in HBM:
+//   tips      u8  [L][ldp]                   state 0..S-1, S = unknown
+//   partials  R   [2I][C][ldp][S]            slot = (v - L) * 2 + selector
+//   scales    i32 [2I][C][ldp]               cumulative rescale count of the
+//                                            subtree below the slot's node
+//   ptab      R   [n][2][C][S+1][S]          per-step transposed transition
+//                                            tables, row S = all ones
+// ldp is the pattern count rounded up to a multiple of 128; padded patterns
+// carry unknown tips and weight 0.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace b3g {
+
+constexpr uint32_t kTipBit = 0x80000000u;
+constexpr int kMaxStates = 20;
+constexpr int kMaxCategories = 16;
+constexpr uint32_t kPatternAlign = 128;
+
+// One entry of the children-first schedule: output slot and the two
+// children, each either a partial slot or (kTipBit | leaf id).
+struct NodeOp {
+	uint32_t out;
+	uint32_t left;
+	uint32_t right;
+	uint32_t pad;
+};
+
+// Substitution model resident on the device.  Written by the host
+// (eigensystem given) or by eigen_kernel (device decomposition).
+struct ModelDev {
+	double V[kMaxStates * kMaxStates];
+	double Vinv[kMaxStates * kMaxStates];
+	double lambda[kMaxStates];
+	double Q[kMaxStates * kMaxStates];
+	double pi[kMaxStates];
+	double cat_rates[kMaxCategories];
+	double rates_in[kMaxStates * (kMaxStates - 1) / 2]; // eigen_kernel input
+	double pi_in[kMaxStates];                           // eigen_kernel input
+	uint32_t shortcuts;
+	uint32_t states;
+	uint32_t jacobi_sweeps; // written by eigen_kernel
+	uint32_t status;        // 0 ok, 1 Jacobi did not converge
+};
+
+struct PtabParams {
+	const double *lengths;  // [n][2] time lengths, or null
+	const double *matrices; // [n][2][C][S][S], or null
+	const ModelDev *model;
+	double clock_rate;
+	uint32_t n;
+	uint32_t C;
+	void *ptab; // R [n][2][C][S+1][S]
+};
+
+struct PruneParams {
+	const uint8_t *tips;
+	void *partials;
+	int32_t *scales;
+	const NodeOp *ops;
+	const void *ptab;
+	const double *pi;
+	const uint32_t *weights;
+	double *site_lnl;   // [ldp]
+	double *cat_lnl;    // [C][ldp] or null
+	double *block_sums; // [gridDim.x]
+	unsigned *ticket;   // zero between launches
+	double *lnl_out;    // [1]
+	uint32_t n;
+	uint32_t ldp;
+	uint32_t C;
+	uint32_t scale_ln;
+	double scale_threshold;
+	double scale_mult;
+	double log_inv_c;
+};
+
+// Launchers (kernels4.cu).  Each returns the launch error.
+cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);
+cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
+			  cudaStream_t s);
+cudaError_t launch_eigen(ModelDev *model, cudaStream_t s);
+
+} // namespace b3g

@@ -1,0 +1,848 @@
+// calculator.cu -- host orchestration of one device-resident pruning store
+// and the C ABI declared in include/b3g.h.
+#include "calculator.hpp"
+#include "host_math.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+#include <new>
+
+namespace b3g {
+
+void check_cuda(cudaError_t e, const char *what)
+{
+	if (e == cudaSuccess)
+		return;
+	const b3g_status s = e == cudaErrorMemoryAllocation
+				     ? B3G_ERR_OUT_OF_MEMORY
+				     : B3G_ERR_CUDA;
+	throw Error(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct DeviceGuard {
+	int prev = -1;
+	explicit DeviceGuard(int dev)
+	{
+		check_cuda(cudaGetDevice(&prev), "cudaGetDevice");
+		if (prev != dev)
+			check_cuda(cudaSetDevice(dev), "cudaSetDevice");
+	}
+	~DeviceGuard()
+	{
+		int cur = -1;
+		if (cudaGetDevice(&cur) == cudaSuccess && cur != prev && prev >= 0)
+			cudaSetDevice(prev);
+	}
+};
+
+template <typename T> void dev_alloc(T *&p, size_t bytes, const char *what)
+{
+	void *v = nullptr;
+	check_cuda(cudaMalloc(&v, bytes ? bytes : 1), what);
+	p = static_cast<T *>(v);
+}
+
+// EditBuf::set_edited (sk/src/editbuf.rs:71-81)
+inline void set_edited(uint8_t &m)
+{
+	if (!(m & 2u))
+		m = static_cast<uint8_t>(((m & 1u) ^ 1u) | 2u);
+}
+
+} // namespace
+
+Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
+{
+	if (cfg.num_leaves < 2)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_leaves must be >= 2");
+	if (cfg.num_patterns < 1)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_patterns must be >= 1");
+	if (cfg.num_states != 4)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "num_states must be 4 for this calculator");
+	if (cfg.num_categories < 1 || cfg.num_categories > kMaxCategories)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "num_categories must be in 1..16");
+	if (cfg.precision != B3G_PRECISION_F64 &&
+	    cfg.precision != B3G_PRECISION_F32)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "unknown precision");
+	if (cfg.reserved != 0)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "reserved must be 0");
+	if (!samples)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "samples is null");
+	if (cfg.num_leaves > (1u << 24) || cfg.num_patterns > (1u << 28))
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "problem too large");
+
+	L_ = cfg.num_leaves;
+	I_ = L_ - 1;
+	P_ = cfg.num_patterns;
+	S_ = cfg.num_states;
+	C_ = cfg.num_categories;
+	f32_ = cfg.precision == B3G_PRECISION_F32;
+	scale_ln_ = cfg.scale_ln;
+	device_ = cfg.device;
+	ldp_ = static_cast<uint32_t>(align_up(P_, kPatternAlign));
+	// patterns per block: 128 threads for up to 4 categories, one warp of
+	// patterns per category above that (at most 16 x 32 = 512 threads)
+	tile_ = C_ <= 1 ? 128 : C_ == 2 ? 64 : 32;
+
+	int ndev = 0;
+	check_cuda(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+	if (device_ < 0 || device_ >= ndev)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "no such CUDA device");
+	DeviceGuard g(device_);
+
+	selectors_.assign(I_, 0);
+	stamp_.assign(2 * L_ - 1, 0);
+
+	const size_t slots = 2ull * I_;
+	const size_t rsz = f32_ ? sizeof(float) : sizeof(double);
+	const size_t nblocks = ldp_ / tile_;
+
+	try {
+		check_cuda(cudaStreamCreateWithFlags(&stream_,
+						     cudaStreamNonBlocking),
+			   "cudaStreamCreate");
+		check_cuda(cudaEventCreateWithFlags(&ev_stage_free_,
+						    cudaEventDisableTiming),
+			   "cudaEventCreate");
+		check_cuda(cudaEventCreateWithFlags(&ev_model_free_,
+						    cudaEventDisableTiming),
+			   "cudaEventCreate");
+		check_cuda(cudaEventCreate(&ev_span0_), "cudaEventCreate");
+		check_cuda(cudaEventCreate(&ev_span1_), "cudaEventCreate");
+		for (auto &slot : ring_) {
+			check_cuda(cudaEventCreate(&slot.k0), "cudaEventCreate");
+			check_cuda(cudaEventCreate(&slot.kmid), "cudaEventCreate");
+			check_cuda(cudaEventCreate(&slot.k1), "cudaEventCreate");
+		}
+
+		dev_alloc(d_tips_, (size_t)L_ * ldp_, "tips");
+		dev_alloc(d_partials_, slots * C_ * ldp_ * S_ * rsz, "partials");
+		dev_alloc(d_scales_, slots * C_ * ldp_ * sizeof(int32_t), "scales");
+		dev_alloc(d_weights_, ldp_ * sizeof(uint32_t), "weights");
+		dev_alloc(d_site_, ldp_ * sizeof(double), "site lnl");
+		dev_alloc(d_cat_, (size_t)C_ * ldp_ * sizeof(double), "cat lnl");
+		dev_alloc(d_block_sums_, nblocks * sizeof(double), "block sums");
+		dev_alloc(d_ticket_, sizeof(unsigned), "ticket");
+		dev_alloc(d_lnl_, sizeof(double), "lnl");
+		dev_alloc(d_model_, sizeof(ModelDev), "model");
+		dev_alloc(d_ptab_, (size_t)I_ * 2 * C_ * (S_ + 1) * S_ * rsz,
+			  "transition tables");
+
+		off_pi_ = align_up((size_t)I_ * sizeof(NodeOp), 256);
+		off_in_ = align_up(off_pi_ + S_ * sizeof(double), 256);
+		stage_bytes_ = off_in_ + (size_t)I_ * 2 * C_ * S_ * S_ * sizeof(double);
+		dev_alloc(d_stage_, stage_bytes_, "stage");
+		check_cuda(cudaHostAlloc((void **)&h_stage_, stage_bytes_,
+					 cudaHostAllocDefault),
+			   "pinned stage");
+		check_cuda(cudaHostAlloc((void **)&h_model_, sizeof(ModelDev),
+					 cudaHostAllocDefault),
+			   "pinned model");
+		check_cuda(cudaHostAlloc((void **)&h_lnl_, sizeof(double),
+					 cudaHostAllocDefault),
+			   "pinned lnl");
+
+		// tips: single bases -> 0..3, everything else -> unknown (4)
+		// (cpu4.rs:117-124); padded patterns are unknown too
+		std::vector<uint8_t> tips((size_t)L_ * ldp_, 4);
+		for (uint32_t l = 0; l < L_; ++l)
+			for (uint32_t p = 0; p < P_; ++p) {
+				uint8_t code = samples[(size_t)l * P_ + p];
+				uint8_t s = code == 1 ? 0 : code == 2 ? 1
+							   : code == 4 ? 2
+							   : code == 8 ? 3
+								       : 4;
+				tips[(size_t)l * ldp_ + p] = s;
+			}
+		check_cuda(cudaMemcpy(d_tips_, tips.data(), tips.size(),
+				      cudaMemcpyHostToDevice),
+			   "upload tips");
+		std::vector<uint32_t> w(ldp_, 0);
+		for (uint32_t p = 0; p < P_; ++p)
+			w[p] = 1;
+		check_cuda(cudaMemcpy(d_weights_, w.data(), ldp_ * sizeof(uint32_t),
+				      cudaMemcpyHostToDevice),
+			   "upload weights");
+		// Buffer::zeroed partials (cpu4.rs:134-136)
+		check_cuda(cudaMemset(d_partials_, 0, slots * C_ * ldp_ * S_ * rsz),
+			   "zero partials");
+		check_cuda(cudaMemset(d_scales_, 0,
+				      slots * C_ * ldp_ * sizeof(int32_t)),
+			   "zero scales");
+		check_cuda(cudaMemset(d_ticket_, 0, sizeof(unsigned)), "ticket");
+
+		std::memset(&model_host_, 0, sizeof(model_host_));
+		model_host_.states = S_;
+		for (uint32_t c = 0; c < C_; ++c)
+			model_host_.cat_rates[c] = 1.0;
+		upload_model();
+		check_cuda(cudaStreamSynchronize(stream_), "construct sync");
+	} catch (...) {
+		release();
+		throw;
+	}
+}
+
+Calculator::~Calculator() { release(); }
+
+void Calculator::release()
+{
+	if (device_ >= 0)
+		cudaSetDevice(device_);
+	if (stream_)
+		cudaStreamSynchronize(stream_);
+	cudaFree(d_tips_);
+	cudaFree(d_partials_);
+	cudaFree(d_scales_);
+	cudaFree(d_weights_);
+	cudaFree(d_site_);
+	cudaFree(d_cat_);
+	cudaFree(d_block_sums_);
+	cudaFree(d_ticket_);
+	cudaFree(d_lnl_);
+	cudaFree(d_model_);
+	cudaFree(d_ptab_);
+	cudaFree(d_stage_);
+	cudaFreeHost(h_stage_);
+	cudaFreeHost(h_model_);
+	cudaFreeHost(h_lnl_);
+	d_tips_ = nullptr;
+	d_partials_ = nullptr;
+	d_scales_ = nullptr;
+	d_weights_ = nullptr;
+	d_site_ = d_cat_ = d_block_sums_ = d_lnl_ = nullptr;
+	d_ticket_ = nullptr;
+	d_model_ = nullptr;
+	d_ptab_ = nullptr;
+	d_stage_ = nullptr;
+	h_stage_ = nullptr;
+	h_model_ = nullptr;
+	h_lnl_ = nullptr;
+	for (cudaEvent_t *e : {&ev_stage_free_, &ev_model_free_, &ev_span0_,
+			       &ev_span1_})
+		if (*e) {
+			cudaEventDestroy(*e);
+			*e = nullptr;
+		}
+	for (auto &slot : ring_)
+		for (cudaEvent_t *e : {&slot.k0, &slot.kmid, &slot.k1})
+			if (*e) {
+				cudaEventDestroy(*e);
+				*e = nullptr;
+			}
+	if (stream_) {
+		cudaStreamDestroy(stream_);
+		stream_ = nullptr;
+	}
+}
+
+void Calculator::upload_model()
+{
+	check_cuda(cudaEventSynchronize(ev_model_free_), "model staging");
+	std::memcpy(h_model_, &model_host_, sizeof(ModelDev));
+	check_cuda(cudaMemcpyAsync(d_model_, h_model_, sizeof(ModelDev),
+				   cudaMemcpyHostToDevice, stream_),
+		   "upload model");
+	check_cuda(cudaEventRecord(ev_model_free_, stream_), "event");
+}
+
+// The dirty list must name distinct internals, children must be valid node
+// ids, and an internal child that is itself listed must come first
+// (children-first order of partials_lists, parameters/tree.rs:398-421).
+void Calculator::validate_lists(const uint32_t *internals,
+				const uint32_t *children, uint32_t n)
+{
+	if (!internals || !children)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null list");
+	if (n < 1 || n > I_)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "dirty list length must be in 1..num_internals");
+	const uint32_t nodes = 2 * L_ - 1;
+	// two stamps per call: `listed` marks the dirty internals, `done` the
+	// ones already visited in list order
+	if (stamp_epoch_ > 0xfffffff0u) {
+		std::fill(stamp_.begin(), stamp_.end(), 0u);
+		stamp_epoch_ = 0;
+	}
+	const uint32_t listed = ++stamp_epoch_;
+	const uint32_t done = ++stamp_epoch_;
+	for (uint32_t i = 0; i < n; ++i) {
+		const uint32_t v = internals[i];
+		if (v < L_ || v >= nodes)
+			throw Error(B3G_ERR_INVALID_ARGUMENT,
+				    "dirty list entry is not an internal node");
+		if (stamp_[v] == listed)
+			throw Error(B3G_ERR_INVALID_ARGUMENT,
+				    "dirty list names a node twice");
+		stamp_[v] = listed;
+	}
+	for (uint32_t i = 0; i < n; ++i) {
+		const uint32_t v = internals[i];
+		const uint32_t l = children[2 * i], r = children[2 * i + 1];
+		for (const uint32_t ch : {l, r}) {
+			if (ch >= nodes || ch == v)
+				throw Error(B3G_ERR_INVALID_ARGUMENT,
+					    "child is not a node id");
+			if (ch >= L_ && stamp_[ch] == listed)
+				throw Error(B3G_ERR_INVALID_ARGUMENT,
+					    "dirty list is not children-first");
+		}
+		if (l == r)
+			throw Error(B3G_ERR_INVALID_ARGUMENT,
+				    "both children are the same node");
+		stamp_[v] = done;
+	}
+}
+
+// Flips the selectors of the listed internals (Cpu4Calculator::
+// set_selectors, cpu4.rs:93-98) and writes the schedule: output slot of each
+// listed node and the slot or leaf of each child.
+void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
+			   uint32_t n)
+{
+	for (uint32_t i = 0; i < n; ++i)
+		set_edited(selectors_[internals[i] - L_]);
+	NodeOp *ops = reinterpret_cast<NodeOp *>(h_stage_);
+	auto slot_of = [&](uint32_t v) {
+		const uint32_t k = v - L_;
+		return k * 2 + (selectors_[k] & 1u);
+	};
+	for (uint32_t i = 0; i < n; ++i) {
+		NodeOp op;
+		op.out = slot_of(internals[i]);
+		const uint32_t l = children[2 * i], r = children[2 * i + 1];
+		op.left = l < L_ ? (kTipBit | l) : slot_of(l);
+		op.right = r < L_ ? (kTipBit | r) : slot_of(r);
+		op.pad = 0;
+		ops[i] = op;
+	}
+}
+
+void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
+			bool want_cat)
+{
+	const size_t in_bytes =
+		matrices_mode ? (size_t)n * 2 * C_ * S_ * S_ * sizeof(double)
+			      : (size_t)n * 2 * sizeof(double);
+	check_cuda(cudaMemcpyAsync(d_stage_, h_stage_, off_in_ + in_bytes,
+				   cudaMemcpyHostToDevice, stream_),
+		   "upload step");
+	check_cuda(cudaEventRecord(ev_stage_free_, stream_), "event");
+	TimingSlot &slot = ring_[ring_next_ % kRing];
+	if (slot.pending)
+		harvest(slot); // recorded kRing proposals ago: long complete
+	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
+
+	PtabParams pt{};
+	pt.lengths = matrices_mode
+			     ? nullptr
+			     : reinterpret_cast<const double *>(d_stage_ + off_in_);
+	pt.matrices = matrices_mode
+			      ? reinterpret_cast<const double *>(d_stage_ + off_in_)
+			      : nullptr;
+	pt.model = d_model_;
+	pt.clock_rate = clock_rate;
+	pt.n = n;
+	pt.C = C_;
+	pt.ptab = d_ptab_;
+	check_cuda(launch_ptab4(pt, f32_, stream_), "transition kernel");
+	check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+
+	PruneParams pp{};
+	pp.tips = d_tips_;
+	pp.partials = d_partials_;
+	pp.scales = d_scales_;
+	pp.ops = reinterpret_cast<const NodeOp *>(d_stage_);
+	pp.ptab = d_ptab_;
+	pp.pi = reinterpret_cast<const double *>(d_stage_ + off_pi_);
+	pp.weights = d_weights_;
+	pp.site_lnl = d_site_;
+	pp.cat_lnl = want_cat ? d_cat_ : nullptr;
+	pp.block_sums = d_block_sums_;
+	pp.ticket = d_ticket_;
+	pp.lnl_out = d_lnl_;
+	pp.n = n;
+	pp.ldp = ldp_;
+	pp.C = C_;
+	pp.scale_ln = scale_ln_;
+	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
+	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
+	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
+	check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
+	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
+	slot.pending = true;
+	++ring_next_;
+	check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
+				   cudaMemcpyDeviceToHost, stream_),
+		   "read lnl");
+	have_result_ = true;
+	cat_valid_ = want_cat;
+}
+
+void Calculator::propose_matrices(const uint32_t *internals,
+				  const uint32_t *children, uint32_t n,
+				  const double *matrices, const double *freqs)
+{
+	DeviceGuard g(device_);
+	validate_lists(internals, children, n);
+	if (!matrices || !freqs)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null matrices");
+	const size_t count = (size_t)n * 2 * C_ * S_ * S_;
+	for (size_t k = 0; k < count; ++k)
+		if (!std::isfinite(matrices[k]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite transition matrix");
+	for (uint32_t s = 0; s < S_; ++s)
+		if (!std::isfinite(freqs[s]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite frequency");
+	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	stage_ops(internals, children, n);
+	std::memcpy(h_stage_ + off_pi_, freqs, S_ * sizeof(double));
+	std::memcpy(h_stage_ + off_in_, matrices, count * sizeof(double));
+	launch(n, true, 1.0, true);
+}
+
+void Calculator::propose_lengths(const uint32_t *internals,
+				 const uint32_t *children, uint32_t n,
+				 const double *lengths, double clock_rate)
+{
+	DeviceGuard g(device_);
+	if (!model_set_)
+		throw Error(B3G_ERR_STATE,
+			    "no substitution model set before propose_lengths");
+	validate_lists(internals, children, n);
+	if (!lengths)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null lengths");
+	for (size_t k = 0; k < (size_t)n * 2; ++k)
+		if (!std::isfinite(lengths[k]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite edge length");
+	if (!std::isfinite(clock_rate))
+		throw Error(B3G_ERR_NUMERIC, "non-finite clock rate");
+	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	stage_ops(internals, children, n);
+	std::memcpy(h_stage_ + off_pi_, model_host_.pi, S_ * sizeof(double));
+	std::memcpy(h_stage_ + off_in_, lengths, (size_t)n * 2 * sizeof(double));
+	launch(n, false, clock_rate, false);
+}
+
+void Calculator::likelihoods(double *out)
+{
+	DeviceGuard g(device_);
+	if (!out)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+	if (!have_result_ || !cat_valid_)
+		throw Error(B3G_ERR_STATE,
+			    "likelihoods() needs a preceding propose()");
+	check_cuda(cudaMemcpy2DAsync(out, P_ * sizeof(double), d_cat_,
+				     ldp_ * sizeof(double), P_ * sizeof(double),
+				     C_, cudaMemcpyDeviceToHost, stream_),
+		   "read likelihoods");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+}
+
+double Calculator::log_likelihood()
+{
+	DeviceGuard g(device_);
+	if (!have_result_)
+		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	return *h_lnl_;
+}
+
+void Calculator::site_log_likelihoods(double *out)
+{
+	DeviceGuard g(device_);
+	if (!out)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+	if (!have_result_)
+		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
+	check_cuda(cudaMemcpyAsync(out, d_site_, P_ * sizeof(double),
+				   cudaMemcpyDeviceToHost, stream_),
+		   "read site lnl");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+}
+
+void Calculator::harvest(TimingSlot &s)
+{
+	check_cuda(cudaEventSynchronize(s.k1), "timing sync");
+	float t = 0.0f, p = 0.0f;
+	check_cuda(cudaEventElapsedTime(&t, s.k0, s.kmid), "elapsed");
+	check_cuda(cudaEventElapsedTime(&p, s.kmid, s.k1), "elapsed");
+	acc_transition_ms_ += t;
+	acc_prune_ms_ += p;
+	++acc_count_;
+	s.pending = false;
+}
+
+void Calculator::last_timing(float *transition_ms, float *prune_ms)
+{
+	DeviceGuard g(device_);
+	if (!have_result_ || ring_next_ == 0)
+		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
+	TimingSlot &s = ring_[(ring_next_ - 1) % kRing];
+	check_cuda(cudaEventSynchronize(s.k1), "sync");
+	check_cuda(cudaEventElapsedTime(transition_ms, s.k0, s.kmid), "elapsed");
+	check_cuda(cudaEventElapsedTime(prune_ms, s.kmid, s.k1), "elapsed");
+}
+
+void Calculator::timing_totals(bool reset, double *transition_ms,
+			       double *prune_ms, uint64_t *proposals)
+{
+	DeviceGuard g(device_);
+	// harvest in recording order
+	const uint64_t first = ring_next_ > kRing ? ring_next_ - kRing : 0;
+	for (uint64_t i = first; i < ring_next_; ++i) {
+		TimingSlot &s = ring_[i % kRing];
+		if (s.pending)
+			harvest(s);
+	}
+	*transition_ms = acc_transition_ms_;
+	*prune_ms = acc_prune_ms_;
+	*proposals = acc_count_;
+	if (reset) {
+		acc_transition_ms_ = acc_prune_ms_ = 0.0;
+		acc_count_ = 0;
+	}
+}
+
+void Calculator::span_begin()
+{
+	DeviceGuard g(device_);
+	check_cuda(cudaEventRecord(ev_span0_, stream_), "event");
+}
+
+float Calculator::span_end()
+{
+	DeviceGuard g(device_);
+	check_cuda(cudaEventRecord(ev_span1_, stream_), "event");
+	check_cuda(cudaEventSynchronize(ev_span1_), "sync");
+	float ms = 0.0f;
+	check_cuda(cudaEventElapsedTime(&ms, ev_span0_, ev_span1_), "elapsed");
+	return ms;
+}
+
+void Calculator::accept()
+{
+	// Cpu4Calculator::accept (cpu4.rs:78-83): EditBuf::accept
+	for (auto &m : selectors_)
+		m &= 1u;
+}
+
+void Calculator::reject()
+{
+	// Cpu4Calculator::reject (cpu4.rs:85-89): EditBuf::reject
+	for (auto &m : selectors_)
+		m = static_cast<uint8_t>((m ^ (m >> 1)) & 1u);
+}
+
+void Calculator::set_weights(const uint32_t *w)
+{
+	DeviceGuard g(device_);
+	if (!w)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null weights");
+	std::vector<uint32_t> padded(ldp_, 0);
+	std::memcpy(padded.data(), w, P_ * sizeof(uint32_t));
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	check_cuda(cudaMemcpy(d_weights_, padded.data(), ldp_ * sizeof(uint32_t),
+			      cudaMemcpyHostToDevice),
+		   "upload weights");
+}
+
+void Calculator::set_eigen(const double *V, const double *Vinv,
+			   const double *lambda, const double *Q,
+			   const double *pi, int shortcuts)
+{
+	DeviceGuard g(device_);
+	if (!V || !Vinv || !lambda || !Q || !pi)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null eigensystem");
+	const uint32_t nn = S_ * S_;
+	for (uint32_t k = 0; k < nn; ++k)
+		if (!std::isfinite(V[k]) || !std::isfinite(Vinv[k]) ||
+		    !std::isfinite(Q[k]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite eigensystem");
+	for (uint32_t k = 0; k < S_; ++k)
+		if (!std::isfinite(lambda[k]) || !std::isfinite(pi[k]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite eigensystem");
+	std::memcpy(model_host_.V, V, nn * sizeof(double));
+	std::memcpy(model_host_.Vinv, Vinv, nn * sizeof(double));
+	std::memcpy(model_host_.Q, Q, nn * sizeof(double));
+	std::memcpy(model_host_.lambda, lambda, S_ * sizeof(double));
+	std::memcpy(model_host_.pi, pi, S_ * sizeof(double));
+	model_host_.shortcuts = shortcuts ? 1u : 0u;
+	upload_model();
+	model_set_ = true;
+}
+
+void Calculator::set_reversible(const double *rates, const double *pi,
+				int shortcuts)
+{
+	DeviceGuard g(device_);
+	if (!rates || !pi)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null model");
+	const uint32_t nr = S_ * (S_ - 1) / 2;
+	double psum = 0.0;
+	for (uint32_t k = 0; k < nr; ++k)
+		if (!std::isfinite(rates[k]) || rates[k] < 0.0)
+			throw Error(B3G_ERR_NUMERIC,
+				    "exchangeabilities must be finite and >= 0");
+	for (uint32_t k = 0; k < S_; ++k) {
+		if (!std::isfinite(pi[k]) || !(pi[k] > 0.0))
+			throw Error(B3G_ERR_NUMERIC,
+				    "frequencies must be finite and > 0");
+		psum += pi[k];
+	}
+	(void)psum;
+	std::memcpy(model_host_.rates_in, rates, nr * sizeof(double));
+	std::memcpy(model_host_.pi_in, pi, S_ * sizeof(double));
+	std::memcpy(model_host_.pi, pi, S_ * sizeof(double));
+	model_host_.shortcuts = shortcuts ? 1u : 0u;
+	upload_model();
+	check_cuda(launch_eigen(d_model_, stream_), "eigen kernel");
+	// the host copy of the decomposition is not needed: the device keeps
+	// V, V^-1, lambda and Q; pi is mirrored for the root reduction
+	model_set_ = true;
+}
+
+void Calculator::set_category_rates(const double *rates)
+{
+	DeviceGuard g(device_);
+	if (!rates)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null rates");
+	for (uint32_t c = 0; c < C_; ++c)
+		if (!std::isfinite(rates[c]) || rates[c] < 0.0)
+			throw Error(B3G_ERR_NUMERIC, "bad category rate");
+	// the device model may hold a decomposition written by eigen_kernel;
+	// update only the category rates in place
+	std::memcpy(model_host_.cat_rates, rates, C_ * sizeof(double));
+	check_cuda(cudaEventSynchronize(ev_model_free_), "model staging");
+	std::memcpy(h_model_->cat_rates, rates, C_ * sizeof(double));
+	check_cuda(cudaMemcpyAsync(d_model_->cat_rates, h_model_->cat_rates,
+				   C_ * sizeof(double), cudaMemcpyHostToDevice,
+				   stream_),
+		   "upload category rates");
+	check_cuda(cudaEventRecord(ev_model_free_, stream_), "event");
+}
+
+void Calculator::set_gamma(double alpha)
+{
+	if (!std::isfinite(alpha) || !(alpha > 0.0))
+		throw Error(B3G_ERR_NUMERIC, "alpha must be finite and > 0");
+	std::vector<double> r(C_);
+	gamma_categories(alpha, static_cast<int>(C_), r.data());
+	set_category_rates(r.data());
+}
+
+} // namespace b3g
+
+// ===========================================================================
+// C ABI
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F> b3g_status guarded(F &&f)
+{
+	try {
+		f();
+		g_last_error.clear();
+		return B3G_OK;
+	} catch (const b3g::Error &e) {
+		g_last_error = e.what();
+		return e.status;
+	} catch (const std::bad_alloc &) {
+		g_last_error = "host allocation failed";
+		return B3G_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		g_last_error = e.what();
+		return B3G_ERR_STATE;
+	} catch (...) {
+		g_last_error = "unknown error";
+		return B3G_ERR_STATE;
+	}
+}
+
+b3g::Calculator *calc_of(b3g_calculator *c)
+{
+	if (!c)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null calculator");
+	return reinterpret_cast<b3g::Calculator *>(c);
+}
+
+} // namespace
+
+extern "C" {
+
+B3G_API const char *b3g_last_error(void) { return g_last_error.c_str(); }
+
+B3G_API const char *b3g_version(void) { return "b3g 0.1.0 sm_103a"; }
+
+B3G_API b3g_status b3g_calculator_create(const b3g_config *config,
+					 const uint8_t *samples,
+					 b3g_calculator **out)
+{
+	return guarded([&] {
+		if (!config || !out)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null argument");
+		*out = nullptr;
+		auto *c = new b3g::Calculator(*config, samples);
+		*out = reinterpret_cast<b3g_calculator *>(c);
+	});
+}
+
+B3G_API void b3g_calculator_destroy(b3g_calculator *calc)
+{
+	delete reinterpret_cast<b3g::Calculator *>(calc);
+}
+
+B3G_API uint32_t b3g_calculator_num_patterns(const b3g_calculator *calc)
+{
+	return calc ? reinterpret_cast<const b3g::Calculator *>(calc)->num_patterns()
+		    : 0u;
+}
+
+B3G_API b3g_status b3g_calculator_propose(b3g_calculator *calc,
+					  const uint32_t *internals,
+					  const uint32_t *children, uint32_t n,
+					  const double *matrices,
+					  const double *frequencies)
+{
+	return guarded([&] {
+		calc_of(calc)->propose_matrices(internals, children, n, matrices,
+						frequencies);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_likelihoods(b3g_calculator *calc,
+					      double *out)
+{
+	return guarded([&] { calc_of(calc)->likelihoods(out); });
+}
+
+B3G_API b3g_status b3g_calculator_accept(b3g_calculator *calc)
+{
+	return guarded([&] { calc_of(calc)->accept(); });
+}
+
+B3G_API b3g_status b3g_calculator_reject(b3g_calculator *calc)
+{
+	return guarded([&] { calc_of(calc)->reject(); });
+}
+
+B3G_API b3g_status b3g_calculator_set_weights(b3g_calculator *calc,
+					      const uint32_t *weights)
+{
+	return guarded([&] { calc_of(calc)->set_weights(weights); });
+}
+
+B3G_API b3g_status b3g_calculator_set_eigen(b3g_calculator *calc,
+					    const double *V,
+					    const double *Vinv,
+					    const double *lambda,
+					    const double *Q,
+					    const double *frequencies,
+					    int shortcuts)
+{
+	return guarded([&] {
+		calc_of(calc)->set_eigen(V, Vinv, lambda, Q, frequencies,
+					 shortcuts);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_set_reversible(b3g_calculator *calc,
+						 const double *rates,
+						 const double *frequencies,
+						 int shortcuts)
+{
+	return guarded([&] {
+		calc_of(calc)->set_reversible(rates, frequencies, shortcuts);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_set_category_rates(b3g_calculator *calc,
+						     const double *rates)
+{
+	return guarded([&] { calc_of(calc)->set_category_rates(rates); });
+}
+
+B3G_API b3g_status b3g_calculator_set_gamma(b3g_calculator *calc,
+					    double alpha)
+{
+	return guarded([&] { calc_of(calc)->set_gamma(alpha); });
+}
+
+B3G_API b3g_status b3g_calculator_propose_lengths(b3g_calculator *calc,
+						  const uint32_t *internals,
+						  const uint32_t *children,
+						  uint32_t n,
+						  const double *lengths,
+						  double clock_rate)
+{
+	return guarded([&] {
+		calc_of(calc)->propose_lengths(internals, children, n, lengths,
+					       clock_rate);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_log_likelihood(b3g_calculator *calc,
+						 double *out)
+{
+	return guarded([&] {
+		if (!out)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*out = calc_of(calc)->log_likelihood();
+	});
+}
+
+B3G_API b3g_status b3g_calculator_site_log_likelihoods(b3g_calculator *calc,
+						       double *out)
+{
+	return guarded([&] { calc_of(calc)->site_log_likelihoods(out); });
+}
+
+B3G_API b3g_status b3g_calculator_last_timing(b3g_calculator *calc,
+					      float *transition_ms,
+					      float *prune_ms)
+{
+	return guarded([&] {
+		if (!transition_ms || !prune_ms)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		calc_of(calc)->last_timing(transition_ms, prune_ms);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
+						int reset,
+						double *transition_ms,
+						double *prune_ms,
+						uint64_t *proposals)
+{
+	return guarded([&] {
+		if (!transition_ms || !prune_ms || !proposals)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		calc_of(calc)->timing_totals(reset != 0, transition_ms, prune_ms,
+					     proposals);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc)
+{
+	return guarded([&] { calc_of(calc)->span_begin(); });
+}
+
+B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms)
+{
+	return guarded([&] {
+		if (!ms)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*ms = calc_of(calc)->span_end();
+	});
+}
+
+} // extern "C"

@@ -1,0 +1,136 @@
+// calculator.hpp -- host side of one device-resident pruning store.
+//
+// Mirrors the reference's calculator life cycle (crates/b3/src/calculator/
+// mod.rs:33-76): propose -> likelihoods -> accept | reject.  The host keeps
+// only the EditBuf selectors (sk/src/editbuf.rs:8-105) and the staging
+// buffers; partials, scale counts, tips, weights, the model and every
+// per-step table live in HBM.  Accept and reject are selector flips: the
+// cumulative scale counts are per slot, so nothing is copied on the device.
+#pragma once
+
+#include "../../include/b3g.h"
+#include "b3g_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace b3g {
+
+struct Error : std::runtime_error {
+	b3g_status status;
+	Error(b3g_status s, const std::string &m)
+	    : std::runtime_error(m), status(s)
+	{
+	}
+};
+
+void check_cuda(cudaError_t e, const char *what);
+
+class Calculator {
+      public:
+	Calculator(const b3g_config &cfg, const uint8_t *samples);
+	~Calculator();
+	Calculator(const Calculator &) = delete;
+	Calculator &operator=(const Calculator &) = delete;
+
+	uint32_t num_patterns() const { return P_; }
+	uint32_t num_leaves() const { return L_; }
+	uint32_t num_categories() const { return C_; }
+	int device() const { return device_; }
+
+	// calculator level
+	void propose_matrices(const uint32_t *internals,
+			      const uint32_t *children, uint32_t n,
+			      const double *matrices, const double *freqs);
+	void likelihoods(double *out);
+	void accept();
+	void reject();
+
+	// likelihood level
+	void set_weights(const uint32_t *w);
+	void set_eigen(const double *V, const double *Vinv,
+		       const double *lambda, const double *Q,
+		       const double *pi, int shortcuts);
+	void set_reversible(const double *rates, const double *pi,
+			    int shortcuts);
+	void set_category_rates(const double *rates);
+	void set_gamma(double alpha);
+	void propose_lengths(const uint32_t *internals,
+			     const uint32_t *children, uint32_t n,
+			     const double *lengths, double clock_rate);
+	double log_likelihood();
+	void site_log_likelihoods(double *out);
+	void last_timing(float *transition_ms, float *prune_ms);
+	void timing_totals(bool reset, double *transition_ms, double *prune_ms,
+			   uint64_t *proposals);
+	void span_begin();
+	float span_end();
+
+      private:
+	void validate_lists(const uint32_t *internals,
+			    const uint32_t *children, uint32_t n);
+	void stage_ops(const uint32_t *internals, const uint32_t *children,
+		       uint32_t n);
+	void launch(uint32_t n, bool matrices_mode, double clock_rate,
+		    bool want_cat);
+	void upload_model();
+	void release();
+
+	// shape
+	uint32_t L_ = 0, I_ = 0, P_ = 0, ldp_ = 0, S_ = 0, C_ = 0, tile_ = 0;
+	bool f32_ = false;
+	uint32_t scale_ln_ = 0;
+	int device_ = -1;
+
+	// host state
+	std::vector<uint8_t> selectors_; // EditBuf over internals
+	std::vector<uint32_t> stamp_;    // list-position scratch per node
+	uint32_t stamp_epoch_ = 0;
+	bool model_set_ = false;
+	bool have_result_ = false;
+	bool cat_valid_ = false;
+	ModelDev model_host_{};
+
+	// stream and events
+	cudaStream_t stream_ = nullptr;
+	cudaEvent_t ev_stage_free_ = nullptr, ev_model_free_ = nullptr;
+	cudaEvent_t ev_span0_ = nullptr, ev_span1_ = nullptr;
+	// per-proposal timing ring: events before the transition kernel,
+	// between the kernels and after the pruning kernel
+	static constexpr uint32_t kRing = 64;
+	struct TimingSlot {
+		cudaEvent_t k0 = nullptr, kmid = nullptr, k1 = nullptr;
+		bool pending = false;
+	};
+	TimingSlot ring_[kRing];
+	uint64_t ring_next_ = 0;
+	double acc_transition_ms_ = 0.0, acc_prune_ms_ = 0.0;
+	uint64_t acc_count_ = 0;
+	void harvest(TimingSlot &s);
+
+	// device buffers
+	uint8_t *d_tips_ = nullptr;
+	void *d_partials_ = nullptr;
+	int32_t *d_scales_ = nullptr;
+	uint32_t *d_weights_ = nullptr;
+	double *d_site_ = nullptr;
+	double *d_cat_ = nullptr;
+	double *d_block_sums_ = nullptr;
+	unsigned *d_ticket_ = nullptr;
+	double *d_lnl_ = nullptr;
+	ModelDev *d_model_ = nullptr;
+	void *d_ptab_ = nullptr;
+	unsigned char *d_stage_ = nullptr;
+
+	// pinned host staging
+	unsigned char *h_stage_ = nullptr;
+	ModelDev *h_model_ = nullptr;
+	double *h_lnl_ = nullptr;
+	size_t stage_bytes_ = 0;
+	size_t off_pi_ = 0, off_in_ = 0;
+};
+
+} // namespace b3g

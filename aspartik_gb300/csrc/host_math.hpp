@@ -1,0 +1,12 @@
+// host_math.hpp -- host-side model arithmetic (Gamma rate categories).
+#pragma once
+
+namespace b3g {
+
+// Quantile of Gamma(shape a, scale 1) at probability p.
+double gamma_quantile(double a, double p);
+// Median-discretised category rates normalised to mean 1
+// (crates/b3/src/likelihood/gamma.rs:205-225).
+void gamma_categories(double alpha, int k, double *rates);
+
+} // namespace b3g

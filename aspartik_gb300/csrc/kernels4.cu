@@ -1,0 +1,494 @@
+// kernels4.cu -- sm_103a kernels of the 4-state (DNA) pruning likelihood.
+//
+//   ptab4_kernel   transition-matrix builder: P = V diag(exp(lambda d)) V^-1
+//                  per (dirty node, child side, rate category), written
+//                  transposed with a trailing row of ones so that both the
+//                  internal-child product (sum_k x_k PT[k]) and the tip
+//                  lookup (PT[code]) are one 4-vector access each.
+//   prune4_kernel  Felsenstein pruning over the children-first dirty list.
+//                  One thread owns one (pattern, category) column and walks
+//                  the whole list, so no inter-block synchronisation exists;
+//                  at the root the block mixes the categories, weights the
+//                  patterns and the last block to finish folds the block
+//                  sums with Neumaier compensation (no atomics on doubles,
+//                  deterministic order).
+//   eigen_kernel   FP64 symmetric Jacobi decomposition of a reversible Q.
+//
+// The arithmetic restates the reference's CPU pruner
+// (crates/b3/src/calculator/cpu4.rs:170-433): tip-tip nodes are products of
+// P rows at the tip codes (unknown -> 1.0), internal children are 4x4
+// matrix-vector products, and in the FP64 form a node whose four entries are
+// all below e^-scale_ln is multiplied by e^scale_ln and counted.  Instead of
+// the reference's per-pattern running sum, which is corrected by the flag of
+// the other buffer, every slot stores the count of its whole subtree, so the
+// root count is always exact, also when a proposal is evaluated twice.
+#include "b3g_device.cuh"
+
+#include <math.h>
+
+namespace b3g {
+namespace {
+
+// ---------------------------------------------------------------------------
+// 4-vectors: double4_32a (one 256-bit access) and float4 (one 128-bit access)
+
+struct V4d {
+	typedef double4_32a T;
+	typedef double R;
+};
+struct V4f {
+	typedef float4 T;
+	typedef float R;
+};
+
+template <typename T, typename R>
+__device__ __forceinline__ T v4_make(R x, R y, R z, R w)
+{
+	T r;
+	r.x = x;
+	r.y = y;
+	r.z = z;
+	r.w = w;
+	return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T v4_mul(const T &a, const T &b)
+{
+	T r;
+	r.x = a.x * b.x;
+	r.y = a.y * b.y;
+	r.z = a.z * b.z;
+	r.w = a.w * b.w;
+	return r;
+}
+
+// sum_k x_k * pt[k], accumulated in k order (the column order of
+// cpu4.rs:386-391).
+template <typename T>
+__device__ __forceinline__ T v4_apply(const T *__restrict__ pt, const T &x)
+{
+	const T p0 = pt[0], p1 = pt[1], p2 = pt[2], p3 = pt[3];
+	T r;
+	r.x = x.x * p0.x;
+	r.y = x.x * p0.y;
+	r.z = x.x * p0.z;
+	r.w = x.x * p0.w;
+	r.x = fma(x.y, p1.x, r.x);
+	r.y = fma(x.y, p1.y, r.y);
+	r.z = fma(x.y, p1.z, r.z);
+	r.w = fma(x.y, p1.w, r.w);
+	r.x = fma(x.z, p2.x, r.x);
+	r.y = fma(x.z, p2.y, r.y);
+	r.z = fma(x.z, p2.z, r.z);
+	r.w = fma(x.z, p2.w, r.w);
+	r.x = fma(x.w, p3.x, r.x);
+	r.y = fma(x.w, p3.y, r.y);
+	r.z = fma(x.w, p3.z, r.z);
+	r.w = fma(x.w, p3.w, r.w);
+	return r;
+}
+
+// FP64 form (cpu4.rs:403-433): rescale by e^scale_ln when all four entries
+// are below e^-scale_ln.  Returns the number of rescalings applied (0 or 1).
+__device__ __forceinline__ int32_t rescale_threshold(double4_32a &y,
+						     double thr, double mult)
+{
+	if (y.x < thr && y.y < thr && y.z < thr && y.w < thr) {
+		y.x *= mult;
+		y.y *= mult;
+		y.z *= mult;
+		y.w *= mult;
+		return 1;
+	}
+	return 0;
+}
+
+// FP32 form: divide by the power of two that brings the largest entry into
+// [1, 2).  The division is exact, so the exponent carries the scale without
+// rounding.  Returns that exponent.
+__device__ __forceinline__ int32_t rescale_pow2(float4 &y)
+{
+	float m = fmaxf(fmaxf(y.x, y.y), fmaxf(y.z, y.w));
+	int32_t shift = 0;
+	uint32_t ex = (__float_as_uint(m) >> 23) & 0xffu;
+	if (ex == 0u) {
+		if (!(m > 0.0f))
+			return 0; // all zero: the pattern is impossible
+		// subnormal maximum: lift by 2^64 first (exact)
+		const float lift = 18446744073709551616.0f;
+		y.x *= lift;
+		y.y *= lift;
+		y.z *= lift;
+		y.w *= lift;
+		shift = -64;
+		m = fmaxf(fmaxf(y.x, y.y), fmaxf(y.z, y.w));
+		ex = (__float_as_uint(m) >> 23) & 0xffu;
+	}
+	const int32_t e = (int32_t)ex - 127;
+	const float f = __uint_as_float((uint32_t)(127 - e) << 23); // 2^-e
+	y.x *= f;
+	y.y *= f;
+	y.z *= f;
+	y.w *= f;
+	return e + shift;
+}
+
+// ---------------------------------------------------------------------------
+// transition matrices
+
+__device__ void transition4(const ModelDev *__restrict__ m, double d,
+			    double P[16])
+{
+	if (m->shortcuts && d > 20.0) {
+		// transition_freqs (substitution.rs:245-252)
+		for (int i = 0; i < 4; i++)
+			for (int j = 0; j < 4; j++)
+				P[i * 4 + j] = m->pi[j];
+		return;
+	}
+	if (m->shortcuts && d < 1e-10) {
+		// transition_q (substitution.rs:258-268): I + Q d, unit diagonal
+		for (int i = 0; i < 4; i++)
+			for (int j = 0; j < 4; j++)
+				P[i * 4 + j] = i == j ? 1.0 : m->Q[i * 4 + j] * d;
+		return;
+	}
+	double e[4];
+	for (int k = 0; k < 4; k++)
+		e[k] = exp(m->lambda[k] * d);
+	for (int i = 0; i < 4; i++) {
+		double t0 = m->V[i * 4 + 0] * e[0], t1 = m->V[i * 4 + 1] * e[1];
+		double t2 = m->V[i * 4 + 2] * e[2], t3 = m->V[i * 4 + 3] * e[3];
+		for (int j = 0; j < 4; j++) {
+			double s = t0 * m->Vinv[0 * 4 + j];
+			s = fma(t1, m->Vinv[1 * 4 + j], s);
+			s = fma(t2, m->Vinv[2 * 4 + j], s);
+			s = fma(t3, m->Vinv[3 * 4 + j], s);
+			P[i * 4 + j] = s;
+		}
+	}
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) ptab4_kernel(PtabParams prm)
+{
+	const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+	if (id >= prm.n * 2u * prm.C)
+		return;
+	const uint32_t c = id % prm.C;
+	const uint32_t es = id / prm.C; // dirty index * 2 + side
+	double P[16];
+	if (prm.matrices) {
+		const double *src = prm.matrices + (size_t)id * 16;
+		for (int k = 0; k < 16; k++)
+			P[k] = src[k];
+	} else {
+		const double d = prm.lengths[es] *
+				 (prm.clock_rate * prm.model->cat_rates[c]);
+		transition4(prm.model, d, P);
+	}
+	R *out = (R *)prm.ptab + (size_t)id * 20;
+	for (int k = 0; k < 4; k++)
+		for (int j = 0; j < 4; j++)
+			out[k * 4 + j] = (R)P[j * 4 + k];
+	for (int j = 0; j < 4; j++)
+		out[16 + j] = (R)1.0;
+}
+
+// ---------------------------------------------------------------------------
+// pruning
+
+__device__ __forceinline__ void neumaier_add(double &sum, double &comp,
+					     double x)
+{
+	const double t = sum + x;
+	if (fabs(sum) >= fabs(x))
+		comp += (sum - t) + x;
+	else
+		comp += (x - t) + sum;
+	sum = t;
+}
+
+template <typename VT, bool kPow2>
+__global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
+{
+	typedef typename VT::T T;
+	typedef typename VT::R R;
+	const uint32_t tp = blockDim.x;
+	const uint32_t c = threadIdx.y;
+	const uint32_t p = blockIdx.x * tp + threadIdx.x;
+	const uint32_t ldp = prm.ldp, C = prm.C;
+	T *__restrict__ partials = (T *)prm.partials;
+	int32_t *__restrict__ scales = prm.scales;
+	const T *__restrict__ ptab = (const T *)prm.ptab;
+
+	T y = v4_make<T, R>(0, 0, 0, 0);
+	int32_t cnt = 0;
+	for (uint32_t i = 0; i < prm.n; ++i) {
+		const NodeOp op = prm.ops[i];
+		const T *tl = ptab + ((size_t)(2 * i) * C + c) * 5;
+		const T *tr = ptab + ((size_t)(2 * i + 1) * C + c) * 5;
+		T a, b;
+		int32_t ca = 0, cb = 0;
+		if (op.left & kTipBit) {
+			const uint32_t code =
+				prm.tips[(size_t)(op.left & ~kTipBit) * ldp + p];
+			a = tl[code];
+		} else {
+			const size_t ix = ((size_t)op.left * C + c) * ldp + p;
+			a = v4_apply(tl, partials[ix]);
+			ca = scales[ix];
+		}
+		if (op.right & kTipBit) {
+			const uint32_t code =
+				prm.tips[(size_t)(op.right & ~kTipBit) * ldp + p];
+			b = tr[code];
+		} else {
+			const size_t ix = ((size_t)op.right * C + c) * ldp + p;
+			b = v4_apply(tr, partials[ix]);
+			cb = scales[ix];
+		}
+		y = v4_mul(a, b);
+		int32_t own;
+		if constexpr (kPow2) {
+			own = rescale_pow2(y);
+		} else {
+			// tip-tip nodes are never rescaled (cpu4.rs:288-318)
+			own = ((op.left & op.right) & kTipBit)
+				      ? 0
+				      : rescale_threshold(y, prm.scale_threshold,
+							  prm.scale_mult);
+		}
+		cnt = ca + cb + own;
+		const size_t ox = ((size_t)op.out * C + c) * ldp + p;
+		partials[ox] = y;
+		scales[ox] = cnt;
+	}
+
+	// ---- root: category mixing, pattern weights, block sum ------------
+	extern __shared__ double smem[];
+	double *s_val = smem;                            // [C][tp]
+	int32_t *s_exp = (int32_t *)(smem + C * tp);     // [C][tp]
+	double *s_warp = smem + C * tp + (C * tp + 1) / 2; // [8]
+	__shared__ unsigned s_last;
+
+	const double root_dot = (double)prm.pi[0] * (double)y.x +
+				(double)prm.pi[1] * (double)y.y +
+				(double)prm.pi[2] * (double)y.z +
+				(double)prm.pi[3] * (double)y.w;
+	if constexpr (kPow2) {
+		s_val[c * tp + threadIdx.x] = root_dot;
+		s_exp[c * tp + threadIdx.x] = cnt;
+		if (prm.cat_lnl)
+			prm.cat_lnl[(size_t)c * ldp + p] =
+				log(root_dot) + (double)cnt * 0.69314718055994530942;
+	} else {
+		// cpu4.rs:277-284 and :63-68; the count times scale_ln is an
+		// unsigned 32-bit product as in the reference
+		const double lcat =
+			log(root_dot) - (double)((uint32_t)cnt * prm.scale_ln);
+		s_val[c * tp + threadIdx.x] = lcat;
+		if (prm.cat_lnl)
+			prm.cat_lnl[(size_t)c * ldp + p] = lcat;
+	}
+	__syncthreads();
+
+	double contrib = 0.0;
+	if (c == 0) {
+		double site;
+		if constexpr (kPow2) {
+			// sum_c s_c 2^E_c = 2^Emax sum_c s_c 2^(E_c - Emax)
+			int32_t emax = INT32_MIN;
+			for (uint32_t k = 0; k < C; k++)
+				if (s_val[k * tp + threadIdx.x] > 0.0)
+					emax = max(emax, s_exp[k * tp + threadIdx.x]);
+			if (emax == INT32_MIN) {
+				site = -INFINITY;
+			} else {
+				double acc = 0.0;
+				for (uint32_t k = 0; k < C; k++)
+					acc += scalbn(s_val[k * tp + threadIdx.x],
+						      s_exp[k * tp + threadIdx.x] - emax);
+				site = log(acc) +
+				       (double)emax * 0.69314718055994530942 +
+				       prm.log_inv_c;
+			}
+		} else {
+			// log_sum_exp (likelihood/mod.rs:141-151) + ln(1/C)
+			// (gamma.rs:155-165); exact identity for C = 1
+			double mx = -INFINITY;
+			for (uint32_t k = 0; k < C; k++)
+				mx = fmax(mx, s_val[k * tp + threadIdx.x]);
+			if (mx == -INFINITY) {
+				site = -INFINITY;
+			} else {
+				double se = 0.0;
+				for (uint32_t k = 0; k < C; k++)
+					se += exp(s_val[k * tp + threadIdx.x] - mx);
+				site = mx + log(se) + prm.log_inv_c;
+			}
+		}
+		prm.site_lnl[p] = site;
+		const uint32_t w = prm.weights[p];
+		contrib = w ? site * (double)w : 0.0;
+	}
+
+	// block sum over the category-0 threads (warps 0 .. tp/32-1), in a
+	// fixed order
+	const uint32_t tid = threadIdx.y * tp + threadIdx.x;
+	const uint32_t lane = tid & 31u, warp = tid >> 5;
+	for (int off = 16; off > 0; off >>= 1)
+		contrib += __shfl_down_sync(0xffffffffu, contrib, off);
+	if (c == 0 && lane == 0)
+		s_warp[warp] = contrib;
+	__syncthreads();
+	if (tid == 0) {
+		double bsum = 0.0;
+		for (uint32_t w = 0; w < tp / 32u; w++)
+			bsum += s_warp[w];
+		prm.block_sums[blockIdx.x] = bsum;
+		__threadfence();
+		const unsigned t = atomicAdd(prm.ticket, 1u);
+		s_last = (t == gridDim.x - 1u);
+	}
+	__syncthreads();
+	if (s_last && tid == 0) {
+		__threadfence();
+		double sum = 0.0, comp = 0.0;
+		for (uint32_t bix = 0; bix < gridDim.x; bix++)
+			neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
+		*prm.lnl_out = sum + comp;
+		*prm.ticket = 0u;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// eigensystem of a reversible Q (FP64, one thread; run when the model
+// changes, not per step).  Cyclic Jacobi (Golub & Van Loan, Matrix
+// Computations, sec. 8.5) on B = D^1/2 Q D^-1/2, D = diag(pi).
+
+__global__ void eigen_kernel(ModelDev *m)
+{
+	if (threadIdx.x != 0 || blockIdx.x != 0)
+		return;
+	const int n = (int)m->states;
+	double Q[kMaxStates * kMaxStates];
+	double B[kMaxStates * kMaxStates];
+	double U[kMaxStates * kMaxStates];
+	double sq[kMaxStates];
+	int k = 0;
+	for (int i = 0; i < n; i++)
+		Q[i * n + i] = 0.0;
+	for (int i = 0; i < n; i++)
+		for (int j = i + 1; j < n; j++, k++) {
+			Q[i * n + j] = m->rates_in[k] * m->pi_in[j];
+			Q[j * n + i] = m->rates_in[k] * m->pi_in[i];
+		}
+	double scale = 0.0;
+	for (int i = 0; i < n; i++) {
+		double s = 0.0;
+		for (int j = 0; j < n; j++)
+			if (j != i)
+				s += Q[i * n + j];
+		Q[i * n + i] = -s;
+		scale += s * m->pi_in[i];
+	}
+	for (int i = 0; i < n * n; i++)
+		Q[i] /= scale;
+	for (int i = 0; i < n; i++)
+		sq[i] = sqrt(m->pi_in[i]);
+	for (int i = 0; i < n; i++)
+		for (int j = 0; j < n; j++) {
+			const double bij = Q[i * n + j] * sq[i] / sq[j];
+			const double bji = Q[j * n + i] * sq[j] / sq[i];
+			B[i * n + j] = 0.5 * (bij + bji);
+			U[i * n + j] = i == j ? 1.0 : 0.0;
+		}
+	int sweep;
+	for (sweep = 0; sweep < 64; sweep++) {
+		double off = 0.0, tot = 0.0;
+		for (int i = 0; i < n * n; i++) {
+			tot += B[i] * B[i];
+			if (i / n != i % n)
+				off += B[i] * B[i];
+		}
+		if (off <= 1e-34 * tot)
+			break;
+		for (int p = 0; p < n - 1; p++)
+			for (int q = p + 1; q < n; q++) {
+				const double apq = B[p * n + q];
+				if (apq == 0.0)
+					continue;
+				const double theta =
+					(B[q * n + q] - B[p * n + p]) / (2.0 * apq);
+				const double t =
+					(theta >= 0.0 ? 1.0 : -1.0) /
+					(fabs(theta) + sqrt(theta * theta + 1.0));
+				const double cs = 1.0 / sqrt(t * t + 1.0);
+				const double sn = t * cs;
+				for (int r = 0; r < n; r++) {
+					const double bp = B[r * n + p], bq = B[r * n + q];
+					B[r * n + p] = cs * bp - sn * bq;
+					B[r * n + q] = sn * bp + cs * bq;
+				}
+				for (int r = 0; r < n; r++) {
+					const double bp = B[p * n + r], bq = B[q * n + r];
+					B[p * n + r] = cs * bp - sn * bq;
+					B[q * n + r] = sn * bp + cs * bq;
+				}
+				for (int r = 0; r < n; r++) {
+					const double up = U[r * n + p], uq = U[r * n + q];
+					U[r * n + p] = cs * up - sn * uq;
+					U[r * n + q] = sn * up + cs * uq;
+				}
+			}
+	}
+	for (int i = 0; i < n; i++) {
+		m->lambda[i] = B[i * n + i];
+		m->pi[i] = m->pi_in[i];
+		for (int j = 0; j < n; j++) {
+			m->V[i * n + j] = U[i * n + j] / sq[i];
+			m->Vinv[j * n + i] = U[i * n + j] * sq[i];
+			m->Q[i * n + j] = Q[i * n + j];
+		}
+	}
+	m->jacobi_sweeps = (uint32_t)sweep;
+	m->status = sweep < 64 ? 0u : 1u;
+}
+
+} // namespace
+
+cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
+{
+	const uint32_t total = p.n * 2u * p.C;
+	if (total == 0)
+		return cudaSuccess;
+	const uint32_t blocks = (total + 127u) / 128u;
+	if (f32)
+		ptab4_kernel<float><<<blocks, 128, 0, s>>>(p);
+	else
+		ptab4_kernel<double><<<blocks, 128, 0, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
+			  cudaStream_t s)
+{
+	const dim3 block(tile, p.C);
+	const dim3 grid(p.ldp / tile);
+	const size_t smem = sizeof(double) * (p.C * tile + (p.C * tile + 1) / 2 + 8);
+	if (f32)
+		prune4_kernel<V4f, true><<<grid, block, smem, s>>>(p);
+	else
+		prune4_kernel<V4d, false><<<grid, block, smem, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_eigen(ModelDev *model, cudaStream_t s)
+{
+	eigen_kernel<<<1, 32, 0, s>>>(model);
+	return cudaGetLastError();
+}
+
+} // namespace b3g

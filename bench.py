@@ -1,0 +1,428 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 pruning likelihood.
+
+One step = one whole-tree evaluation of the b3 pruning likelihood (every
+internal dirty, as after ``mark_all_edges_updated``) on a synthetic workload
+with the shape of the largest configuration: 256 taxa, 20,000 DNA sites
+simulated under GTR + Gamma4 (exchangeabilities ~ Gamma(2,1), frequencies ~
+Dirichlet(5,5,5,5), alpha 0.5) on a Yule tree of root height 1.0, in the
+chosen form (FP32 partials, power-of-two rescaling, FP64 site sum).
+
+Metric: pruning GB/s = algorithmic bytes of one evaluation (a closed formula
+over the dirty list, see aspartik_gb300/schedule.py) / time.
+  value     K back-to-back evaluations, device time between CUDA events on
+            the calculator's stream; the alignment, partials and model are
+            resident; each step still uploads its dirty list and lengths.
+  e2e       the same steps through the public C ABI with host buffers: every
+            step copies its dirty list and edge lengths host->device, runs,
+            and reads the log-likelihood back (blocking), host-timed.
+  roofline  the pruning kernel alone (per-launch CUDA events) against the
+            measured HBM copy bandwidth.
+
+``--impl reference`` times the reference's CPU pruner (the C restatement of
+crates/b3/src/calculator/cpu4.rs, all host threads) on the same workload and
+prints the same metric computed with the same byte count, so the ratio of the
+two arms is the ratio of evaluations per second.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from aspartik_gb300 import schedule, sim  # noqa: E402
+
+METRIC = "pruning GB/s (whole-tree evaluation, chosen FP32 form)"
+UNIT = "GB/s"
+
+WORKLOADS = {
+    # largest configuration: 256 taxa, 20,000 sites, GTR + Gamma4
+    "dna256x20000_gtr_g4": dict(taxa=256, sites=20000, model="gtr", alpha=0.5, categories=4,
+                                root_height=1.0, pi_conc=5.0),
+    # 64 taxa, 10,000 sites, GTR + Gamma4
+    "dna64x10000_gtr_g4": dict(taxa=64, sites=10000, model="gtr", alpha=0.5, categories=4,
+                               root_height=1.0, pi_conc=5.0),
+    # 16 taxa, 1,000 sites, HKY(kappa 2), one category
+    "dna16x1000_hky": dict(taxa=16, sites=1000, model="hky", alpha=None, categories=1,
+                           root_height=0.5, pi_conc=10.0),
+}
+DEFAULT_WORKLOAD = "dna256x20000_gtr_g4"
+
+
+def make_workload(name: str, seed: int = 4) -> dict:
+    spec = WORKLOADS[name]
+    rng = np.random.default_rng(seed)
+    tree = sim.yule_tree(spec["taxa"], rng, root_height=spec["root_height"])
+    pi = sim.dirichlet([spec["pi_conc"]] * 4, rng)
+    rates = sim.hky_rates(2.0) if spec["model"] == "hky" else rng.gamma(2.0, 1.0, size=6)
+    Q = sim.reversible_q(rates, pi)
+    K = spec["categories"]
+    cats = sim.gamma_rates(spec["alpha"], K) if spec["alpha"] else np.ones(1)
+    states = sim.simulate_alignment(tree, spec["sites"], Q, pi, rng, cat_rates=cats)
+    leaves, weights, _ = sim.deduplicate(sim.to_dna_codes(states))
+    return dict(spec=spec, tree=tree, pi=pi, rates=rates, cats=cats, leaves=leaves,
+                weights=weights, top=schedule.Topology(tree.parents, tree.heights))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def stage_bytes(num_internals: int, n: int, states: int = 4) -> int:
+    """Bytes the library copies host->device per step (its staged dirty
+    list, frequencies and lengths; calculator.cu)."""
+    def up(x, a):
+        return (x + a - 1) // a * a
+
+    off_pi = up(num_internals * 16, 256)
+    off_in = up(off_pi + states * 8, 256)
+    return off_in + n * 2 * 8
+
+
+def make_calc(wl, precision: str, device: int):
+    from aspartik_gb300.calculator import Calculator
+
+    K = wl["spec"]["categories"]
+    calc = Calculator.GB300(device, precision).make4(wl["leaves"], wl["leaves"].shape[1],
+                                                     num_categories=K)
+    calc.set_weights(wl["weights"])
+    calc.set_reversible(wl["rates"], wl["pi"])
+    if wl["spec"]["alpha"]:
+        calc.set_gamma(wl["spec"]["alpha"])
+    return calc
+
+
+def device_throughput(calc, lists, steps, warmup, world):
+    internals, children, lengths = lists
+    for _ in range(warmup):
+        calc.propose_lengths(internals, children, lengths, 1.0)
+    calc.log_likelihood()
+    calc.timing_totals(reset=True)
+    barrier(world)
+    calc.span_begin()
+    for _ in range(steps):
+        calc.propose_lengths(internals, children, lengths, 1.0)
+    ms = calc.span_end()
+    barrier(world)
+    tt, tp, n = calc.timing_totals(reset=True)
+    return ms, tt / max(n, 1), tp / max(n, 1), n
+
+
+def cpu_oracle_eval(wl, num_threads: int, pattern_limit: int | None = None):
+    """One whole-tree evaluation on the CPU oracle (restated cpu4, one
+    calculator per category as GammaLikelihood runs them).  Returns
+    (seconds, patterns used, threads)."""
+    from oracle import oracle as O
+
+    leaves = wl["leaves"]
+    weights = wl["weights"]
+    if pattern_limit is not None and pattern_limit < leaves.shape[1]:
+        leaves = np.ascontiguousarray(leaves[:, :pattern_limit])
+        weights = weights[:pattern_limit]
+    P = leaves.shape[1]
+    top = wl["top"]
+    internals, children, lengths = top.full()
+    model = O.gtr(wl["rates"], wl["pi"])
+    cats = O.gamma_categories(wl["spec"]["alpha"], wl["spec"]["categories"]) \
+        if wl["spec"]["alpha"] else np.ones(1)
+    mats = [np.stack([model.transition(d * r) for d in lengths.reshape(-1)]) for r in cats]
+    calcs = [O.Cpu4Calculator(leaves, P, 30, num_threads) for _ in cats]
+    t0 = time.perf_counter()
+    per = []
+    for calc, m in zip(calcs, mats):
+        calc.propose(internals, children, m, wl["pi"])
+        per.append(calc.likelihoods())
+    per = np.array(per)
+    mx = per.max(axis=0)
+    site = mx + np.log(np.exp(per - mx).sum(axis=0)) + np.log(1.0 / len(cats))
+    lnl = float(site @ weights.astype(np.float64))
+    dt = time.perf_counter() - t0
+    return dt, P, calcs[0].num_threads(), lnl
+
+
+def run_ours(args):
+    world, rank, local = dist_setup()
+    device = local
+    wl = make_workload(args.workload)
+    spec = wl["spec"]
+    top = wl["top"]
+    P = int(wl["leaves"].shape[1])
+    C = spec["categories"]
+    full = top.full()
+    I = top.L - 1
+    B32 = schedule.algorithmic_bytes(top, full[0], P, C, 4, w=4, e_b=4, w_p=4)
+    B64 = schedule.algorithmic_bytes(top, full[0], P, C, 4, w=8, e_b=4, w_p=8)
+    pk = peaks()
+
+    calc = make_calc(wl, "f32", device)
+    clocks = ClockSampler(device)
+    clocks.start()
+    time.sleep(0.3)
+    ms, t_tr, t_pr, nlaunch = device_throughput(calc, full, args.steps, args.warmup, world)
+    clk = clocks.stop()
+    ms_max = allreduce_max(ms, world)
+    value = world * args.steps * B32 / (ms_max * 1e-3) / 1e9
+    achieved = B32 / (t_pr * 1e-3) / 1e9
+
+    # e2e: host buffers in, log-likelihood out, blocking every step
+    internals, children, lengths = full
+    barrier(world)
+    t0 = time.perf_counter()
+    lnl = None
+    for _ in range(args.steps):
+        calc.propose_lengths(internals, children, lengths, 1.0)
+        lnl = calc.log_likelihood()
+    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+    e2e = world * args.steps * B32 / e2e_s / 1e9
+
+    # dirty path: height change of a random internal node
+    rng = np.random.default_rng(7)
+    nodes = rng.integers(top.L, 2 * top.L - 1, size=min(args.steps, 512))
+    paths = [top.path(int(v)) for v in nodes]
+    for p in paths[:args.warmup]:
+        calc.propose_lengths(*p, 1.0)
+    calc.log_likelihood()
+    calc.timing_totals(reset=True)
+    calc.span_begin()
+    for p in paths:
+        calc.propose_lengths(*p, 1.0)
+    dms = calc.span_end()
+    _, dprune, dn = calc.timing_totals(reset=True)
+    dbytes = sum(schedule.algorithmic_bytes(top, p[0], P, C, 4, w=4, e_b=4, w_p=4) for p in paths)
+    mean_path = float(np.mean([len(p[0]) for p in paths]))
+    calc.close()
+
+    # plain FP64 form, same workload
+    c64 = make_calc(wl, "f64", device)
+    k64 = max(3, min(args.steps, 200))
+    ms64, _, pr64, _ = device_throughput(c64, full, k64, args.warmup, world)
+    lnl64 = c64.log_likelihood()
+    c64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        dt1, Pu, thr, cpu_lnl = cpu_oracle_eval(wl, cores)
+        reps = int(max(1, min(20, 5.0 / max(dt1, 1e-3))))
+        times = [cpu_oracle_eval(wl, cores)[0] for _ in range(reps)]
+        t_cpu = statistics.median(times)
+        cpu = {"value": round(B32 / t_cpu / 1e9, 4), "unit": UNIT, "cores": thr,
+               "kind": "port",
+               "sample": f"{reps} whole-tree evaluations of the full workload ({Pu} patterns x "
+                         f"{C} categories), median {t_cpu * 1e3:.1f} ms each; restated cpu4 "
+                         f"(FP64, e^30 rescaling), one calculator per category, {thr} threads",
+               "ms_per_eval": round(t_cpu * 1e3, 3),
+               "lnl_rel_err_vs_gpu_f64": abs(cpu_lnl - lnl64) / abs(cpu_lnl)}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_max / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Yule tree + GTR+Gamma4 simulated alignment, seed 4)",
+        "config": {"workload": args.workload, "taxa": spec["taxa"], "sites": spec["sites"],
+                   "patterns": P, "categories": C, "states": 4,
+                   "evaluation": "whole tree (all internals dirty)",
+                   "bytes_per_step": B32,
+                   "l2": "inputs larger than L2 (FP32 partials %.2f GB)"
+                         % (2 * I * C * P * 16 / 1e9),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                     "traffic": None, "peak_source": pk["source"],
+                     "kernel": "prune4_kernel<float4, pow2>",
+                     "kernel_ms": round(t_pr, 5), "transition_kernel_ms": round(t_tr, 5)},
+        "e2e": {"value": round(e2e, 2), "unit": UNIT,
+                "h2d_bytes_per_step": stage_bytes(I, len(full[0])),
+                "d2h_bytes_per_step": 8, "ms_per_step": round(e2e_s * 1e3 / args.steps, 5)},
+        "gpu_launches": int(nlaunch * 2),
+        "clocks": clk,
+        "lnl": lnl,
+        "plain_f64": {"value": round(k64 * B64 / (ms64 * 1e-3) / 1e9, 2),
+                      "ms_per_step": round(ms64 / k64, 5),
+                      "kernel_ms": round(pr64, 5), "bytes_per_step": B64,
+                      "lnl": lnl64, "f32_rel_err": abs(lnl - lnl64) / abs(lnl64)},
+        "dirty_path": {"value": round(dbytes / (dms * 1e-3) / 1e9, 2),
+                       "us_per_eval": round(dms * 1e3 / len(paths), 3),
+                       "mean_nodes": mean_path,
+                       "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    wl = make_workload(args.workload)
+    spec = wl["spec"]
+    top = wl["top"]
+    P = int(wl["leaves"].shape[1])
+    C = spec["categories"]
+    full = top.full()
+    cores = os.cpu_count() or 1
+    # bound the run: size each step's pattern sample so that warmup + steps
+    # take about a minute at most
+    dt1, _, thr, _ = cpu_oracle_eval(wl, cores)
+    budget = 60.0
+    frac = min(1.0, budget / max(dt1 * (args.steps + args.warmup), 1e-9))
+    Pu = max(128, int(P * frac)) if frac < 1.0 else P
+    for _ in range(args.warmup):
+        cpu_oracle_eval(wl, cores, Pu)
+    total = 0.0
+    for _ in range(args.steps):
+        total += cpu_oracle_eval(wl, cores, Pu)[0]
+    B = schedule.algorithmic_bytes(top, full[0], Pu, C, 4, w=4, e_b=4, w_p=4)
+    value = args.steps * B / total / 1e9
+    sample = (f"whole-tree evaluations over {Pu} of {P} patterns x {C} categories per step; "
+              f"restated cpu4 (FP64, e^30 rescaling), {thr} threads")
+    print(json.dumps({
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total * 1e3 / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded Yule tree + GTR+Gamma4 simulated alignment, seed 4)",
+        "config": {"workload": args.workload, "taxa": spec["taxa"], "sites": spec["sites"],
+                   "patterns": P, "categories": C, "sampled_patterns": Pu,
+                   "bytes_per_step": B,
+                   "note": "reference Rust workspace not buildable here; its CPU pruner "
+                           "restated in C (oracle/b3oracle.c)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": thr, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,198 @@
+/*
+ * b3g.h -- C ABI of the GB300 (sm_103a) Felsenstein-pruning likelihood.
+ *
+ * The library replaces the likelihood path of the b3 MCMC engine of
+ * kaathewisegit/aspartik (crate b3).  Two levels are exported:
+ *
+ *  1. Calculator level -- a drop-in for `trait Calculator<f64>`
+ *     (crates/b3/src/calculator/mod.rs:54-76) as built by
+ *     `CalculatorConfig::make4` (mod.rs:159-200).  The caller passes exactly
+ *     what the reference's calculators consume: the children-first dirty list
+ *     from `DatedTree::partials_lists` (parameters/tree.rs:456-461), the child
+ *     transition matrices gathered by `Transitions::write_matrices`
+ *     (transitions.rs:62-72) and the base frequencies.
+ *
+ *  2. Likelihood level -- a drop-in for the body of
+ *     `DnaLikelihood::likelihood` / `GammaLikelihood::likelihood`
+ *     (likelihood/dna.rs:68-100, likelihood/gamma.rs:97-169).  The caller
+ *     passes the dirty list and the time lengths of the child edges; the
+ *     device builds P(t) = V diag(exp(lambda r t)) V^-1 for every category,
+ *     prunes, rescales, mixes the rate categories and returns the weighted
+ *     root log-likelihood as one double.
+ *
+ * Conventions: every call returns a b3g_status; no exception crosses the ABI;
+ * b3g_last_error() gives the message of the calling thread's last failure.
+ * A handle belongs to one host thread at a time.  Device pointers are never
+ * exposed.  Node ids follow the reference: leaves 0..L-1, internals L..2L-2,
+ * edge id = child node id (tree.rs:728-736).  Matrices are row-major with
+ * P[i][j] = Prob(i -> j).
+ */
+#ifndef B3G_H
+#define B3G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define B3G_API __attribute__((visibility("default")))
+#else
+#define B3G_API
+#endif
+
+typedef enum b3g_status {
+	B3G_OK = 0,
+	B3G_ERR_INVALID_ARGUMENT = 1, /* bad size, index or order */
+	B3G_ERR_OUT_OF_MEMORY = 2,    /* device or pinned host allocation */
+	B3G_ERR_CUDA = 3,             /* CUDA runtime error */
+	B3G_ERR_TIMEOUT = 4,          /* a bounded device wait gave up */
+	B3G_ERR_NUMERIC = 5,          /* NaN/inf in a model input */
+	B3G_ERR_STATE = 6             /* call out of order */
+} b3g_status;
+
+/* Arithmetic of the partial likelihoods. */
+enum {
+	/* Plain form: FP64 partials with the reference's e^scale_ln rescaling
+	 * (calculator/cpu4.rs:403-433). */
+	B3G_PRECISION_F64 = 0,
+	/* Chosen form: FP32 partials renormalised by an exact power of two at
+	 * every node, integer exponents per (node, pattern, category), FP64
+	 * log-scale bookkeeping and a compensated FP64 site sum. */
+	B3G_PRECISION_F32 = 1
+};
+
+typedef struct b3g_config {
+	uint32_t num_leaves;     /* L >= 2 */
+	uint32_t num_patterns;   /* P >= 1, site patterns after deduplication */
+	uint32_t num_states;     /* 4 (DNA) */
+	uint32_t num_categories; /* C in 1..16 rate categories */
+	uint32_t precision;      /* B3G_PRECISION_* */
+	uint32_t scale_ln;       /* FP64 form: rescale threshold e^-scale_ln;
+				    the reference default is 30
+				    (calculator/mod.rs:103-110) */
+	int32_t device;          /* CUDA device ordinal */
+	uint32_t reserved;       /* must be 0 */
+} b3g_config;
+
+typedef struct b3g_calculator b3g_calculator;
+typedef struct b3g_batch b3g_batch;
+
+/* Message of the calling thread's last failed call ("" if none). */
+B3G_API const char *b3g_last_error(void);
+/* Library version string. */
+B3G_API const char *b3g_version(void);
+
+/* ---- construction ------------------------------------------------------
+ * Replaces CalculatorConfig::make4 (calculator/mod.rs:159-200) and
+ * Cpu4Calculator::new / CudaPartialsCalculator::new (cpu4.rs:108-165,
+ * cuda_partials/mod.rs:171-284).  `samples` is the leaf-major
+ * [num_leaves][num_patterns] array of 4-bit IUPAC codes that `deduplicate`
+ * produces (likelihood/mod.rs:74-132); single bases map to states 0..3 and
+ * every other code to "unknown" (cpu4.rs:117-124).  Partials start zeroed. */
+B3G_API b3g_status b3g_calculator_create(const b3g_config *config,
+					 const uint8_t *samples,
+					 b3g_calculator **out);
+B3G_API void b3g_calculator_destroy(b3g_calculator *calc);
+B3G_API uint32_t b3g_calculator_num_patterns(const b3g_calculator *calc);
+
+/* ---- calculator level (trait Calculator<f64>) ---------------------------
+ * Replaces Calculator::propose (cpu4.rs:39-76, cuda_partials/mod.rs:63-101).
+ *   internals[n]          children-first dirty internals, root last
+ *   children[n][2]        child node ids of each listed internal
+ *   matrices[n][2][C][4][4] transition matrices of the left and right child
+ *                         edge per rate category (C = 1: the reference's
+ *                         [n*2][4][4] layout)
+ *   frequencies[4]        base frequencies (Transitions::frequencies)
+ * The launch is asynchronous; results are read by the calls below. */
+B3G_API b3g_status b3g_calculator_propose(b3g_calculator *calc,
+					  const uint32_t *internals,
+					  const uint32_t *children, uint32_t n,
+					  const double *matrices,
+					  const double *frequencies);
+/* Calculator::likelihoods: per-pattern log-likelihoods with the scaling
+ * removed, [C][P] (C = 1: [P]).  Blocks until the last proposal is done. */
+B3G_API b3g_status b3g_calculator_likelihoods(b3g_calculator *calc,
+					      double *out);
+/* Calculator::accept / reject (cpu4.rs:78-90, sk/src/editbuf.rs:48-65):
+ * selector flips only, no device copies. */
+B3G_API b3g_status b3g_calculator_accept(b3g_calculator *calc);
+B3G_API b3g_status b3g_calculator_reject(b3g_calculator *calc);
+
+/* ---- likelihood level (DnaLikelihood / GammaLikelihood) -----------------
+ * Pattern weights from deduplicate (likelihood/mod.rs:74-132). Default 1. */
+B3G_API b3g_status b3g_calculator_set_weights(b3g_calculator *calc,
+					      const uint32_t *weights);
+/* Substitution model given as an eigensystem, e.g. the analytic HKY one
+ * (substitution.rs:336-388): Q = V diag(lambda) V^-1, all row-major.  With
+ * `shortcuts` set, d > 20 gives rows equal to the frequencies and d < 1e-10
+ * gives I + Q d with a unit diagonal, as HKY/GTR::write_transition do
+ * (substitution.rs:403-420, 571-588). */
+B3G_API b3g_status b3g_calculator_set_eigen(b3g_calculator *calc,
+					    const double *V,
+					    const double *Vinv,
+					    const double *lambda,
+					    const double *Q,
+					    const double *frequencies,
+					    int shortcuts);
+/* Reversible model from symmetric exchangeabilities in upper-triangle
+ * row-major order (AC, AG, AT, CG, CT, GT for DNA: GTR::update_matrices,
+ * substitution.rs:502-555) and frequencies.  Q is normalised to mean rate 1
+ * and decomposed on the device in FP64 (symmetric Jacobi). */
+B3G_API b3g_status b3g_calculator_set_reversible(b3g_calculator *calc,
+						 const double *rates,
+						 const double *frequencies,
+						 int shortcuts);
+/* Rate multipliers per category, [C] (default all 1). */
+B3G_API b3g_status b3g_calculator_set_category_rates(b3g_calculator *calc,
+						     const double *rates);
+/* Median-discretised Gamma(alpha) rates, normalised to mean 1
+ * (update_categories, likelihood/gamma.rs:205-225). */
+B3G_API b3g_status b3g_calculator_set_gamma(b3g_calculator *calc,
+					    double alpha);
+/* Dirty-path evaluation from edge time lengths.  lengths[n][2] are the time
+ * lengths (parent height - child height) of the left and right child edge of
+ * each listed internal; the transition distance of category c is
+ * length * (clock_rate * rate_c), as GammaLikelihood computes it
+ * (gamma.rs:126-134).  Asynchronous. */
+B3G_API b3g_status b3g_calculator_propose_lengths(b3g_calculator *calc,
+						  const uint32_t *internals,
+						  const uint32_t *children,
+						  uint32_t n,
+						  const double *lengths,
+						  double clock_rate);
+/* Weighted root log-likelihood of the last proposal: sum over patterns of
+ * weight * (log-sum-exp over categories + ln(1/C)); for C = 1 this is
+ * weighted_sum (likelihood/mod.rs:134-139).  Blocks. */
+B3G_API b3g_status b3g_calculator_log_likelihood(b3g_calculator *calc,
+						 double *out);
+/* Per-pattern mixed log-likelihoods of the last proposal, [P].  Blocks. */
+B3G_API b3g_status b3g_calculator_site_log_likelihoods(b3g_calculator *calc,
+						       double *out);
+/* Device time of the last proposal in milliseconds, from CUDA events on the
+ * calculator's stream: the transition-matrix kernel and the pruning kernel
+ * (which includes the root reduction).  Blocks. */
+B3G_API b3g_status b3g_calculator_last_timing(b3g_calculator *calc,
+					      float *transition_ms,
+					      float *prune_ms);
+/* Sums of those device times over every proposal since the last reset, and
+ * the number of proposals.  The events live in a ring that is harvested
+ * without stalling back-to-back proposals.  Blocks until all are done. */
+B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
+						int reset,
+						double *transition_ms,
+						double *prune_ms,
+						uint64_t *proposals);
+/* Device time between two markers on the calculator's stream: span_begin
+ * records the first, span_end records the second, waits and returns the
+ * elapsed milliseconds. */
+B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc);
+B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

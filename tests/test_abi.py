@@ -1,0 +1,93 @@
+"""The C ABI library without a GPU: it loads, exports every symbol that
+include/b3g.h declares, the ctypes table covers all of them, and calls fail
+with a status and a message instead of crashing."""
+
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "b3g.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"B3G_API[^;(]*?\b(b3g_\w+)\s*\(", text, flags=re.S)))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "b3g_calculator_create" in names
+    assert "b3g_calculator_propose" in names
+    assert len(names) >= 18
+
+
+def test_library_exports_every_declared_symbol():
+    from aspartik_gb300 import _native
+
+    lib = ct.CDLL(str(_native.LIB_PATH))
+    for name in declared_symbols():
+        assert hasattr(lib, name), f"libb3g.so does not export {name}"
+    assert set(declared_symbols()) == set(_native.SIGNATURES), \
+        "ctypes signature table and header disagree"
+
+
+def test_only_declared_symbols_are_exported():
+    import subprocess
+
+    from aspartik_gb300 import _native
+
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_native.LIB_PATH)],
+                         capture_output=True, text=True, check=True).stdout
+    ours = sorted({ln.split()[-1] for ln in out.splitlines() if ln.split()[-1].startswith("b3g_")})
+    assert ours == declared_symbols()
+
+
+def test_version_string():
+    from aspartik_gb300._native import lib
+
+    assert b"sm_103a" in lib.b3g_version()
+
+
+def test_create_rejects_bad_config_without_touching_a_gpu():
+    from aspartik_gb300 import _native as nat
+
+    handle = ct.c_void_p()
+    samples = np.ones(8, dtype=np.uint8)
+    cfg = nat.Config(1, 8, 4, 1, 0, 30, 0, 0)  # one leaf: invalid
+    st = nat.lib.b3g_calculator_create(ct.byref(cfg), nat.as_ptr(samples, ct.c_uint8),
+                                       ct.byref(handle))
+    assert st == nat.B3G_ERR_INVALID_ARGUMENT
+    assert b"num_leaves" in nat.lib.b3g_last_error()
+    cfg = nat.Config(2, 4, 5, 1, 0, 30, 0, 0)  # 5 states: unsupported
+    st = nat.lib.b3g_calculator_create(ct.byref(cfg), nat.as_ptr(samples, ct.c_uint8),
+                                       ct.byref(handle))
+    assert st == nat.B3G_ERR_INVALID_ARGUMENT
+
+
+def test_null_handles_are_reported():
+    from aspartik_gb300 import _native as nat
+
+    assert nat.lib.b3g_calculator_accept(None) == nat.B3G_ERR_INVALID_ARGUMENT
+    assert nat.lib.b3g_calculator_num_patterns(None) == 0
+    nat.lib.b3g_calculator_destroy(None)  # no-op
+
+
+def test_no_gpu_reports_cuda_error():
+    """On a machine without a GPU, construction fails with a CUDA status."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from aspartik_gb300 import _native as nat
+
+    handle = ct.c_void_p()
+    samples = np.ones(8, dtype=np.uint8)
+    cfg = nat.Config(2, 4, 4, 1, 0, 30, 0, 0)
+    st = nat.lib.b3g_calculator_create(ct.byref(cfg), nat.as_ptr(samples, ct.c_uint8),
+                                       ct.byref(handle))
+    assert st in (nat.B3G_ERR_CUDA, nat.B3G_ERR_INVALID_ARGUMENT)
+    assert nat.lib.b3g_last_error()
