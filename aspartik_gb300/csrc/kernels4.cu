@@ -203,10 +203,14 @@ __device__ __forceinline__ void neumaier_add(double &sum, double &comp,
 					     double x)
 {
 	const double t = sum + x;
-	if (fabs(sum) >= fabs(x))
-		comp += (sum - t) + x;
-	else
-		comp += (x - t) + sum;
+	// an impossible pattern (-inf) makes the sum -inf; the compensation
+	// of infinities would be NaN, so it only tracks finite sums
+	if (isfinite(t)) {
+		if (fabs(sum) >= fabs(x))
+			comp += (sum - t) + x;
+		else
+			comp += (x - t) + sum;
+	}
 	sum = t;
 }
 
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 		double sum = 0.0, comp = 0.0;
 		for (uint32_t bix = 0; bix < gridDim.x; bix++)
 			neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
-		*prm.lnl_out = sum + comp;
+		*prm.lnl_out = isfinite(sum) ? sum + comp : sum;
 		*prm.ticket = 0u;
 	}
 }
