@@ -99,6 +99,8 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 
 	selectors_.assign(I_, 0);
 	stamp_.assign(2 * L_ - 1, 0);
+	pos_.assign(2 * L_ - 1, 0);
+	run_of_.assign(I_, 0);
 
 	const size_t slots = 2ull * I_;
 	const size_t rsz = f32_ ? sizeof(float) : sizeof(double);
@@ -314,15 +316,29 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 		const uint32_t k = v - L_;
 		return k * 2 + (selectors_[k] & 1u);
 	};
+	// Runs of mutually independent entries: entry i opens a new run when
+	// one of its children is listed inside the current run.  validate_lists
+	// left stamp_[v] == stamp_epoch_ on every listed internal.
+	uint32_t run_start = 0;
 	for (uint32_t i = 0; i < n; ++i) {
 		NodeOp op;
 		op.out = slot_of(internals[i]);
 		const uint32_t l = children[2 * i], r = children[2 * i + 1];
 		op.left = l < L_ ? (kTipBit | l) : slot_of(l);
 		op.right = r < L_ ? (kTipBit | r) : slot_of(r);
-		op.pad = 0;
+		for (const uint32_t ch : {l, r})
+			if (ch >= L_ && stamp_[ch] == stamp_epoch_ &&
+			    pos_[ch] >= run_start)
+				run_start = i;
+		pos_[internals[i]] = i;
+		run_of_[i] = run_start;
 		ops[i] = op;
 	}
+	// NodeOp::pad = entries left in the run, this one included
+	for (uint32_t i = n; i-- > 0;)
+		ops[i].pad = (i + 1 < n && run_of_[i + 1] == run_of_[i])
+				     ? ops[i + 1].pad + 1
+				     : 1;
 }
 
 void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,

@@ -87,7 +87,9 @@ class Calculator {
 
 	// host state
 	std::vector<uint8_t> selectors_; // EditBuf over internals
-	std::vector<uint32_t> stamp_;    // list-position scratch per node
+	std::vector<uint32_t> stamp_;    // per-node epoch stamps
+	std::vector<uint32_t> pos_;      // list position of each listed node
+	std::vector<uint32_t> run_of_;   // start of the run of each entry
 	uint32_t stamp_epoch_ = 0;
 	bool model_set_ = false;
 	bool have_result_ = false;

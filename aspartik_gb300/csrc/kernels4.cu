@@ -214,6 +214,94 @@ __device__ __forceinline__ void neumaier_add(double &sum, double &comp,
 	sum = t;
 }
 
+// Inputs of one child of a node: a tip code, or a partial with the
+// cumulative rescale count of its subtree.
+template <typename T> struct ChildIn {
+	T x;
+	int32_t s;
+	uint32_t code;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_child(const PruneParams &prm,
+					   const T *__restrict__ partials,
+					   uint32_t id, uint32_t p, uint32_t c,
+					   ChildIn<T> &in)
+{
+	if (id & kTipBit) {
+		in.code = prm.tips[(size_t)(id & ~kTipBit) * prm.ldp + p];
+		in.s = 0;
+	} else {
+		const size_t ix = ((size_t)id * prm.C + c) * prm.ldp + p;
+		in.x = partials[ix];
+		in.s = prm.scales[ix];
+		in.code = 0;
+	}
+}
+
+// P(t) applied to the child: the transposed table row of the tip code, or
+// the 4x4 product with the child's partial.
+template <typename T>
+__device__ __forceinline__ T apply_child(uint32_t id, const T *__restrict__ pt,
+					 const ChildIn<T> &in)
+{
+	return (id & kTipBit) ? pt[in.code] : v4_apply(pt, in.x);
+}
+
+// U consecutive schedule entries that are mutually independent: every load
+// of the batch is issued before any product, so a thread keeps 2U child
+// partials in flight instead of 2.
+template <typename VT, bool kPow2, int U>
+__device__ __forceinline__ void prune_batch(const PruneParams &prm,
+					    typename VT::T *__restrict__ partials,
+					    const typename VT::T *__restrict__ ptab,
+					    uint32_t i0, uint32_t p, uint32_t c,
+					    typename VT::T &y_out, int32_t &cnt_out)
+{
+	typedef typename VT::T T;
+	NodeOp op[U];
+	ChildIn<T> l[U], r[U];
+#pragma unroll
+	for (int u = 0; u < U; ++u) {
+		op[u] = prm.ops[i0 + u];
+		load_child(prm, partials, op[u].left, p, c, l[u]);
+		load_child(prm, partials, op[u].right, p, c, r[u]);
+	}
+#pragma unroll
+	for (int u = 0; u < U; ++u) {
+		const uint32_t i = i0 + u;
+		const T *tl = ptab + ((size_t)(2 * i) * prm.C + c) * 5;
+		const T *tr = ptab + ((size_t)(2 * i + 1) * prm.C + c) * 5;
+		T y = v4_mul(apply_child(op[u].left, tl, l[u]),
+			     apply_child(op[u].right, tr, r[u]));
+		int32_t own;
+		if constexpr (kPow2) {
+			own = rescale_pow2(y);
+		} else {
+			// tip-tip nodes are never rescaled (cpu4.rs:288-318)
+			own = ((op[u].left & op[u].right) & kTipBit)
+				      ? 0
+				      : rescale_threshold(y, prm.scale_threshold,
+							  prm.scale_mult);
+		}
+		const int32_t cnt = l[u].s + r[u].s + own;
+		const size_t ox = ((size_t)op[u].out * prm.C + c) * prm.ldp + p;
+		partials[ox] = y;
+		prm.scales[ox] = cnt;
+		y_out = y;
+		cnt_out = cnt;
+	}
+}
+
+// Neumaier merge of two compensated partial sums.
+__device__ __forceinline__ void neumaier_merge(double &sum, double &comp,
+					       double sum2, double comp2)
+{
+	neumaier_add(sum, comp, sum2);
+	if (isfinite(sum))
+		comp += comp2;
+}
+
 template <typename VT, bool kPow2>
 __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 {
@@ -224,57 +312,35 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 	const uint32_t p = blockIdx.x * tp + threadIdx.x;
 	const uint32_t ldp = prm.ldp, C = prm.C;
 	T *__restrict__ partials = (T *)prm.partials;
-	int32_t *__restrict__ scales = prm.scales;
 	const T *__restrict__ ptab = (const T *)prm.ptab;
 
+	// The schedule is split on the host into runs of mutually independent
+	// entries; NodeOp::pad of an entry is the number of entries left in its
+	// run (itself included).
 	T y = v4_make<T, R>(0, 0, 0, 0);
 	int32_t cnt = 0;
-	for (uint32_t i = 0; i < prm.n; ++i) {
-		const NodeOp op = prm.ops[i];
-		const T *tl = ptab + ((size_t)(2 * i) * C + c) * 5;
-		const T *tr = ptab + ((size_t)(2 * i + 1) * C + c) * 5;
-		T a, b;
-		int32_t ca = 0, cb = 0;
-		if (op.left & kTipBit) {
-			const uint32_t code =
-				prm.tips[(size_t)(op.left & ~kTipBit) * ldp + p];
-			a = tl[code];
+	for (uint32_t i = 0; i < prm.n;) {
+		const uint32_t avail = prm.ops[i].pad;
+		// FP64 partials take twice the registers: batches of at most 2
+		constexpr uint32_t kMaxU = sizeof(R) == 4 ? 4u : 2u;
+		if (kMaxU >= 4 && avail >= 4) {
+			prune_batch<VT, kPow2, 4>(prm, partials, ptab, i, p, c, y, cnt);
+			i += 4;
+		} else if (avail >= 2) {
+			prune_batch<VT, kPow2, 2>(prm, partials, ptab, i, p, c, y, cnt);
+			i += 2;
 		} else {
-			const size_t ix = ((size_t)op.left * C + c) * ldp + p;
-			a = v4_apply(tl, partials[ix]);
-			ca = scales[ix];
+			prune_batch<VT, kPow2, 1>(prm, partials, ptab, i, p, c, y, cnt);
+			i += 1;
 		}
-		if (op.right & kTipBit) {
-			const uint32_t code =
-				prm.tips[(size_t)(op.right & ~kTipBit) * ldp + p];
-			b = tr[code];
-		} else {
-			const size_t ix = ((size_t)op.right * C + c) * ldp + p;
-			b = v4_apply(tr, partials[ix]);
-			cb = scales[ix];
-		}
-		y = v4_mul(a, b);
-		int32_t own;
-		if constexpr (kPow2) {
-			own = rescale_pow2(y);
-		} else {
-			// tip-tip nodes are never rescaled (cpu4.rs:288-318)
-			own = ((op.left & op.right) & kTipBit)
-				      ? 0
-				      : rescale_threshold(y, prm.scale_threshold,
-							  prm.scale_mult);
-		}
-		cnt = ca + cb + own;
-		const size_t ox = ((size_t)op.out * C + c) * ldp + p;
-		partials[ox] = y;
-		scales[ox] = cnt;
 	}
 
 	// ---- root: category mixing, pattern weights, block sum ------------
+	const uint32_t nthr = tp * C;
 	extern __shared__ double smem[];
-	double *s_val = smem;                            // [C][tp]
-	int32_t *s_exp = (int32_t *)(smem + C * tp);     // [C][tp]
-	double *s_warp = smem + C * tp + (C * tp + 1) / 2; // [8]
+	double *s_val = smem;                          // [nthr]
+	int32_t *s_exp = (int32_t *)(smem + nthr);     // [nthr]
+	double *s_warp = smem + 2 * nthr;              // [16]
 	__shared__ unsigned s_last;
 
 	const double root_dot = (double)prm.pi[0] * (double)y.x +
@@ -357,12 +423,36 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 		s_last = (t == gridDim.x - 1u);
 	}
 	__syncthreads();
-	if (s_last && tid == 0) {
-		__threadfence();
-		double sum = 0.0, comp = 0.0;
-		for (uint32_t bix = 0; bix < gridDim.x; bix++)
-			neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
-		*prm.lnl_out = isfinite(sum) ? sum + comp : sum;
+	if (!s_last)
+		return;
+	// The last block folds every block sum: each thread a fixed strided
+	// subset with Neumaier compensation, then a fixed-shape tree in shared
+	// memory, so the result does not depend on block completion order.
+	__threadfence();
+	double sum = 0.0, comp = 0.0;
+	for (uint32_t bix = tid; bix < gridDim.x; bix += nthr)
+		neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
+	double *s_sum = smem;         // reuses s_val
+	double *s_comp = smem + nthr; // reuses s_exp
+	__syncthreads();
+	s_sum[tid] = sum;
+	s_comp[tid] = comp;
+	__syncthreads();
+	uint32_t span = 1;
+	while (span < nthr)
+		span <<= 1;
+	for (uint32_t stride = span >> 1; stride > 0; stride >>= 1) {
+		if (tid < stride && tid + stride < nthr) {
+			double a = s_sum[tid], ac = s_comp[tid];
+			neumaier_merge(a, ac, s_sum[tid + stride], s_comp[tid + stride]);
+			s_sum[tid] = a;
+			s_comp[tid] = ac;
+		}
+		__syncthreads();
+	}
+	if (tid == 0) {
+		const double total = s_sum[0];
+		*prm.lnl_out = isfinite(total) ? total + s_comp[0] : total;
 		*prm.ticket = 0u;
 	}
 }
@@ -481,7 +571,7 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 {
 	const dim3 block(tile, p.C);
 	const dim3 grid(p.ldp / tile);
-	const size_t smem = sizeof(double) * (p.C * tile + (p.C * tile + 1) / 2 + 8);
+	const size_t smem = sizeof(double) * (2 * p.C * tile + 16);
 	if (f32)
 		prune4_kernel<V4f, true><<<grid, block, smem, s>>>(p);
 	else
