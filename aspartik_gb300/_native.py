@@ -57,6 +57,31 @@ class Config(ct.Structure):
     ]
 
 
+class PruneBuffers(ct.Structure):
+    """b3g_prune_buffers: device pointers and sizes for b3g_prune_noalloc."""
+
+    _fields_ = [
+        ("tips", ct.c_void_p),
+        ("partials", ct.c_void_p),
+        ("scales", ct.c_void_p),
+        ("ops", ct.c_void_p),
+        ("tables", ct.c_void_p),
+        ("frequencies", ct.c_void_p),
+        ("weights", ct.c_void_p),
+        ("site_lnl", ct.c_void_p),
+        ("lnl", ct.c_void_p),
+        ("n", ct.c_uint32),
+        ("ldp", ct.c_uint32),
+        ("num_categories", ct.c_uint32),
+        ("precision", ct.c_uint32),
+        ("scale_ln", ct.c_uint32),
+        ("reserved", ct.c_uint32),
+    ]
+
+
+NOALLOC_MAX_BLOCKS = 16384
+TIP = 0x80000000
+
 _u8p = ct.POINTER(ct.c_uint8)
 _u32p = ct.POINTER(ct.c_uint32)
 _f64p = ct.POINTER(ct.c_double)
@@ -88,6 +113,7 @@ SIGNATURES = {
         ct.c_int, [_vp, ct.c_int, _f64p, _f64p, ct.POINTER(ct.c_uint64)]),
     "b3g_calculator_span_begin": (ct.c_int, [_vp]),
     "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
+    "b3g_prune_noalloc": (ct.c_int, [ct.POINTER(PruneBuffers), _vp]),
 }
 
 

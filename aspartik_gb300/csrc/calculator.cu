@@ -693,6 +693,17 @@ b3g::Calculator *calc_of(b3g_calculator *c)
 
 } // namespace
 
+namespace b3g {
+
+// Records the outcome of an entry point defined in another translation unit
+// in the per-thread message that b3g_last_error() returns.
+void set_last_error(const char *message)
+{
+	g_last_error = message ? message : "";
+}
+
+} // namespace b3g
+
 extern "C" {
 
 B3G_API const char *b3g_last_error(void) { return g_last_error.c_str(); }

@@ -191,6 +191,83 @@ B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
 B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc);
 B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
 
+/* ---- allocation-free pruning --------------------------------------------
+ * This entry point has no counterpart in the reference.
+ *
+ * It is for callers that must not have this library allocate device memory:
+ * a host program whose every device buffer comes from its own allocator or
+ * pool (for example a Rust CUDA wrapper that owns the calculator's buffers,
+ * as the reference's CUDA calculators own theirs), or code that runs where a
+ * cudaMalloc/cudaFree is not allowed or would stall the whole device, such
+ * as a loop that is being recorded into a CUDA graph or a latency-critical
+ * MCMC step.  The caller passes every input and output as device memory in
+ * the layouts below; the only working memory of the call, one double per
+ * thread block plus a completion counter, is a fixed array compiled into
+ * the library (B3G_NOALLOC_MAX_BLOCKS blocks, 128 KiB + 256 bytes), which
+ * every GPU that loads the library holds until the process exits.
+ *
+ * Limits and rules:
+ *  - At most B3G_NOALLOC_MAX_BLOCKS blocks: ldp / tile with tile = 128
+ *    patterns for 1 category, 64 for 2, 32 for more (so up to 2,097,152
+ *    padded patterns for 1 category, 524,288 for 4).  Larger problems are
+ *    rejected with B3G_ERR_INVALID_ARGUMENT.
+ *  - Runs on the calling thread's current device; `stream` (a cudaStream_t,
+ *    or NULL for the default stream) must belong to it.  The call is
+ *    asynchronous.
+ *  - The first call on a device looks up the array's device address (once
+ *    per device); make that first call before any stream capture begins.
+ *  - All calls in the process share the one array per device, and each call
+ *    clears its counter first: calls that can overlap on the GPU (different
+ *    streams without ordering between them) race and must not be issued.
+ *  - The device data is trusted: the caller guarantees that every slot,
+ *    leaf and tip code in `ops` and `tips` lies inside the buffers.
+ *
+ * Layouts (ldp = padded pattern count, a multiple of 128; C categories;
+ * R = double for B3G_PRECISION_F64, float for B3G_PRECISION_F32):
+ *   tips        u8  [L][ldp]   states 0..3, 4 = unknown (padding: 4)
+ *   partials    R   [slots][C][ldp][4]
+ *   scales      i32 [slots][C][ldp]
+ *   ops         b3g_node_op [n], children-first, root last
+ *   tables      R   [n][2][C][5][4]: for entry i, side s (0 left, 1 right),
+ *               category c: element [k][j] = P(t)[j][k] for k < 4 and 1 for
+ *               k = 4 (P(t) transposed, then a row of ones)
+ *   frequencies f64 [4]
+ *   weights     u32 [ldp] (0 on padding)
+ *   site_lnl    f64 [ldp] out: per-pattern mixed log-likelihood
+ *   lnl         f64 [1]   out: weighted sum over patterns
+ */
+#define B3G_NOALLOC_MAX_BLOCKS 16384u
+#define B3G_TIP 0x80000000u /* b3g_node_op child: B3G_TIP | leaf id */
+
+typedef struct b3g_node_op {
+	uint32_t out;   /* output slot */
+	uint32_t left;  /* child slot, or B3G_TIP | leaf id */
+	uint32_t right; /* child slot, or B3G_TIP | leaf id */
+	uint32_t run;   /* entries from this one on that are mutually
+			   independent (1 is always valid) */
+} b3g_node_op;
+
+typedef struct b3g_prune_buffers {
+	const uint8_t *tips;
+	void *partials;
+	int32_t *scales;
+	const b3g_node_op *ops;
+	const void *tables;
+	const double *frequencies;
+	const uint32_t *weights;
+	double *site_lnl;
+	double *lnl;
+	uint32_t n;              /* entries in ops, >= 1 */
+	uint32_t ldp;            /* padded patterns, multiple of 128 */
+	uint32_t num_categories; /* 1..16 */
+	uint32_t precision;      /* B3G_PRECISION_* */
+	uint32_t scale_ln;       /* FP64 form rescale exponent */
+	uint32_t reserved;       /* must be 0 */
+} b3g_prune_buffers;
+
+B3G_API b3g_status b3g_prune_noalloc(const b3g_prune_buffers *buffers,
+				     void *stream);
+
 #ifdef __cplusplus
 }
 #endif
