@@ -75,6 +75,8 @@ struct PruneParams {
 	uint32_t ldp;
 	uint32_t C;
 	uint32_t scale_ln;
+	uint32_t num_leaves; // rows of tips
+	uint32_t tips_smem;  // stage the block's tip codes in shared memory
 	double scale_threshold;
 	double scale_mult;
 	double log_inv_c;

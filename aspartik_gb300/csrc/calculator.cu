@@ -320,12 +320,14 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 	// one of its children is listed inside the current run.  validate_lists
 	// left stamp_[v] == stamp_epoch_ on every listed internal.
 	uint32_t run_start = 0;
+	tip_children_ = 0;
 	for (uint32_t i = 0; i < n; ++i) {
 		NodeOp op;
 		op.out = slot_of(internals[i]);
 		const uint32_t l = children[2 * i], r = children[2 * i + 1];
 		op.left = l < L_ ? (kTipBit | l) : slot_of(l);
 		op.right = r < L_ ? (kTipBit | r) : slot_of(r);
+		tip_children_ += (l < L_) + (r < L_);
 		for (const uint32_t ch : {l, r})
 			if (ch >= L_ && stamp_[ch] == stamp_epoch_ &&
 			    pos_[ch] >= run_start)
@@ -388,6 +390,13 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pp.ldp = ldp_;
 	pp.C = C_;
 	pp.scale_ln = scale_ln_;
+	pp.num_leaves = L_;
+	// stage the tip tile when the list reads at least a quarter of the
+	// leaves and the tile fits in 64 KiB of shared memory
+	pp.tips_smem = (4ull * tip_children_ >= L_ &&
+			(size_t)L_ * tile_ <= 64u * 1024u)
+			       ? 1u
+			       : 0u;
 	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
 	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));

@@ -91,6 +91,7 @@ class Calculator {
 	std::vector<uint32_t> pos_;      // list position of each listed node
 	std::vector<uint32_t> run_of_;   // start of the run of each entry
 	uint32_t stamp_epoch_ = 0;
+	uint32_t tip_children_ = 0;      // tip children in the staged list
 	bool model_set_ = false;
 	bool have_result_ = false;
 	bool cat_valid_ = false;

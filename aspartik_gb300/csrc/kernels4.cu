@@ -302,6 +302,304 @@ __device__ __forceinline__ void neumaier_merge(double &sum, double &comp,
 		comp += comp2;
 }
 
+// Root of the schedule: category mixing, pattern weights, block sum and the
+// fold of all block sums by the last block to finish.  One `lead` thread per
+// (pattern, category) column reports its root dot product pi . x and count;
+// `pl` is the column's pattern inside the block.  Shared memory: 2 * nthr +
+// 32 doubles, nthr = threads per block.
+template <bool kPow2>
+__device__ __forceinline__ void finish_root(const PruneParams &prm, double *smem,
+					    uint32_t tp, uint32_t pl, uint32_t p,
+					    uint32_t c, bool lead, double root_dot,
+					    int32_t cnt)
+{
+	const uint32_t C = prm.C, ldp = prm.ldp;
+	const uint32_t nthr = blockDim.x * blockDim.y;
+	double *s_val = smem;                         // [tp * C]
+	int32_t *s_exp = (int32_t *)(smem + nthr);    // [tp * C]
+	double *s_warp = smem + 2 * nthr;             // [32]
+	__shared__ unsigned s_last;
+
+	if (lead) {
+		if constexpr (kPow2) {
+			s_val[c * tp + pl] = root_dot;
+			s_exp[c * tp + pl] = cnt;
+			if (prm.cat_lnl)
+				prm.cat_lnl[(size_t)c * ldp + p] =
+					log(root_dot) +
+					(double)cnt * 0.69314718055994530942;
+		} else {
+			// cpu4.rs:277-284 and :63-68; the count times scale_ln
+			// is an unsigned 32-bit product as in the reference
+			const double lcat = log(root_dot) -
+					    (double)((uint32_t)cnt * prm.scale_ln);
+			s_val[c * tp + pl] = lcat;
+			if (prm.cat_lnl)
+				prm.cat_lnl[(size_t)c * ldp + p] = lcat;
+		}
+	}
+	__syncthreads();
+
+	double contrib = 0.0;
+	if (c == 0 && lead) {
+		double site;
+		if constexpr (kPow2) {
+			// sum_c s_c 2^E_c = 2^Emax sum_c s_c 2^(E_c - Emax)
+			int32_t emax = INT32_MIN;
+			for (uint32_t k = 0; k < C; k++)
+				if (s_val[k * tp + pl] > 0.0)
+					emax = max(emax, s_exp[k * tp + pl]);
+			if (emax == INT32_MIN) {
+				site = -INFINITY;
+			} else {
+				double acc = 0.0;
+				for (uint32_t k = 0; k < C; k++)
+					acc += scalbn(s_val[k * tp + pl],
+						      s_exp[k * tp + pl] - emax);
+				site = log(acc) +
+				       (double)emax * 0.69314718055994530942 +
+				       prm.log_inv_c;
+			}
+		} else {
+			// log_sum_exp (likelihood/mod.rs:141-151) + ln(1/C)
+			// (gamma.rs:155-165); exact identity for C = 1
+			double mx = -INFINITY;
+			for (uint32_t k = 0; k < C; k++)
+				mx = fmax(mx, s_val[k * tp + pl]);
+			if (mx == -INFINITY) {
+				site = -INFINITY;
+			} else {
+				double se = 0.0;
+				for (uint32_t k = 0; k < C; k++)
+					se += exp(s_val[k * tp + pl] - mx);
+				site = mx + log(se) + prm.log_inv_c;
+			}
+		}
+		prm.site_lnl[p] = site;
+		const uint32_t w = prm.weights[p];
+		contrib = w ? site * (double)w : 0.0;
+	}
+
+	// block sum over the category-0 warps, in a fixed order
+	const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+	const uint32_t lane = tid & 31u, warp = tid >> 5;
+	for (int off = 16; off > 0; off >>= 1)
+		contrib += __shfl_down_sync(0xffffffffu, contrib, off);
+	if (c == 0 && lane == 0)
+		s_warp[warp] = contrib;
+	__syncthreads();
+	if (tid == 0) {
+		double bsum = 0.0;
+		for (uint32_t w = 0; w < blockDim.x / 32u; w++)
+			bsum += s_warp[w];
+		prm.block_sums[blockIdx.x] = bsum;
+		__threadfence();
+		const unsigned t = atomicAdd(prm.ticket, 1u);
+		s_last = (t == gridDim.x - 1u);
+	}
+	__syncthreads();
+	if (!s_last)
+		return;
+	// The last block folds every block sum: each thread a fixed strided
+	// subset with Neumaier compensation, then a fixed-shape tree in shared
+	// memory, so the result does not depend on block completion order.
+	__threadfence();
+	double sum = 0.0, comp = 0.0;
+	for (uint32_t bix = tid; bix < gridDim.x; bix += nthr)
+		neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
+	double *s_sum = smem;
+	double *s_comp = smem + nthr;
+	__syncthreads();
+	s_sum[tid] = sum;
+	s_comp[tid] = comp;
+	__syncthreads();
+	uint32_t span = 1;
+	while (span < nthr)
+		span <<= 1;
+	for (uint32_t stride = span >> 1; stride > 0; stride >>= 1) {
+		if (tid < stride && tid + stride < nthr) {
+			double a = s_sum[tid], ac = s_comp[tid];
+			neumaier_merge(a, ac, s_sum[tid + stride],
+				       s_comp[tid + stride]);
+			s_sum[tid] = a;
+			s_comp[tid] = ac;
+		}
+		__syncthreads();
+	}
+	if (tid == 0) {
+		const double total = s_sum[0];
+		*prm.lnl_out = isfinite(total) ? total + s_comp[0] : total;
+		*prm.ticket = 0u;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// FP32 chosen form, two lanes per (pattern, category) column.  Lane h of a
+// pair holds states 2h and 2h+1 of every partial; a child product needs the
+// partner's two states, one shfl.xor each.  This doubles the threads of the
+// one-lane layout (the kernel is latency-bound by occupancy) and halves the
+// registers per batched node.
+
+__device__ __forceinline__ float2 f2_apply(const float2 *__restrict__ pt,
+					   float2 x, uint32_t h)
+{
+	// pt[2k] = columns (2h, 2h+1) of row k of the transposed table
+	const float ox = __shfl_xor_sync(0xffffffffu, x.x, 1);
+	const float oy = __shfl_xor_sync(0xffffffffu, x.y, 1);
+	const float x0 = h ? ox : x.x, x1 = h ? oy : x.y;
+	const float x2 = h ? x.x : ox, x3 = h ? x.y : oy;
+	const float2 p0 = pt[0], p1 = pt[2], p2 = pt[4], p3 = pt[6];
+	float2 r;
+	r.x = x0 * p0.x;
+	r.y = x0 * p0.y;
+	r.x = fmaf(x1, p1.x, r.x);
+	r.y = fmaf(x1, p1.y, r.y);
+	r.x = fmaf(x2, p2.x, r.x);
+	r.y = fmaf(x2, p2.y, r.y);
+	r.x = fmaf(x3, p3.x, r.x);
+	r.y = fmaf(x3, p3.y, r.y);
+	return r;
+}
+
+// Power-of-two rescale of a pair's four states (see rescale_pow2).
+__device__ __forceinline__ int32_t rescale_pow2_pair(float2 &y)
+{
+	float m = fmaxf(y.x, y.y);
+	m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+	int32_t shift = 0;
+	uint32_t ex = (__float_as_uint(m) >> 23) & 0xffu;
+	if (ex == 0u) {
+		if (!(m > 0.0f))
+			return 0;
+		const float lift = 18446744073709551616.0f; // 2^64, exact
+		y.x *= lift;
+		y.y *= lift;
+		m *= lift;
+		shift = -64;
+		ex = (__float_as_uint(m) >> 23) & 0xffu;
+	}
+	const int32_t e = (int32_t)ex - 127;
+	const float f = __uint_as_float((uint32_t)(127 - e) << 23);
+	y.x *= f;
+	y.y *= f;
+	return e + shift;
+}
+
+struct PairChild {
+	float2 x;
+	int32_t s;
+	uint32_t code;
+};
+
+__device__ __forceinline__ void load_pair_child(const PruneParams &prm,
+						const float2 *__restrict__ part2,
+						const uint8_t *__restrict__ s_tips,
+						uint32_t tp, uint32_t id, uint32_t p,
+						uint32_t pl, uint32_t c, uint32_t h,
+						PairChild &in)
+{
+	if (id & kTipBit) {
+		const uint32_t leaf = id & ~kTipBit;
+		in.code = s_tips ? s_tips[leaf * tp + pl]
+				 : prm.tips[(size_t)leaf * prm.ldp + p];
+		in.s = 0;
+	} else {
+		const size_t ix = ((size_t)id * prm.C + c) * prm.ldp + p;
+		in.x = part2[ix * 2 + h];
+		in.s = prm.scales[ix];
+		in.code = 0;
+	}
+}
+
+template <int U>
+__device__ __forceinline__ void prune_batch_pair(const PruneParams &prm,
+						 float2 *__restrict__ part2,
+						 const float2 *__restrict__ pt2,
+						 const uint8_t *__restrict__ s_tips,
+						 uint32_t tp, uint32_t i0, uint32_t p,
+						 uint32_t pl, uint32_t c, uint32_t h,
+						 float2 &y_out, int32_t &cnt_out)
+{
+	NodeOp op[U];
+	PairChild l[U], r[U];
+#pragma unroll
+	for (int u = 0; u < U; ++u) {
+		op[u] = prm.ops[i0 + u];
+		load_pair_child(prm, part2, s_tips, tp, op[u].left, p, pl, c, h, l[u]);
+		load_pair_child(prm, part2, s_tips, tp, op[u].right, p, pl, c, h, r[u]);
+	}
+#pragma unroll
+	for (int u = 0; u < U; ++u) {
+		const uint32_t i = i0 + u;
+		// table rows as float2 columns: [n][2][C][5 rows][2 halves]
+		const float2 *tl = pt2 + ((size_t)(2 * i) * prm.C + c) * 10 + h;
+		const float2 *tr = pt2 + ((size_t)(2 * i + 1) * prm.C + c) * 10 + h;
+		const float2 a = (op[u].left & kTipBit) ? tl[2 * l[u].code]
+							: f2_apply(tl, l[u].x, h);
+		const float2 b = (op[u].right & kTipBit) ? tr[2 * r[u].code]
+							 : f2_apply(tr, r[u].x, h);
+		float2 y;
+		y.x = a.x * b.x;
+		y.y = a.y * b.y;
+		const int32_t cnt = l[u].s + r[u].s + rescale_pow2_pair(y);
+		const size_t ox = ((size_t)op[u].out * prm.C + c) * prm.ldp + p;
+		part2[ox * 2 + h] = y;
+		if (h == 0)
+			prm.scales[ox] = cnt;
+		y_out = y;
+		cnt_out = cnt;
+	}
+}
+
+__global__ void __launch_bounds__(512) prune4_pair_kernel(PruneParams prm)
+{
+	const uint32_t tp = blockDim.x >> 1; // patterns per block
+	const uint32_t pl = threadIdx.x >> 1, h = threadIdx.x & 1u;
+	const uint32_t c = threadIdx.y;
+	const uint32_t p0 = blockIdx.x * tp;
+	const uint32_t p = p0 + pl;
+	float2 *__restrict__ part2 = (float2 *)prm.partials;
+	const float2 *__restrict__ pt2 = (const float2 *)prm.ptab;
+	const uint32_t nthr = blockDim.x * blockDim.y;
+	extern __shared__ double smem[];
+
+	// tip codes of this block's patterns for every leaf, staged once
+	const uint8_t *s_tips = nullptr;
+	if (prm.tips_smem) {
+		uint32_t *s_t32 = (uint32_t *)(smem + 2 * nthr + 32);
+		const uint32_t wpr = tp >> 2; // 4-byte words per leaf row
+		const uint32_t total = prm.num_leaves * wpr;
+		const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+		for (uint32_t w = tid; w < total; w += nthr) {
+			const uint32_t leaf = w / wpr, col = w - leaf * wpr;
+			s_t32[w] = *(const uint32_t *)(prm.tips + (size_t)leaf * prm.ldp +
+						       p0 + col * 4);
+		}
+		__syncthreads();
+		s_tips = (const uint8_t *)s_t32;
+	}
+
+	float2 y = make_float2(0.f, 0.f);
+	int32_t cnt = 0;
+	for (uint32_t i = 0; i < prm.n;) {
+		const uint32_t avail = prm.ops[i].pad;
+		if (avail >= 4) {
+			prune_batch_pair<4>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
+			i += 4;
+		} else if (avail >= 2) {
+			prune_batch_pair<2>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
+			i += 2;
+		} else {
+			prune_batch_pair<1>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
+			i += 1;
+		}
+	}
+	double root_dot = (double)prm.pi[2 * h] * (double)y.x +
+			  (double)prm.pi[2 * h + 1] * (double)y.y;
+	root_dot += __shfl_xor_sync(0xffffffffu, root_dot, 1);
+	finish_root<true>(prm, smem, tp, pl, p, c, h == 0, root_dot, cnt);
+}
+
 template <typename VT, bool kPow2>
 __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 {
@@ -335,126 +633,12 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 		}
 	}
 
-	// ---- root: category mixing, pattern weights, block sum ------------
-	const uint32_t nthr = tp * C;
-	extern __shared__ double smem[];
-	double *s_val = smem;                          // [nthr]
-	int32_t *s_exp = (int32_t *)(smem + nthr);     // [nthr]
-	double *s_warp = smem + 2 * nthr;              // [16]
-	__shared__ unsigned s_last;
-
 	const double root_dot = (double)prm.pi[0] * (double)y.x +
 				(double)prm.pi[1] * (double)y.y +
 				(double)prm.pi[2] * (double)y.z +
 				(double)prm.pi[3] * (double)y.w;
-	if constexpr (kPow2) {
-		s_val[c * tp + threadIdx.x] = root_dot;
-		s_exp[c * tp + threadIdx.x] = cnt;
-		if (prm.cat_lnl)
-			prm.cat_lnl[(size_t)c * ldp + p] =
-				log(root_dot) + (double)cnt * 0.69314718055994530942;
-	} else {
-		// cpu4.rs:277-284 and :63-68; the count times scale_ln is an
-		// unsigned 32-bit product as in the reference
-		const double lcat =
-			log(root_dot) - (double)((uint32_t)cnt * prm.scale_ln);
-		s_val[c * tp + threadIdx.x] = lcat;
-		if (prm.cat_lnl)
-			prm.cat_lnl[(size_t)c * ldp + p] = lcat;
-	}
-	__syncthreads();
-
-	double contrib = 0.0;
-	if (c == 0) {
-		double site;
-		if constexpr (kPow2) {
-			// sum_c s_c 2^E_c = 2^Emax sum_c s_c 2^(E_c - Emax)
-			int32_t emax = INT32_MIN;
-			for (uint32_t k = 0; k < C; k++)
-				if (s_val[k * tp + threadIdx.x] > 0.0)
-					emax = max(emax, s_exp[k * tp + threadIdx.x]);
-			if (emax == INT32_MIN) {
-				site = -INFINITY;
-			} else {
-				double acc = 0.0;
-				for (uint32_t k = 0; k < C; k++)
-					acc += scalbn(s_val[k * tp + threadIdx.x],
-						      s_exp[k * tp + threadIdx.x] - emax);
-				site = log(acc) +
-				       (double)emax * 0.69314718055994530942 +
-				       prm.log_inv_c;
-			}
-		} else {
-			// log_sum_exp (likelihood/mod.rs:141-151) + ln(1/C)
-			// (gamma.rs:155-165); exact identity for C = 1
-			double mx = -INFINITY;
-			for (uint32_t k = 0; k < C; k++)
-				mx = fmax(mx, s_val[k * tp + threadIdx.x]);
-			if (mx == -INFINITY) {
-				site = -INFINITY;
-			} else {
-				double se = 0.0;
-				for (uint32_t k = 0; k < C; k++)
-					se += exp(s_val[k * tp + threadIdx.x] - mx);
-				site = mx + log(se) + prm.log_inv_c;
-			}
-		}
-		prm.site_lnl[p] = site;
-		const uint32_t w = prm.weights[p];
-		contrib = w ? site * (double)w : 0.0;
-	}
-
-	// block sum over the category-0 threads (warps 0 .. tp/32-1), in a
-	// fixed order
-	const uint32_t tid = threadIdx.y * tp + threadIdx.x;
-	const uint32_t lane = tid & 31u, warp = tid >> 5;
-	for (int off = 16; off > 0; off >>= 1)
-		contrib += __shfl_down_sync(0xffffffffu, contrib, off);
-	if (c == 0 && lane == 0)
-		s_warp[warp] = contrib;
-	__syncthreads();
-	if (tid == 0) {
-		double bsum = 0.0;
-		for (uint32_t w = 0; w < tp / 32u; w++)
-			bsum += s_warp[w];
-		prm.block_sums[blockIdx.x] = bsum;
-		__threadfence();
-		const unsigned t = atomicAdd(prm.ticket, 1u);
-		s_last = (t == gridDim.x - 1u);
-	}
-	__syncthreads();
-	if (!s_last)
-		return;
-	// The last block folds every block sum: each thread a fixed strided
-	// subset with Neumaier compensation, then a fixed-shape tree in shared
-	// memory, so the result does not depend on block completion order.
-	__threadfence();
-	double sum = 0.0, comp = 0.0;
-	for (uint32_t bix = tid; bix < gridDim.x; bix += nthr)
-		neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
-	double *s_sum = smem;         // reuses s_val
-	double *s_comp = smem + nthr; // reuses s_exp
-	__syncthreads();
-	s_sum[tid] = sum;
-	s_comp[tid] = comp;
-	__syncthreads();
-	uint32_t span = 1;
-	while (span < nthr)
-		span <<= 1;
-	for (uint32_t stride = span >> 1; stride > 0; stride >>= 1) {
-		if (tid < stride && tid + stride < nthr) {
-			double a = s_sum[tid], ac = s_comp[tid];
-			neumaier_merge(a, ac, s_sum[tid + stride], s_comp[tid + stride]);
-			s_sum[tid] = a;
-			s_comp[tid] = ac;
-		}
-		__syncthreads();
-	}
-	if (tid == 0) {
-		const double total = s_sum[0];
-		*prm.lnl_out = isfinite(total) ? total + s_comp[0] : total;
-		*prm.ticket = 0u;
-	}
+	extern __shared__ double smem[];
+	finish_root<kPow2>(prm, smem, tp, threadIdx.x, p, c, true, root_dot, cnt);
 }
 
 // ---------------------------------------------------------------------------
@@ -569,13 +753,30 @@ cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
 cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 			  cudaStream_t s)
 {
-	const dim3 block(tile, p.C);
 	const dim3 grid(p.ldp / tile);
-	const size_t smem = sizeof(double) * (2 * p.C * tile + 16);
-	if (f32)
-		prune4_kernel<V4f, true><<<grid, block, smem, s>>>(p);
-	else
-		prune4_kernel<V4d, false><<<grid, block, smem, s>>>(p);
+	if (f32 && 2 * tile * p.C <= 512) {
+		// two lanes per (pattern, category) column
+		const dim3 block(2 * tile, p.C);
+		const size_t nthr = 2 * (size_t)tile * p.C;
+		size_t smem = sizeof(double) * (2 * nthr + 32);
+		if (p.tips_smem)
+			smem += (size_t)p.num_leaves * tile;
+		if (smem > 48 * 1024) {
+			const cudaError_t e = cudaFuncSetAttribute(
+				prune4_pair_kernel,
+				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess)
+				return e;
+		}
+		prune4_pair_kernel<<<grid, block, smem, s>>>(p);
+	} else {
+		const dim3 block(tile, p.C);
+		const size_t smem = sizeof(double) * (2 * (size_t)p.C * tile + 32);
+		if (f32) // more than 8 categories: one lane per column
+			prune4_kernel<V4f, true><<<grid, block, smem, s>>>(p);
+		else
+			prune4_kernel<V4d, false><<<grid, block, smem, s>>>(p);
+	}
 	return cudaGetLastError();
 }
 
