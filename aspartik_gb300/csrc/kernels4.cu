@@ -214,6 +214,20 @@ __device__ __forceinline__ void neumaier_add(double &sum, double &comp,
 	sum = t;
 }
 
+// Per-thread constants of the pruning walk.  Partial and scale elements of
+// slot `s` for this thread's (pattern, category) column sit at
+// s * stride + col; table rows of entry i start at (2i) * 5C + 5c.
+template <typename T, typename Idx> struct Walk {
+	T *partials;
+	int32_t *scales;
+	const T *ptab_c;        // ptab + 5c
+	const uint8_t *tips_p;  // tips + p (global) or the block's tile + pl
+	Idx stride;             // C * ldp
+	Idx col;                // c * ldp + p
+	uint32_t tip_row;       // ldp (global) or patterns per block (tile)
+	uint32_t row5c;         // 5C
+};
+
 // Inputs of one child of a node: a tip code, or a partial with the
 // cumulative rescale count of its subtree.
 template <typename T> struct ChildIn {
@@ -222,19 +236,17 @@ template <typename T> struct ChildIn {
 	uint32_t code;
 };
 
-template <typename T>
-__device__ __forceinline__ void load_child(const PruneParams &prm,
-					   const T *__restrict__ partials,
-					   uint32_t id, uint32_t p, uint32_t c,
+template <typename T, typename Idx>
+__device__ __forceinline__ void load_child(const Walk<T, Idx> &w, uint32_t id,
 					   ChildIn<T> &in)
 {
 	if (id & kTipBit) {
-		in.code = prm.tips[(size_t)(id & ~kTipBit) * prm.ldp + p];
+		in.code = w.tips_p[(Idx)(id & ~kTipBit) * w.tip_row];
 		in.s = 0;
 	} else {
-		const size_t ix = ((size_t)id * prm.C + c) * prm.ldp + p;
-		in.x = partials[ix];
-		in.s = prm.scales[ix];
+		const Idx ix = (Idx)id * w.stride + w.col;
+		in.x = w.partials[ix];
+		in.s = w.scales[ix];
 		in.code = 0;
 	}
 }
@@ -251,12 +263,11 @@ __device__ __forceinline__ T apply_child(uint32_t id, const T *__restrict__ pt,
 // U consecutive schedule entries that are mutually independent: every load
 // of the batch is issued before any product, so a thread keeps 2U child
 // partials in flight instead of 2.
-template <typename VT, bool kPow2, int U>
+template <typename VT, bool kPow2, int U, typename Idx>
 __device__ __forceinline__ void prune_batch(const PruneParams &prm,
-					    typename VT::T *__restrict__ partials,
-					    const typename VT::T *__restrict__ ptab,
-					    uint32_t i0, uint32_t p, uint32_t c,
-					    typename VT::T &y_out, int32_t &cnt_out)
+					    const Walk<typename VT::T, Idx> &w,
+					    uint32_t i0, typename VT::T &y_out,
+					    int32_t &cnt_out)
 {
 	typedef typename VT::T T;
 	NodeOp op[U];
@@ -264,14 +275,13 @@ __device__ __forceinline__ void prune_batch(const PruneParams &prm,
 #pragma unroll
 	for (int u = 0; u < U; ++u) {
 		op[u] = prm.ops[i0 + u];
-		load_child(prm, partials, op[u].left, p, c, l[u]);
-		load_child(prm, partials, op[u].right, p, c, r[u]);
+		load_child(w, op[u].left, l[u]);
+		load_child(w, op[u].right, r[u]);
 	}
 #pragma unroll
 	for (int u = 0; u < U; ++u) {
-		const uint32_t i = i0 + u;
-		const T *tl = ptab + ((size_t)(2 * i) * prm.C + c) * 5;
-		const T *tr = ptab + ((size_t)(2 * i + 1) * prm.C + c) * 5;
+		const T *tl = w.ptab_c + (2 * (i0 + u)) * w.row5c;
+		const T *tr = tl + w.row5c;
 		T y = v4_mul(apply_child(op[u].left, tl, l[u]),
 			     apply_child(op[u].right, tr, r[u]));
 		int32_t own;
@@ -285,9 +295,9 @@ __device__ __forceinline__ void prune_batch(const PruneParams &prm,
 							  prm.scale_mult);
 		}
 		const int32_t cnt = l[u].s + r[u].s + own;
-		const size_t ox = ((size_t)op[u].out * prm.C + c) * prm.ldp + p;
-		partials[ox] = y;
-		prm.scales[ox] = cnt;
+		const Idx ox = (Idx)op[u].out * w.stride + w.col;
+		w.partials[ox] = y;
+		w.scales[ox] = cnt;
 		y_out = y;
 		cnt_out = cnt;
 	}
@@ -433,184 +443,46 @@ __device__ __forceinline__ void finish_root(const PruneParams &prm, double *smem
 	}
 }
 
-// ---------------------------------------------------------------------------
-// FP32 chosen form, two lanes per (pattern, category) column.  Lane h of a
-// pair holds states 2h and 2h+1 of every partial; a child product needs the
-// partner's two states, one shfl.xor each.  This doubles the threads of the
-// one-lane layout (the kernel is latency-bound by occupancy) and halves the
-// registers per batched node.
-
-__device__ __forceinline__ float2 f2_apply(const float2 *__restrict__ pt,
-					   float2 x, uint32_t h)
-{
-	// pt[2k] = columns (2h, 2h+1) of row k of the transposed table
-	const float ox = __shfl_xor_sync(0xffffffffu, x.x, 1);
-	const float oy = __shfl_xor_sync(0xffffffffu, x.y, 1);
-	const float x0 = h ? ox : x.x, x1 = h ? oy : x.y;
-	const float x2 = h ? x.x : ox, x3 = h ? x.y : oy;
-	const float2 p0 = pt[0], p1 = pt[2], p2 = pt[4], p3 = pt[6];
-	float2 r;
-	r.x = x0 * p0.x;
-	r.y = x0 * p0.y;
-	r.x = fmaf(x1, p1.x, r.x);
-	r.y = fmaf(x1, p1.y, r.y);
-	r.x = fmaf(x2, p2.x, r.x);
-	r.y = fmaf(x2, p2.y, r.y);
-	r.x = fmaf(x3, p3.x, r.x);
-	r.y = fmaf(x3, p3.y, r.y);
-	return r;
-}
-
-// Power-of-two rescale of a pair's four states (see rescale_pow2).
-__device__ __forceinline__ int32_t rescale_pow2_pair(float2 &y)
-{
-	float m = fmaxf(y.x, y.y);
-	m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
-	int32_t shift = 0;
-	uint32_t ex = (__float_as_uint(m) >> 23) & 0xffu;
-	if (ex == 0u) {
-		if (!(m > 0.0f))
-			return 0;
-		const float lift = 18446744073709551616.0f; // 2^64, exact
-		y.x *= lift;
-		y.y *= lift;
-		m *= lift;
-		shift = -64;
-		ex = (__float_as_uint(m) >> 23) & 0xffu;
-	}
-	const int32_t e = (int32_t)ex - 127;
-	const float f = __uint_as_float((uint32_t)(127 - e) << 23);
-	y.x *= f;
-	y.y *= f;
-	return e + shift;
-}
-
-struct PairChild {
-	float2 x;
-	int32_t s;
-	uint32_t code;
-};
-
-__device__ __forceinline__ void load_pair_child(const PruneParams &prm,
-						const float2 *__restrict__ part2,
-						const uint8_t *__restrict__ s_tips,
-						uint32_t tp, uint32_t id, uint32_t p,
-						uint32_t pl, uint32_t c, uint32_t h,
-						PairChild &in)
-{
-	if (id & kTipBit) {
-		const uint32_t leaf = id & ~kTipBit;
-		in.code = s_tips ? s_tips[leaf * tp + pl]
-				 : prm.tips[(size_t)leaf * prm.ldp + p];
-		in.s = 0;
-	} else {
-		const size_t ix = ((size_t)id * prm.C + c) * prm.ldp + p;
-		in.x = part2[ix * 2 + h];
-		in.s = prm.scales[ix];
-		in.code = 0;
-	}
-}
-
-template <int U>
-__device__ __forceinline__ void prune_batch_pair(const PruneParams &prm,
-						 float2 *__restrict__ part2,
-						 const float2 *__restrict__ pt2,
-						 const uint8_t *__restrict__ s_tips,
-						 uint32_t tp, uint32_t i0, uint32_t p,
-						 uint32_t pl, uint32_t c, uint32_t h,
-						 float2 &y_out, int32_t &cnt_out)
-{
-	NodeOp op[U];
-	PairChild l[U], r[U];
-#pragma unroll
-	for (int u = 0; u < U; ++u) {
-		op[u] = prm.ops[i0 + u];
-		load_pair_child(prm, part2, s_tips, tp, op[u].left, p, pl, c, h, l[u]);
-		load_pair_child(prm, part2, s_tips, tp, op[u].right, p, pl, c, h, r[u]);
-	}
-#pragma unroll
-	for (int u = 0; u < U; ++u) {
-		const uint32_t i = i0 + u;
-		// table rows as float2 columns: [n][2][C][5 rows][2 halves]
-		const float2 *tl = pt2 + ((size_t)(2 * i) * prm.C + c) * 10 + h;
-		const float2 *tr = pt2 + ((size_t)(2 * i + 1) * prm.C + c) * 10 + h;
-		const float2 a = (op[u].left & kTipBit) ? tl[2 * l[u].code]
-							: f2_apply(tl, l[u].x, h);
-		const float2 b = (op[u].right & kTipBit) ? tr[2 * r[u].code]
-							 : f2_apply(tr, r[u].x, h);
-		float2 y;
-		y.x = a.x * b.x;
-		y.y = a.y * b.y;
-		const int32_t cnt = l[u].s + r[u].s + rescale_pow2_pair(y);
-		const size_t ox = ((size_t)op[u].out * prm.C + c) * prm.ldp + p;
-		part2[ox * 2 + h] = y;
-		if (h == 0)
-			prm.scales[ox] = cnt;
-		y_out = y;
-		cnt_out = cnt;
-	}
-}
-
-__global__ void __launch_bounds__(512) prune4_pair_kernel(PruneParams prm)
-{
-	const uint32_t tp = blockDim.x >> 1; // patterns per block
-	const uint32_t pl = threadIdx.x >> 1, h = threadIdx.x & 1u;
-	const uint32_t c = threadIdx.y;
-	const uint32_t p0 = blockIdx.x * tp;
-	const uint32_t p = p0 + pl;
-	float2 *__restrict__ part2 = (float2 *)prm.partials;
-	const float2 *__restrict__ pt2 = (const float2 *)prm.ptab;
-	const uint32_t nthr = blockDim.x * blockDim.y;
-	extern __shared__ double smem[];
-
-	// tip codes of this block's patterns for every leaf, staged once
-	const uint8_t *s_tips = nullptr;
-	if (prm.tips_smem) {
-		uint32_t *s_t32 = (uint32_t *)(smem + 2 * nthr + 32);
-		const uint32_t wpr = tp >> 2; // 4-byte words per leaf row
-		const uint32_t total = prm.num_leaves * wpr;
-		const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
-		for (uint32_t w = tid; w < total; w += nthr) {
-			const uint32_t leaf = w / wpr, col = w - leaf * wpr;
-			s_t32[w] = *(const uint32_t *)(prm.tips + (size_t)leaf * prm.ldp +
-						       p0 + col * 4);
-		}
-		__syncthreads();
-		s_tips = (const uint8_t *)s_t32;
-	}
-
-	float2 y = make_float2(0.f, 0.f);
-	int32_t cnt = 0;
-	for (uint32_t i = 0; i < prm.n;) {
-		const uint32_t avail = prm.ops[i].pad;
-		if (avail >= 4) {
-			prune_batch_pair<4>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
-			i += 4;
-		} else if (avail >= 2) {
-			prune_batch_pair<2>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
-			i += 2;
-		} else {
-			prune_batch_pair<1>(prm, part2, pt2, s_tips, tp, i, p, pl, c, h, y, cnt);
-			i += 1;
-		}
-	}
-	double root_dot = (double)prm.pi[2 * h] * (double)y.x +
-			  (double)prm.pi[2 * h + 1] * (double)y.y;
-	root_dot += __shfl_xor_sync(0xffffffffu, root_dot, 1);
-	finish_root<true>(prm, smem, tp, pl, p, c, h == 0, root_dot, cnt);
-}
-
-template <typename VT, bool kPow2>
+template <typename VT, bool kPow2, typename Idx>
 __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 {
 	typedef typename VT::T T;
 	typedef typename VT::R R;
 	const uint32_t tp = blockDim.x;
 	const uint32_t c = threadIdx.y;
-	const uint32_t p = blockIdx.x * tp + threadIdx.x;
-	const uint32_t ldp = prm.ldp, C = prm.C;
-	T *__restrict__ partials = (T *)prm.partials;
-	const T *__restrict__ ptab = (const T *)prm.ptab;
+	const uint32_t p0 = blockIdx.x * tp;
+	const uint32_t p = p0 + threadIdx.x;
+	const uint32_t nthr = blockDim.x * blockDim.y;
+	extern __shared__ double smem[];
+
+	Walk<T, Idx> w;
+	w.partials = (T *)prm.partials;
+	w.scales = prm.scales;
+	w.ptab_c = (const T *)prm.ptab + 5 * c;
+	w.stride = (Idx)prm.C * prm.ldp;
+	w.col = (Idx)c * prm.ldp + p;
+	w.row5c = 5 * prm.C;
+	if (prm.tips_smem) {
+		// the tip codes of this block's patterns for every leaf, staged
+		// once with 4-byte loads (rows are 16-byte aligned: ldp and p0 are
+		// multiples of 32)
+		uint32_t *s_t32 = (uint32_t *)(smem + 2 * nthr + 32);
+		const uint32_t wpr = tp >> 2;
+		const uint32_t total = prm.num_leaves * wpr;
+		const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+		for (uint32_t k = tid; k < total; k += nthr) {
+			const uint32_t leaf = k / wpr, col = k - leaf * wpr;
+			s_t32[k] = *(const uint32_t *)(prm.tips +
+						       (size_t)leaf * prm.ldp +
+						       p0 + col * 4);
+		}
+		__syncthreads();
+		w.tips_p = (const uint8_t *)s_t32 + threadIdx.x;
+		w.tip_row = tp;
+	} else {
+		w.tips_p = prm.tips + p;
+		w.tip_row = prm.ldp;
+	}
 
 	// The schedule is split on the host into runs of mutually independent
 	// entries; NodeOp::pad of an entry is the number of entries left in its
@@ -622,13 +494,13 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 		// FP64 partials take twice the registers: batches of at most 2
 		constexpr uint32_t kMaxU = sizeof(R) == 4 ? 4u : 2u;
 		if (kMaxU >= 4 && avail >= 4) {
-			prune_batch<VT, kPow2, 4>(prm, partials, ptab, i, p, c, y, cnt);
+			prune_batch<VT, kPow2, 4, Idx>(prm, w, i, y, cnt);
 			i += 4;
 		} else if (avail >= 2) {
-			prune_batch<VT, kPow2, 2>(prm, partials, ptab, i, p, c, y, cnt);
+			prune_batch<VT, kPow2, 2, Idx>(prm, w, i, y, cnt);
 			i += 2;
 		} else {
-			prune_batch<VT, kPow2, 1>(prm, partials, ptab, i, p, c, y, cnt);
+			prune_batch<VT, kPow2, 1, Idx>(prm, w, i, y, cnt);
 			i += 1;
 		}
 	}
@@ -637,7 +509,6 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 				(double)prm.pi[1] * (double)y.y +
 				(double)prm.pi[2] * (double)y.z +
 				(double)prm.pi[3] * (double)y.w;
-	extern __shared__ double smem[];
 	finish_root<kPow2>(prm, smem, tp, threadIdx.x, p, c, true, root_dot, cnt);
 }
 
@@ -750,34 +621,35 @@ cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
 	return cudaGetLastError();
 }
 
+template <typename VT, bool kPow2>
+static cudaError_t launch_prune4_t(const PruneParams &p, uint32_t tile,
+				   cudaStream_t s)
+{
+	const dim3 grid(p.ldp / tile);
+	const dim3 block(tile, p.C);
+	size_t smem = sizeof(double) * (2 * (size_t)p.C * tile + 32);
+	if (p.tips_smem)
+		smem += (size_t)p.num_leaves * tile;
+	// 32-bit element indices when every slot index fits
+	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
+	auto kern = narrow ? prune4_kernel<VT, kPow2, uint32_t>
+			   : prune4_kernel<VT, kPow2, size_t>;
+	if (smem > 48 * 1024) {
+		const cudaError_t e = cudaFuncSetAttribute(
+			kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess)
+			return e;
+	}
+	kern<<<grid, block, smem, s>>>(p);
+	return cudaGetLastError();
+}
+
 cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 			  cudaStream_t s)
 {
-	const dim3 grid(p.ldp / tile);
-	if (f32 && 2 * tile * p.C <= 512) {
-		// two lanes per (pattern, category) column
-		const dim3 block(2 * tile, p.C);
-		const size_t nthr = 2 * (size_t)tile * p.C;
-		size_t smem = sizeof(double) * (2 * nthr + 32);
-		if (p.tips_smem)
-			smem += (size_t)p.num_leaves * tile;
-		if (smem > 48 * 1024) {
-			const cudaError_t e = cudaFuncSetAttribute(
-				prune4_pair_kernel,
-				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-			if (e != cudaSuccess)
-				return e;
-		}
-		prune4_pair_kernel<<<grid, block, smem, s>>>(p);
-	} else {
-		const dim3 block(tile, p.C);
-		const size_t smem = sizeof(double) * (2 * (size_t)p.C * tile + 32);
-		if (f32) // more than 8 categories: one lane per column
-			prune4_kernel<V4f, true><<<grid, block, smem, s>>>(p);
-		else
-			prune4_kernel<V4d, false><<<grid, block, smem, s>>>(p);
-	}
-	return cudaGetLastError();
+	if (f32)
+		return launch_prune4_t<V4f, true>(p, tile, s);
+	return launch_prune4_t<V4d, false>(p, tile, s);
 }
 
 cudaError_t launch_eigen(ModelDev *model, cudaStream_t s)
