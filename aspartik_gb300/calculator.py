@@ -186,6 +186,12 @@ class GpuCalculator:
                                                ct.byref(p), ct.byref(n)))
         return t.value, p.value, int(n.value)
 
+    def last_upload_bytes(self) -> int:
+        """Bytes the last proposal copied host -> device."""
+        n = ct.c_uint64()
+        check(lib.b3g_calculator_last_upload_bytes(self._h, ct.byref(n)))
+        return int(n.value)
+
     def span_begin(self) -> None:
         check(lib.b3g_calculator_span_begin(self._h))
 

@@ -77,6 +77,11 @@ struct PruneParams {
 	uint32_t scale_ln;
 	uint32_t num_leaves; // rows of tips
 	uint32_t tips_smem;  // stage the block's tip codes in shared memory
+	// run-synchronous walk (prune4_runs_kernel): runs[0..n_runs] are the
+	// first entries of the runs of mutually independent entries, then n
+	const uint32_t *runs;
+	uint32_t n_runs;
+	uint32_t tile; // patterns per tile
 	double scale_threshold;
 	double scale_mult;
 	double log_inv_c;
@@ -86,6 +91,10 @@ struct PruneParams {
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);
 cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 			  cudaStream_t s);
+// Run-synchronous FP32 walk: `ctas` persistent blocks over ldp / p.tile
+// pattern tiles.  Needs p.runs; block sums sized for `ctas`.
+cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
+			       cudaStream_t s);
 cudaError_t launch_eigen(ModelDev *model, cudaStream_t s);
 
 } // namespace b3g

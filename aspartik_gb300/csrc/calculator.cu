@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <cstdlib>
 #include <new>
 
 namespace b3g {
@@ -96,6 +97,22 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	if (device_ < 0 || device_ >= ndev)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "no such CUDA device");
 	DeviceGuard g(device_);
+	int sms = 0;
+	check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
+					  device_),
+		   "SM count");
+	num_sms_ = static_cast<uint32_t>(sms);
+	// run-synchronous FP32 walk: 64 patterns x C categories per tile while
+	// a tile's columns fit one 512-thread block
+	runs_tile_ = 64;
+	while (runs_tile_ > 32 && runs_tile_ * C_ > 512)
+		runs_tile_ >>= 1;
+	if (const char *env = std::getenv("B3G_RUNS_TILE")) {
+		const uint32_t t = static_cast<uint32_t>(std::atoi(env));
+		if (t == 32 || t == 64 || t == 128)
+			runs_tile_ = t;
+	}
+	use_runs_ = f32_ && runs_tile_ * C_ <= 512;
 
 	selectors_.assign(I_, 0);
 	stamp_.assign(2 * L_ - 1, 0);
@@ -104,7 +121,9 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 
 	const size_t slots = 2ull * I_;
 	const size_t rsz = f32_ ? sizeof(float) : sizeof(double);
-	const size_t nblocks = ldp_ / tile_;
+	// one block sum per thread block of either walk: at most one block
+	// per 32 patterns
+	const size_t nblocks = ldp_ / 32;
 
 	try {
 		check_cuda(cudaStreamCreateWithFlags(&stream_,
@@ -138,7 +157,8 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 			  "transition tables");
 
 		off_pi_ = align_up((size_t)I_ * sizeof(NodeOp), 256);
-		off_in_ = align_up(off_pi_ + S_ * sizeof(double), 256);
+		off_runs_ = align_up(off_pi_ + S_ * sizeof(double), 256);
+		off_in_ = align_up(off_runs_ + (size_t)(I_ + 1) * sizeof(uint32_t), 256);
 		stage_bytes_ = off_in_ + (size_t)I_ * 2 * C_ * S_ * S_ * sizeof(double);
 		dev_alloc(d_stage_, stage_bytes_, "stage");
 		check_cuda(cudaHostAlloc((void **)&h_stage_, stage_bytes_,
@@ -341,6 +361,13 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 		ops[i].pad = (i + 1 < n && run_of_[i + 1] == run_of_[i])
 				     ? ops[i + 1].pad + 1
 				     : 1;
+	// run starts, then n
+	uint32_t *runs = reinterpret_cast<uint32_t *>(h_stage_ + off_runs_);
+	n_runs_ = 0;
+	for (uint32_t i = 0; i < n; ++i)
+		if (run_of_[i] == i)
+			runs[n_runs_++] = i;
+	runs[n_runs_] = n;
 }
 
 void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
@@ -349,7 +376,8 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	const size_t in_bytes =
 		matrices_mode ? (size_t)n * 2 * C_ * S_ * S_ * sizeof(double)
 			      : (size_t)n * 2 * sizeof(double);
-	check_cuda(cudaMemcpyAsync(d_stage_, h_stage_, off_in_ + in_bytes,
+	last_upload_bytes_ = off_in_ + in_bytes;
+	check_cuda(cudaMemcpyAsync(d_stage_, h_stage_, last_upload_bytes_,
 				   cudaMemcpyHostToDevice, stream_),
 		   "upload step");
 	check_cuda(cudaEventRecord(ev_stage_free_, stream_), "event");
@@ -400,7 +428,16 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
 	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
-	check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
+	if (use_runs_) {
+		pp.runs = reinterpret_cast<const uint32_t *>(d_stage_ + off_runs_);
+		pp.n_runs = n_runs_;
+		pp.tile = runs_tile_;
+		const uint32_t tiles = ldp_ / runs_tile_;
+		const uint32_t ctas = std::min(tiles, 2 * num_sms_);
+		check_cuda(launch_prune4_runs(pp, ctas, stream_), "pruning kernel");
+	} else {
+		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
+	}
 	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
 	slot.pending = true;
 	++ring_next_;
@@ -864,6 +901,16 @@ B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
 		calc_of(calc)->timing_totals(reset != 0, transition_ms, prune_ms,
 					     proposals);
+	});
+}
+
+B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
+						    uint64_t *bytes)
+{
+	return guarded([&] {
+		if (!bytes)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*bytes = calc_of(calc)->last_upload_bytes();
 	});
 }
 

@@ -68,6 +68,7 @@ class Calculator {
 			   uint64_t *proposals);
 	void span_begin();
 	float span_end();
+	uint64_t last_upload_bytes() const { return last_upload_bytes_; }
 
       private:
 	void validate_lists(const uint32_t *internals,
@@ -133,7 +134,12 @@ class Calculator {
 	ModelDev *h_model_ = nullptr;
 	double *h_lnl_ = nullptr;
 	size_t stage_bytes_ = 0;
-	size_t off_pi_ = 0, off_in_ = 0;
+	size_t off_pi_ = 0, off_runs_ = 0, off_in_ = 0;
+	uint32_t n_runs_ = 0;
+	uint64_t last_upload_bytes_ = 0;
+	uint32_t num_sms_ = 1;
+	uint32_t runs_tile_ = 64;
+	bool use_runs_ = false;
 };
 
 } // namespace b3g

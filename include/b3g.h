@@ -185,6 +185,10 @@ B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
 						double *transition_ms,
 						double *prune_ms,
 						uint64_t *proposals);
+/* Bytes the last proposal copied host -> device (its staged dirty list,
+ * schedule runs, frequencies and lengths or matrices). */
+B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
+						    uint64_t *bytes);
 /* Device time between two markers on the calculator's stream: span_begin
  * records the first, span_end records the second, waits and returns the
  * elapsed milliseconds. */
