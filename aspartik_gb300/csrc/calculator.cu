@@ -428,10 +428,16 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
 	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
-	if (use_runs_) {
+	// the run-synchronous walk stages the schedule in shared memory: keep
+	// it for lists up to 4,096 entries
+	if (use_runs_ && n <= 4096) {
 		pp.runs = reinterpret_cast<const uint32_t *>(d_stage_ + off_runs_);
 		pp.n_runs = n_runs_;
 		pp.tile = runs_tile_;
+		pp.tips_smem = (4ull * tip_children_ >= L_ &&
+				(size_t)L_ * runs_tile_ <= 32u * 1024u)
+				       ? 1u
+				       : 0u;
 		const uint32_t tiles = ldp_ / runs_tile_;
 		const uint32_t ctas = std::min(tiles, 2 * num_sms_);
 		check_cuda(launch_prune4_runs(pp, ctas, stream_), "pruning kernel");

@@ -529,21 +529,27 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 // group g; the block has cols * groups threads and group g handles entries
 // g, g + groups, ... of every run.
 
+// Tip codes come from the block's shared-memory tile (tip_row = tile) or
+// from global memory (tips_p = tips + p, tip_row = ldp); the schedule from
+// shared memory.
 template <typename Idx>
 __device__ __forceinline__ void run_item(const PruneParams &prm,
+					 const NodeOp *__restrict__ ops,
+					 const uint8_t *__restrict__ tips_p,
+					 uint32_t tip_row,
 					 const float4 *__restrict__ ptab,
 					 float4 *__restrict__ part,
 					 int32_t *__restrict__ scales, Idx stride,
-					 Idx col_off, uint32_t c, uint32_t p,
-					 uint32_t i, float4 &y, int32_t &cnt)
+					 Idx col_off, uint32_t c, uint32_t i,
+					 float4 &y, int32_t &cnt)
 {
-	const NodeOp op = prm.ops[i];
+	const NodeOp op = ops[i];
 	const float4 *tl = ptab + ((size_t)(2 * i) * prm.C + c) * 5;
 	const float4 *tr = tl + 5 * prm.C;
 	float4 a, b;
 	int32_t sa = 0, sb = 0;
 	if (op.left & kTipBit) {
-		a = tl[prm.tips[(Idx)(op.left & ~kTipBit) * prm.ldp + p]];
+		a = tl[tips_p[(Idx)(op.left & ~kTipBit) * tip_row]];
 	} else {
 		const Idx ix = (Idx)op.left * stride + col_off;
 		const float4 x = part[ix];
@@ -551,7 +557,7 @@ __device__ __forceinline__ void run_item(const PruneParams &prm,
 		a = v4_apply(tl, x);
 	}
 	if (op.right & kTipBit) {
-		b = tr[prm.tips[(Idx)(op.right & ~kTipBit) * prm.ldp + p]];
+		b = tr[tips_p[(Idx)(op.right & ~kTipBit) * tip_row]];
 	} else {
 		const Idx ix = (Idx)op.right * stride + col_off;
 		const float4 x = part[ix];
@@ -583,25 +589,56 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	extern __shared__ double smem[];
 	double *s_dot = smem;                        // [cols] root pi . x
 	int32_t *s_cnt = (int32_t *)(smem + cols);   // [cols] root exponents
-	double *s_red = smem + cols + (cols + 1) / 2; // [blockDim.x] reductions
+	double *s_red = smem + cols + (cols + 1) / 2; // [2 * blockDim.x]
+	// schedule and run starts, staged once per block
+	NodeOp *s_ops = (NodeOp *)(s_red + 2 * blockDim.x);  // [n]
+	uint32_t *s_runs = (uint32_t *)(s_ops + prm.n);     // [n_runs + 1]
+	// tip codes of the current tile for every leaf: [L][tile]
+	uint8_t *s_tips = (uint8_t *)(s_runs + ((prm.n_runs + 4) & ~3u));
 	__shared__ unsigned s_last;
+
+	for (uint32_t k = tid; k < prm.n; k += blockDim.x)
+		s_ops[k] = prm.ops[k];
+	for (uint32_t k = tid; k <= prm.n_runs; k += blockDim.x)
+		s_runs[k] = prm.runs[k];
 
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
 
 	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 		const uint32_t p = t * tile + pl;
 		const Idx col_off = (Idx)c * prm.ldp + p;
+		const uint8_t *tips_p;
+		uint32_t tip_row;
+		if (prm.tips_smem) {
+			// 4-byte loads: rows start at multiples of 32 patterns
+			const uint32_t wpr = tile >> 2;
+			const uint32_t total = prm.num_leaves * wpr;
+			uint32_t *s_t32 = (uint32_t *)s_tips;
+			for (uint32_t k = tid; k < total; k += blockDim.x) {
+				const uint32_t leaf = k / wpr, w4 = k - leaf * wpr;
+				s_t32[k] = *(const uint32_t *)(prm.tips +
+							       (size_t)leaf * prm.ldp +
+							       t * tile + w4 * 4);
+			}
+			tips_p = s_tips + pl;
+			tip_row = tile;
+		} else {
+			tips_p = prm.tips + p;
+			tip_row = prm.ldp;
+		}
+		__syncthreads();
 		for (uint32_t r = 0; r < prm.n_runs; ++r) {
-			const uint32_t start = prm.runs[r], end = prm.runs[r + 1];
+			const uint32_t start = s_runs[r], end = s_runs[r + 1];
 			uint32_t i = start + g;
 			// two independent entries per iteration: all their loads
 			// are issued before either product
 			for (; i + groups < end; i += 2 * groups) {
 				float4 y0, y1;
 				int32_t c0, c1;
-				run_item(prm, ptab, part, scales, stride, col_off, c, p, i, y0, c0);
-				run_item(prm, ptab, part, scales, stride, col_off, c, p,
-					 i + groups, y1, c1);
+				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
+					 stride, col_off, c, i, y0, c0);
+				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
+					 stride, col_off, c, i + groups, y1, c1);
 				if (i + groups == prm.n - 1) {
 					s_dot[col] = (double)prm.pi[0] * y1.x + (double)prm.pi[1] * y1.y +
 						     (double)prm.pi[2] * y1.z + (double)prm.pi[3] * y1.w;
@@ -611,7 +648,8 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 			if (i < end) {
 				float4 y0;
 				int32_t c0;
-				run_item(prm, ptab, part, scales, stride, col_off, c, p, i, y0, c0);
+				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
+					 stride, col_off, c, i, y0, c0);
 				if (i == prm.n - 1) {
 					s_dot[col] = (double)prm.pi[0] * y0.x + (double)prm.pi[1] * y0.y +
 						     (double)prm.pi[2] * y0.z + (double)prm.pi[3] * y0.w;
@@ -851,13 +889,19 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 	if (cols > 512)
 		return cudaErrorInvalidValue;
 	const uint32_t threads = cols * (512 / cols);
-	const size_t smem =
-		sizeof(double) * (cols + (cols + 1) / 2 + 2 * (size_t)threads);
+	size_t smem = sizeof(double) * (cols + (cols + 1) / 2 + 2 * (size_t)threads) +
+		      sizeof(NodeOp) * p.n + sizeof(uint32_t) * ((p.n_runs + 4) & ~3u);
+	if (p.tips_smem)
+		smem += (size_t)p.num_leaves * p.tile;
 	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
-	if (narrow)
-		prune4_runs_kernel<uint32_t><<<ctas, threads, smem, s>>>(p);
-	else
-		prune4_runs_kernel<size_t><<<ctas, threads, smem, s>>>(p);
+	auto kern = narrow ? prune4_runs_kernel<uint32_t> : prune4_runs_kernel<size_t>;
+	if (smem > 48 * 1024) {
+		const cudaError_t e = cudaFuncSetAttribute(
+			kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess)
+			return e;
+	}
+	kern<<<ctas, threads, smem, s>>>(p);
 	return cudaGetLastError();
 }
 
