@@ -79,6 +79,27 @@ class PruneBuffers(ct.Structure):
     ]
 
 
+OP_COUNT = 8
+
+
+class McmcConfig(ct.Structure):
+    """b3g_mcmc_config."""
+
+    _fields_ = [
+        ("num_chains", ct.c_uint32),
+        ("num_categories", ct.c_uint32),
+        ("precision", ct.c_uint32),
+        ("model", ct.c_uint32),
+        ("seed", ct.c_uint64),
+        ("heat", ct.c_double),
+        ("swap_every", ct.c_uint32),
+        ("sample_every", ct.c_uint32),
+        ("tune_every", ct.c_uint32),
+        ("device", ct.c_int32),
+        ("op_weights", ct.c_double * OP_COUNT),
+    ]
+
+
 NOALLOC_MAX_BLOCKS = 16384
 TIP = 0x80000000
 
@@ -115,6 +136,18 @@ SIGNATURES = {
     "b3g_calculator_span_begin": (ct.c_int, [_vp]),
     "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
     "b3g_prune_noalloc": (ct.c_int, [ct.POINTER(PruneBuffers), _vp]),
+    "b3g_mcmc_create": (ct.c_int, [ct.POINTER(McmcConfig), ct.c_uint32, ct.c_uint32, _u8p,
+                                   _u32p, _u32p, _f64p, ct.POINTER(_vp)]),
+    "b3g_mcmc_destroy": (None, [_vp]),
+    "b3g_mcmc_set_parameters": (ct.c_int, [_vp, ct.c_double, _f64p, _f64p, ct.c_double,
+                                           ct.c_double]),
+    "b3g_mcmc_run": (ct.c_int, [_vp, ct.c_uint64]),
+    "b3g_mcmc_trace": (ct.c_int, [_vp, ct.c_uint32, _f64p, ct.c_uint64,
+                                  ct.POINTER(ct.c_uint64)]),
+    "b3g_mcmc_operator_stats": (ct.c_int, [_vp, ct.c_uint32, ct.POINTER(ct.c_uint64), _f64p]),
+    "b3g_mcmc_swaps": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
+    "b3g_mcmc_check": (ct.c_int, [_vp, _f64p]),
+    "b3g_mcmc_chain_state": (ct.c_int, [_vp, ct.c_uint32, _u32p, _f64p, _f64p, _f64p]),
 }
 
 

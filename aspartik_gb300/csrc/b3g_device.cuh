@@ -95,6 +95,6 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 // pattern tiles.  Needs p.runs; block sums sized for `ctas`.
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			       cudaStream_t s);
-cudaError_t launch_eigen(ModelDev *model, cudaStream_t s);
+cudaError_t launch_eigen(ModelDev *model, uint32_t states, cudaStream_t s);
 
 } // namespace b3g

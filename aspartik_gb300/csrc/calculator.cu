@@ -671,7 +671,7 @@ void Calculator::set_reversible(const double *rates, const double *pi,
 	std::memcpy(model_host_.pi, pi, S_ * sizeof(double));
 	model_host_.shortcuts = shortcuts ? 1u : 0u;
 	upload_model();
-	check_cuda(launch_eigen(d_model_, stream_), "eigen kernel");
+	check_cuda(launch_eigen(d_model_, S_, stream_), "eigen kernel");
 	// the host copy of the decomposition is not needed: the device keeps
 	// V, V^-1, lambda and Q; pi is mirrored for the root reduction
 	model_set_ = true;

@@ -114,6 +114,39 @@ double gamma_quantile(double a, double p)
 	return x;
 }
 
+void hky_eigen(double kappa, const double *pi, double *V, double *Vinv,
+	       double *lambda, double *Q)
+{
+	const double a = pi[0], c = pi[1], g = pi[2], t = pi[3];
+	const double r = a + g, y = c + t;
+	// unnormalised off-diagonal rates, rows A C G T
+	const double q[16] = {0.0,       c,         kappa * g, t,
+			      a,         0.0,       g,         kappa * t,
+			      kappa * a, c,         0.0,       t,
+			      a,         kappa * c, g,         0.0};
+	const double div = 2.0 * (g * t + a * c + a * t + c * g +
+				  kappa * (a * g + c * t));
+	for (int i = 0; i < 4; ++i) {
+		const double rs = q[i * 4] + q[i * 4 + 1] + q[i * 4 + 2] + q[i * 4 + 3];
+		for (int j = 0; j < 4; ++j)
+			Q[i * 4 + j] = (i == j ? -rs : q[i * 4 + j]) / div;
+	}
+	const double v[16] = {1.0, -y / r, -g / a, 0.0,    1.0, 1.0, 0.0, -t / c,
+			      1.0, -y / r, 1.0,    0.0,    1.0, 1.0, 0.0, 1.0};
+	const double vi[16] = {a,      c,          g,     t,
+			       -a,     c * r / y,  -g,    t * r / y,
+			       -a / r, 0.0,        a / r, 0.0,
+			       0.0,    -c / y,     0.0,   c / y};
+	for (int k = 0; k < 16; ++k) {
+		V[k] = v[k];
+		Vinv[k] = vi[k];
+	}
+	lambda[0] = 0.0;
+	lambda[1] = -1.0 / div;
+	lambda[2] = -(y + r * kappa) / div;
+	lambda[3] = -(r + y * kappa) / div;
+}
+
 void gamma_categories(double alpha, int k, double *rates)
 {
 	double sum = 0.0;

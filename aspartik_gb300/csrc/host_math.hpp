@@ -9,4 +9,9 @@ double gamma_quantile(double a, double p);
 // (crates/b3/src/likelihood/gamma.rs:205-225).
 void gamma_categories(double alpha, int k, double *rates);
 
+// Analytic HKY eigensystem and normalised Q, all 4x4 row-major
+// (HKY::update_matrices, crates/b3/src/substitution.rs:336-388).
+void hky_eigen(double kappa, const double *pi, double *V, double *Vinv,
+	       double *lambda, double *Q);
+
 } // namespace b3g

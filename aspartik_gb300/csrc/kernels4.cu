@@ -743,97 +743,154 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 }
 
 // ---------------------------------------------------------------------------
-// eigensystem of a reversible Q (FP64, one thread; run when the model
-// changes, not per step).  Cyclic Jacobi (Golub & Van Loan, Matrix
-// Computations, sec. 8.5) on B = D^1/2 Q D^-1/2, D = diag(pi).
+// Eigensystem of a reversible Q (FP64; run when the model changes, not per
+// step).  Parallel cyclic Jacobi on the symmetric B = D^1/2 Q D^-1/2,
+// D = diag(pi): in every round the indices form disjoint pairs in the
+// round-robin ("chess tournament") order of Brent and Luk, all pairs are
+// rotated at once (disjoint rotations commute), and one thread owns one
+// element of B and of the accumulated rotations U.  Then Q = V L V^-1 with
+// V = D^-1/2 U and V^-1 = U^T D^1/2.  One block of m x m threads, m = n
+// rounded up to even (the extra index is a dummy that never rotates).
 
-__global__ void eigen_kernel(ModelDev *m)
+constexpr int kEigMax = kMaxStates; // even
+
+__global__ void __launch_bounds__(kEigMax *kEigMax) eigen_kernel(ModelDev *mdl)
 {
-	if (threadIdx.x != 0 || blockIdx.x != 0)
-		return;
-	const int n = (int)m->states;
-	double Q[kMaxStates * kMaxStates];
-	double B[kMaxStates * kMaxStates];
-	double U[kMaxStates * kMaxStates];
-	double sq[kMaxStates];
-	int k = 0;
-	for (int i = 0; i < n; i++)
-		Q[i * n + i] = 0.0;
-	for (int i = 0; i < n; i++)
-		for (int j = i + 1; j < n; j++, k++) {
-			Q[i * n + j] = m->rates_in[k] * m->pi_in[j];
-			Q[j * n + i] = m->rates_in[k] * m->pi_in[i];
-		}
-	double scale = 0.0;
-	for (int i = 0; i < n; i++) {
-		double s = 0.0;
-		for (int j = 0; j < n; j++)
-			if (j != i)
-				s += Q[i * n + j];
-		Q[i * n + i] = -s;
-		scale += s * m->pi_in[i];
-	}
-	for (int i = 0; i < n * n; i++)
-		Q[i] /= scale;
-	for (int i = 0; i < n; i++)
-		sq[i] = sqrt(m->pi_in[i]);
-	for (int i = 0; i < n; i++)
-		for (int j = 0; j < n; j++) {
-			const double bij = Q[i * n + j] * sq[i] / sq[j];
-			const double bji = Q[j * n + i] * sq[j] / sq[i];
-			B[i * n + j] = 0.5 * (bij + bji);
-			U[i * n + j] = i == j ? 1.0 : 0.0;
-		}
-	int sweep;
-	for (sweep = 0; sweep < 64; sweep++) {
-		double off = 0.0, tot = 0.0;
-		for (int i = 0; i < n * n; i++) {
-			tot += B[i] * B[i];
-			if (i / n != i % n)
-				off += B[i] * B[i];
-		}
-		if (off <= 1e-34 * tot)
-			break;
-		for (int p = 0; p < n - 1; p++)
-			for (int q = p + 1; q < n; q++) {
-				const double apq = B[p * n + q];
-				if (apq == 0.0)
-					continue;
-				const double theta =
-					(B[q * n + q] - B[p * n + p]) / (2.0 * apq);
-				const double t =
-					(theta >= 0.0 ? 1.0 : -1.0) /
-					(fabs(theta) + sqrt(theta * theta + 1.0));
-				const double cs = 1.0 / sqrt(t * t + 1.0);
-				const double sn = t * cs;
-				for (int r = 0; r < n; r++) {
-					const double bp = B[r * n + p], bq = B[r * n + q];
-					B[r * n + p] = cs * bp - sn * bq;
-					B[r * n + q] = sn * bp + cs * bq;
-				}
-				for (int r = 0; r < n; r++) {
-					const double bp = B[p * n + r], bq = B[q * n + r];
-					B[p * n + r] = cs * bp - sn * bq;
-					B[q * n + r] = sn * bp + cs * bq;
-				}
-				for (int r = 0; r < n; r++) {
-					const double up = U[r * n + p], uq = U[r * n + q];
-					U[r * n + p] = cs * up - sn * uq;
-					U[r * n + q] = sn * up + cs * uq;
-				}
+	__shared__ double B[kEigMax][kEigMax + 1];
+	__shared__ double U[kEigMax][kEigMax + 1];
+	__shared__ double Qs[kEigMax][kEigMax];
+	__shared__ double cs[kEigMax], sn[kEigMax], sq[kEigMax];
+	__shared__ int partner[kEigMax], order[kEigMax];
+	__shared__ double s_off, s_tot;
+
+	const int n = (int)mdl->states;
+	const int m = (n + 1) & ~1;
+	const int i = threadIdx.y, j = threadIdx.x; // element (i, j)
+	const bool live = i < n && j < n;
+	const int tid = i * blockDim.x + j;
+
+	// Q_ij = r_ij pi_j, rows summing to zero, normalised to mean rate 1
+	if (tid == 0) {
+		int k = 0;
+		for (int a = 0; a < n; a++) {
+			Qs[a][a] = 0.0;
+			for (int b = a + 1; b < n; b++, k++) {
+				Qs[a][b] = mdl->rates_in[k] * mdl->pi_in[b];
+				Qs[b][a] = mdl->rates_in[k] * mdl->pi_in[a];
 			}
+		}
+		double scale = 0.0;
+		for (int a = 0; a < n; a++) {
+			double rsum = 0.0;
+			for (int b = 0; b < n; b++)
+				if (b != a)
+					rsum += Qs[a][b];
+			Qs[a][a] = -rsum;
+			scale += rsum * mdl->pi_in[a];
+		}
+		for (int a = 0; a < n; a++) {
+			sq[a] = sqrt(mdl->pi_in[a]);
+			for (int b = 0; b < n; b++)
+				Qs[a][b] /= scale;
+		}
+		for (int a = 0; a < m; a++)
+			order[a] = a;
 	}
-	for (int i = 0; i < n; i++) {
-		m->lambda[i] = B[i * n + i];
-		m->pi[i] = m->pi_in[i];
-		for (int j = 0; j < n; j++) {
-			m->V[i * n + j] = U[i * n + j] / sq[i];
-			m->Vinv[j * n + i] = U[i * n + j] * sq[i];
-			m->Q[i * n + j] = Q[i * n + j];
+	__syncthreads();
+	if (i < m && j < m) {
+		double b = 0.0;
+		if (live)
+			b = 0.5 * (Qs[i][j] * sq[i] / sq[j] + Qs[j][i] * sq[j] / sq[i]);
+		B[i][j] = b;
+		U[i][j] = i == j ? 1.0 : 0.0;
+	}
+	__syncthreads();
+
+	int sweep = 0;
+	for (; sweep < 40; ++sweep) {
+		// off-diagonal and total squared norms, summed in a fixed order
+		if (tid == 0) {
+			double off = 0.0, tot = 0.0;
+			for (int a = 0; a < n; a++)
+				for (int b = 0; b < n; b++) {
+					const double b2 = B[a][b] * B[a][b];
+					tot += b2;
+					if (a != b)
+						off += b2;
+				}
+			s_off = off;
+			s_tot = tot;
+		}
+		__syncthreads();
+		if (s_off <= 1e-34 * s_tot)
+			break;
+		for (int round = 0; round < m - 1; ++round) {
+			// rotation of every pair of this round, by thread (k, 0)
+			if (j == 0 && i < m / 2) {
+				int p = order[i], q = order[m - 1 - i];
+				if (p > q) {
+					const int t = p;
+					p = q;
+					q = t;
+				}
+				double c = 1.0, s = 0.0;
+				const double apq = B[p][q];
+				if (q < n && apq != 0.0) {
+					const double theta = (B[q][q] - B[p][p]) / (2.0 * apq);
+					const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+							 (fabs(theta) + sqrt(theta * theta + 1.0));
+					c = 1.0 / sqrt(t * t + 1.0);
+					s = t * c;
+				}
+				// new row/column k = c * k + coef * partner
+				partner[p] = q;
+				partner[q] = p;
+				cs[p] = c;
+				cs[q] = c;
+				sn[p] = -s;
+				sn[q] = s;
+			}
+			__syncthreads();
+			double rb = 0.0;
+			if (i < m && j < m)
+				rb = cs[i] * B[i][j] + sn[i] * B[partner[i]][j];
+			__syncthreads();
+			if (i < m && j < m)
+				B[i][j] = rb;
+			__syncthreads();
+			double cb = 0.0, cu = 0.0;
+			if (i < m && j < m) {
+				cb = cs[j] * B[i][j] + sn[j] * B[i][partner[j]];
+				cu = cs[j] * U[i][j] + sn[j] * U[i][partner[j]];
+			}
+			__syncthreads();
+			if (i < m && j < m) {
+				B[i][j] = cb;
+				U[i][j] = cu;
+			}
+			// next round: keep order[0], rotate order[1..m-1]
+			if (tid == 0) {
+				const int last = order[m - 1];
+				for (int a = m - 1; a > 1; --a)
+					order[a] = order[a - 1];
+				order[1] = last;
+			}
+			__syncthreads();
 		}
 	}
-	m->jacobi_sweeps = (uint32_t)sweep;
-	m->status = sweep < 64 ? 0u : 1u;
+	if (live) {
+		if (i == j)
+			mdl->lambda[i] = B[i][i];
+		mdl->V[i * n + j] = U[i][j] / sq[i];
+		mdl->Vinv[j * n + i] = U[i][j] * sq[i];
+		mdl->Q[i * n + j] = Qs[i][j];
+	}
+	if (tid == 0) {
+		for (int a = 0; a < n; a++)
+			mdl->pi[a] = mdl->pi_in[a];
+		mdl->jacobi_sweeps = (uint32_t)sweep;
+		mdl->status = sweep < 40 ? 0u : 1u;
+	}
 }
 
 } // namespace
@@ -905,9 +962,10 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 	return cudaGetLastError();
 }
 
-cudaError_t launch_eigen(ModelDev *model, cudaStream_t s)
+cudaError_t launch_eigen(ModelDev *model, uint32_t states, cudaStream_t s)
 {
-	eigen_kernel<<<1, 32, 0, s>>>(model);
+	const uint32_t m = (states + 1) & ~1u;
+	eigen_kernel<<<1, dim3(m, m), 0, s>>>(model);
 	return cudaGetLastError();
 }
 

@@ -1,0 +1,581 @@
+// mcmc.cpp -- native MCMC driver (see mcmc.hpp).
+#include "mcmc.hpp"
+#include "host_math.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+namespace b3g {
+
+// ---------------------------------------------------------------------------
+// RNG
+
+namespace {
+
+uint64_t splitmix64(uint64_t &x)
+{
+	uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+const double kNegInf = -std::numeric_limits<double>::infinity();
+
+double lognormal_lnpdf(double x, double mu, double sigma)
+{
+	if (!(x > 0.0))
+		return kNegInf;
+	const double z = (std::log(x) - mu) / sigma;
+	return -std::log(x * sigma * std::sqrt(2.0 * M_PI)) - 0.5 * z * z;
+}
+
+// SymmetricDirichlet (crates/b3/src/priors/dirichlet.rs:22-36): the
+// concentration is sum / k; the values are not required to sum to 1
+double sym_dirichlet_lnpdf(const std::vector<double> &x, double sum)
+{
+	const double k = static_cast<double>(x.size());
+	const double a = sum / k;
+	double out = std::lgamma(sum) - k * std::lgamma(a);
+	for (const double v : x)
+		out += (a - 1.0) * std::log(v);
+	return out;
+}
+
+} // namespace
+
+Rng::Rng(uint64_t seed)
+{
+	uint64_t x = seed;
+	for (auto &w : s_)
+		w = splitmix64(x);
+}
+
+uint64_t Rng::next()
+{
+	const uint64_t result = rotl(s_[1] * 5, 7) * 9;
+	const uint64_t t = s_[1] << 17;
+	s_[2] ^= s_[0];
+	s_[3] ^= s_[1];
+	s_[1] ^= s_[2];
+	s_[0] ^= s_[3];
+	s_[2] ^= t;
+	s_[3] = rotl(s_[3], 45);
+	return result;
+}
+
+double Rng::uniform() { return (next() >> 11) * 0x1.0p-53; }
+
+uint32_t Rng::below(uint32_t n)
+{
+	return static_cast<uint32_t>((static_cast<unsigned __int128>(next()) * n) >> 64);
+}
+
+// ---------------------------------------------------------------------------
+
+Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
+	   const uint8_t *samples, const uint32_t *weights,
+	   const uint32_t *parents, const double *heights)
+    : cfg_(cfg), swap_rng_(cfg.seed ^ 0x5EEDu)
+{
+	if (cfg.num_chains < 1 || cfg.num_chains > 256)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_chains must be 1..256");
+	if (cfg.model > 1)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "model must be 0 (HKY) or 1 (GTR)");
+	for (uint32_t k = 0; k < kOpCount; ++k) {
+		if (!(cfg.weights[k] >= 0.0) || !std::isfinite(cfg.weights[k]))
+			throw Error(B3G_ERR_INVALID_ARGUMENT, "bad operator weight");
+		weight_total_ += cfg.weights[k];
+	}
+	if (!(weight_total_ > 0.0))
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "all operator weights are 0");
+	// DeltaExchange starts at tuning 0.75 like the scale operators
+	for (auto &o : ops_)
+		o.tuning = 0.75;
+	b3g_config cc{};
+	cc.num_leaves = L;
+	cc.num_patterns = P;
+	cc.num_states = 4;
+	cc.num_categories = cfg.num_categories;
+	cc.precision = cfg.precision;
+	cc.scale_ln = 30;
+	cc.device = cfg.device;
+	for (uint32_t i = 0; i < cfg.num_chains; ++i) {
+		auto ch = std::make_unique<Chain>(cfg.seed + 0x9E37u * (i + 1));
+		try {
+			ch->tree = std::make_unique<DatedTree>(parents, heights, 2 * L - 1);
+		} catch (const std::exception &e) {
+			throw Error(B3G_ERR_INVALID_ARGUMENT, e.what());
+		}
+		ch->calc = std::make_unique<Calculator>(cc, samples);
+		ch->calc->set_weights(weights);
+		ch->beta = 1.0 / (1.0 + cfg.heat * i);
+		ch->kappa.v = 2.0;
+		ch->alpha.v = 0.5;
+		ch->birth_rate.v = 1.0;
+		ch->rates.v.assign(6, 1.0);
+		ch->freqs.v.assign(4, 0.25);
+		chains_.push_back(std::move(ch));
+	}
+	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
+}
+
+double Mcmc::send_model(Chain &ch, bool mark_all)
+{
+	if (cfg_.model == 1) {
+		ch.calc->set_reversible(ch.rates.v.data(), ch.freqs.v.data(), 1);
+	} else {
+		double V[16], Vi[16], lam[4], Q[16];
+		hky_eigen(ch.kappa.v, ch.freqs.v.data(), V, Vi, lam, Q);
+		ch.calc->set_eigen(V, Vi, lam, Q, ch.freqs.v.data(), 1);
+	}
+	if (mark_all)
+		ch.tree->mark_all_edges_updated();
+	return 0.0;
+}
+
+void Mcmc::set_parameters(double kappa, const double *rates,
+			  const double *freqs, double alpha, double birth_rate)
+{
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		ch.kappa.v = kappa;
+		if (rates)
+			ch.rates.v.assign(rates, rates + 6);
+		if (freqs)
+			ch.freqs.v.assign(freqs, freqs + 4);
+		ch.alpha.v = alpha;
+		ch.birth_rate.v = birth_rate;
+		send_model(ch, true);
+		if (cfg_.num_categories > 1)
+			ch.calc->set_gamma(alpha);
+		// DnaLikelihood::new: mark all, evaluate, accept (dna.rs:34-66)
+		ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+		ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
+					 (uint32_t)ch.internals.size(),
+					 ch.lengths.data(), 1.0);
+	}
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		ch.lnl_cache = ch.calc->log_likelihood();
+		ch.calc->accept();
+		ch.tree->accept();
+		ch.prior_cache = prior(ch);
+		ch.launched = ch.model_sent = ch.alpha_sent = false;
+	}
+}
+
+// Yule (priors/yule.rs:23-40), LogNormal parameter priors and symmetric
+// Dirichlet priors as _b3_config sets them up (config/__init__.py:660-730);
+// the Gamma shape gets LogNormal(0, 1).
+double Mcmc::prior(const Chain &ch) const
+{
+	const DatedTree &t = *ch.tree;
+	const double lam = ch.birth_rate.v;
+	double out = static_cast<double>(t.num_internals()) * std::log(lam);
+	for (uint32_t v = t.num_leaves(); v < t.num_nodes(); ++v) {
+		const double diff = -lam * t.height(v);
+		out += diff;
+		if (v == t.root())
+			out += diff;
+	}
+	out += lognormal_lnpdf(lam, 1.0, 1.5);
+	if (cfg_.model == 0) {
+		out += lognormal_lnpdf(ch.kappa.v, 1.0, 1.25);
+	} else {
+		out += sym_dirichlet_lnpdf(ch.rates.v, 6.0);
+	}
+	out += sym_dirichlet_lnpdf(ch.freqs.v, 1.0);
+	if (cfg_.num_categories > 1)
+		out += lognormal_lnpdf(ch.alpha.v, 0.0, 1.0);
+	return std::isnan(out) ? kNegInf : out;
+}
+
+namespace {
+
+// intersections (operators/_subtree_slide.py): the nodes under `node`
+// whose parent edge crosses `height`
+void intersections(const DatedTree &t, uint32_t node, double height,
+		   std::vector<uint32_t> &out)
+{
+	if (t.height(node) < height) {
+		out.push_back(node);
+		return;
+	}
+	if (!t.is_leaf(node)) {
+		intersections(t, t.left(node), height, out);
+		intersections(t, t.right(node), height, out);
+	}
+}
+
+uint32_t random_nonroot(const DatedTree &t, Rng &rng)
+{
+	uint32_t v;
+	do
+		v = rng.below(t.num_nodes());
+	while (v == t.root());
+	return v;
+}
+
+} // namespace
+
+// One proposal per operator kind, restating python/aspartik/b3/operators.
+void Mcmc::propose(Chain &ch)
+{
+	DatedTree &t = *ch.tree;
+	double u = ch.rng.uniform() * weight_total_;
+	uint32_t op = 0;
+	for (; op + 1 < kOpCount; ++op) {
+		if (u < cfg_.weights[op])
+			break;
+		u -= cfg_.weights[op];
+	}
+	while (cfg_.weights[op] == 0.0 && op > 0)
+		--op;
+	ch.op = op;
+	ch.hastings = 0.0;
+	ch.status = 0;
+	const double f = ops_[op].tuning;
+	auto scale_factor = [&]() {
+		// sample_range(f, 1 / f, Uniform(0, 1)) (operators/_util.py)
+		return f + (1.0 / f - f) * ch.rng.uniform();
+	};
+	switch (op) {
+	case kOpTreeScale: { // _tree_scale.py
+		const double s = scale_factor();
+		t.scale(s);
+		ch.hastings = std::log(s) * (double(t.num_internals()) - 2.0);
+		break;
+	}
+	case kOpScaleKappa:
+	case kOpScaleAlpha:
+	case kOpScaleBirthRate: { // _param_scale.py ScaleReal
+		Real &r = op == kOpScaleKappa ? ch.kappa
+			  : op == kOpScaleAlpha ? ch.alpha
+						: ch.birth_rate;
+		const double s = scale_factor();
+		r.set(r.v * s);
+		ch.hastings = -std::log(s);
+		break;
+	}
+	case kOpDeltaRates:
+	case kOpDeltaFreqs: { // _delta_exchange.py
+		RealVec &vec = op == kOpDeltaRates ? ch.rates : ch.freqs;
+		const double delta = ch.rng.uniform() * (1.0 - f) / 10.0;
+		const uint32_t n = (uint32_t)vec.v.size();
+		uint32_t d1 = ch.rng.below(n), d2 = d1;
+		while (d2 == d1)
+			d1 = ch.rng.below(n);
+		vec.set(d1, vec.v[d1] - delta);
+		vec.set(d2, vec.v[d2] + delta);
+		break;
+	}
+	case kOpNarrowExchange: { // _tree_exchange.py BeastNarrowExchange
+		if (t.num_internals() < 2) {
+			ch.status = 1;
+			break;
+		}
+		uint32_t node;
+		do
+			node = ch.rng.below(t.num_nodes());
+		while (node == t.root() || t.parent_of(node) == t.root());
+		const uint32_t parent = t.parent_of(node);
+		const uint32_t gp = t.parent_of(parent);
+		const uint32_t uncle = t.other_child(gp, parent);
+		if (t.height(uncle) < t.height(parent)) {
+			if (!t.swap_parents(node, uncle))
+				ch.status = 1;
+		} else {
+			ch.status = 1;
+		}
+		break;
+	}
+	case kOpSubtreeSlide: { // _subtree_slide.py
+		if (t.num_internals() < 2) {
+			ch.status = 1;
+			break;
+		}
+		const uint32_t node = random_nonroot(t, ch.rng);
+		const uint32_t parent = t.parent_of(node);
+		const uint32_t gp = t.parent_of(parent);
+		const uint32_t sibling = t.other_child(parent, node);
+		// distribution Uniform(-0.5, 0.5) times the tuning factor
+		const double delta = (ch.rng.uniform() - 0.5) * f;
+		const double old_h = t.height(parent);
+		const double new_h = old_h + delta;
+		std::vector<uint32_t> dest;
+		if (delta > 0.0) {
+			if (gp != kTombstone && t.height(gp) < new_h) {
+				uint32_t new_child = parent, new_parent = gp;
+				while (t.height(new_parent) < new_h) {
+					new_child = new_parent;
+					new_parent = t.parent_of(new_child);
+					if (new_parent == kTombstone)
+						break;
+				}
+				if (new_parent == kTombstone) {
+					t.replace_child(parent, sibling, new_child);
+					t.replace_child(gp, parent, sibling);
+					t.set_root(parent);
+				} else {
+					t.replace_child(parent, sibling, new_child);
+					t.replace_child(gp, parent, sibling);
+					t.replace_child(new_parent, new_child, parent);
+				}
+				intersections(t, new_child, old_h, dest);
+				ch.hastings = -std::log(double(dest.size()));
+			}
+		} else {
+			if (t.height(node) > new_h) {
+				ch.status = 1;
+				break;
+			}
+			if (t.height(sibling) > new_h) {
+				intersections(t, sibling, new_h, dest);
+				if (dest.empty()) {
+					ch.status = 1;
+					break;
+				}
+				const uint32_t new_child = dest[ch.rng.below((uint32_t)dest.size())];
+				const uint32_t new_parent = t.parent_of(new_child);
+				if (gp == kTombstone) {
+					t.replace_child(parent, sibling, new_child);
+					t.replace_child(new_parent, new_child, parent);
+					t.set_root(sibling);
+				} else {
+					t.replace_child(parent, sibling, new_child);
+					t.replace_child(gp, parent, sibling);
+					t.replace_child(new_parent, new_child, parent);
+				}
+				ch.hastings = -std::log(double(dest.size()));
+			}
+		}
+		t.set_height(parent, new_h);
+		break;
+	}
+	default:
+		ch.status = 1;
+	}
+}
+
+// The body of DnaLikelihood/GammaLikelihood::likelihood (dna.rs:68-100,
+// gamma.rs:97-169) up to the asynchronous launch.
+void Mcmc::launch(Chain &ch)
+{
+	const bool model_changed =
+		ch.kappa.changed || ch.rates.changed || ch.freqs.changed;
+	if (model_changed) {
+		send_model(ch, true);
+		ch.model_sent = true;
+	}
+	if (ch.alpha.changed && cfg_.num_categories > 1) {
+		ch.calc->set_gamma(ch.alpha.v);
+		ch.alpha_sent = true;
+		ch.tree->mark_all_edges_updated();
+	}
+	if (!ch.tree->is_changed()) {
+		ch.launched = false;
+		ch.lnl_new = ch.lnl_cache;
+		return;
+	}
+	ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+	ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
+				 (uint32_t)ch.internals.size(), ch.lengths.data(),
+				 1.0);
+	ch.launched = true;
+}
+
+// Metropolis-Hastings and finalize_step (mcmc.rs:337-393).
+void Mcmc::finish(Chain &ch)
+{
+	OpStats &st = ops_[ch.op];
+	bool accept = false;
+	if (ch.status == 0) {
+		const double lnl = ch.launched ? ch.calc->log_likelihood() : ch.lnl_cache;
+		ch.lnl_new = lnl;
+		if (lnl != kNegInf && !std::isnan(lnl)) {
+			const double new_post = lnl + ch.prior_new;
+			const double old_post = ch.lnl_cache + ch.prior_cache;
+			const double ratio = ch.beta * (new_post - old_post) + ch.hastings;
+			accept = ratio > std::log(ch.rng.uniform());
+		}
+	}
+	if (ch.status == 1)
+		++st.aborts;
+	else if (ch.status == 2)
+		++st.prior_rejects;
+	if (accept) {
+		++st.accepts;
+		++st.window_accepts;
+		ch.tree->accept();
+		ch.kappa.accept();
+		ch.alpha.accept();
+		ch.birth_rate.accept();
+		ch.rates.accept();
+		ch.freqs.accept();
+		if (ch.launched)
+			ch.calc->accept();
+		ch.lnl_cache = ch.lnl_new;
+		ch.prior_cache = ch.prior_new;
+	} else {
+		if (ch.status == 0) {
+			++st.rejects;
+			++st.window_rejects;
+		}
+		const bool restore_model = ch.model_sent;
+		const bool restore_alpha = ch.alpha_sent;
+		ch.tree->reject();
+		ch.kappa.reject();
+		ch.alpha.reject();
+		ch.birth_rate.reject();
+		ch.rates.reject();
+		ch.freqs.reject();
+		if (ch.launched)
+			ch.calc->reject();
+		if (restore_model)
+			send_model(ch, false);
+		if (restore_alpha)
+			ch.calc->set_gamma(ch.alpha.v);
+	}
+	ch.launched = false;
+	ch.model_sent = false;
+	ch.alpha_sent = false;
+}
+
+// Metropolis coupling: adjacent temperatures exchange with probability
+// min(1, exp((b_i - b_j) (post_j - post_i))); the betas move, not the states.
+void Mcmc::swap_temperatures()
+{
+	const uint32_t n = (uint32_t)chains_.size();
+	if (n < 2)
+		return;
+	std::vector<uint32_t> by_beta(n);
+	for (uint32_t i = 0; i < n; ++i)
+		by_beta[i] = i;
+	std::sort(by_beta.begin(), by_beta.end(), [&](uint32_t a, uint32_t b) {
+		return chains_[a]->beta > chains_[b]->beta;
+	});
+	const uint32_t k = swap_rng_.below(n - 1);
+	Chain &a = *chains_[by_beta[k]];
+	Chain &b = *chains_[by_beta[k + 1]];
+	const double pa = a.lnl_cache + a.prior_cache;
+	const double pb = b.lnl_cache + b.prior_cache;
+	const double lr = (a.beta - b.beta) * (pb - pa);
+	++swaps_tried_;
+	if (lr > std::log(swap_rng_.uniform())) {
+		std::swap(a.beta, b.beta);
+		++swaps_accepted_;
+	}
+}
+
+// Operator tuning toward 0.234 acceptance (operators/mod.rs:165-193) with a
+// rate that decays as 1/sqrt(round).
+void Mcmc::tune()
+{
+	++tune_rounds_;
+	const double r = 1.0 / std::sqrt(static_cast<double>(tune_rounds_));
+	for (uint32_t k = 0; k < kOpCount; ++k) {
+		OpStats &o = ops_[k];
+		if (k == kOpNarrowExchange)
+			continue; // not tunable
+		const double n = double(o.window_accepts + o.window_rejects);
+		if (n == 0.0)
+			continue;
+		const double acc = double(o.window_accepts) / n;
+		o.tuning = std::clamp(o.tuning + r * (0.234 - acc), 0.01, 0.99);
+		o.window_accepts = o.window_rejects = 0;
+	}
+}
+
+void Mcmc::record()
+{
+	const Chain *cold = chains_[0].get();
+	for (const auto &c : chains_)
+		if (c->beta > cold->beta)
+			cold = c.get();
+	const DatedTree &t = *cold->tree;
+	double length = 0.0;
+	for (uint32_t v = 0; v < t.num_nodes(); ++v)
+		if (v != t.root())
+			length += t.edge_length(v);
+	trace_[0].push_back(cold->lnl_cache);
+	trace_[1].push_back(cold->prior_cache);
+	trace_[2].push_back(cold->lnl_cache + cold->prior_cache);
+	trace_[3].push_back(t.root_height());
+	trace_[4].push_back(cfg_.model == 0 ? cold->kappa.v : cold->rates.v[0]);
+	trace_[5].push_back(cold->alpha.v);
+	trace_[6].push_back(length);
+}
+
+void Mcmc::run(uint64_t steps)
+{
+	for (uint64_t s = 0; s < steps; ++s) {
+		for (auto &ch : chains_)
+			propose(*ch);
+		for (auto &ch : chains_) {
+			if (ch->status != 0)
+				continue;
+			ch->prior_new = prior(*ch);
+			if (ch->prior_new == kNegInf)
+				ch->status = 2; // mcmc.rs:331-335
+		}
+		// every chain's device work is queued before any result is read
+		for (auto &ch : chains_)
+			if (ch->status == 0)
+				launch(*ch);
+		for (auto &ch : chains_)
+			finish(*ch);
+		++step_;
+		if (cfg_.swap_every && step_ % cfg_.swap_every == 0)
+			swap_temperatures();
+		if (cfg_.tune_every && step_ % cfg_.tune_every == 0)
+			tune();
+		if (cfg_.sample_every && step_ % cfg_.sample_every == 0)
+			record();
+	}
+}
+
+double Mcmc::check_full_recompute()
+{
+	double worst = 0.0;
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		ch.tree->mark_all_edges_updated();
+		ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+		ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
+					 (uint32_t)ch.internals.size(),
+					 ch.lengths.data(), 1.0);
+		const double full = ch.calc->log_likelihood();
+		ch.calc->reject();
+		ch.tree->reject();
+		const double rel = std::fabs(full - ch.lnl_cache) /
+				   std::max(1.0, std::fabs(full));
+		worst = std::max(worst, rel);
+	}
+	return worst;
+}
+
+void Mcmc::op_stats(uint32_t op, uint64_t out[4], double *tuning) const
+{
+	const OpStats &o = ops_[op];
+	out[0] = o.accepts;
+	out[1] = o.rejects;
+	out[2] = o.aborts;
+	out[3] = o.prior_rejects;
+	*tuning = o.tuning;
+}
+
+void Mcmc::chain_state(uint32_t chain, uint32_t *parents, double *heights,
+		       double *lnl, double *beta) const
+{
+	const Chain &ch = *chains_.at(chain);
+	std::copy(ch.tree->parents().begin(), ch.tree->parents().end(), parents);
+	std::copy(ch.tree->heights().begin(), ch.tree->heights().end(), heights);
+	*lnl = ch.lnl_cache;
+	*beta = ch.beta;
+}
+
+} // namespace b3g

@@ -1,0 +1,178 @@
+// mcmc.hpp -- native MCMC driver around the device likelihood.
+//
+// Restates the step of b3's engine (crates/b3/src/mcmc.rs:314-393):
+// operator proposal -> prior (reject at -inf before any likelihood work) ->
+// likelihood -> Metropolis-Hastings -> accept or reject of every parameter,
+// the tree and the likelihood.  Operators follow python/aspartik/b3/
+// operators (TreeScale, ScaleReal, SubtreeSlide, BeastNarrowExchange,
+// DeltaExchange) and the priors python/aspartik/b3/config/__init__.py:
+// 660-800 (Yule, LogNormal, SymmetricDirichlet).  Beyond the reference it
+// runs several chains at once (independent replicates or Metropolis-coupled
+// temperatures) and evaluates the proposals of all chains before reading
+// any result back, so their GPU work overlaps.
+#pragma once
+
+#include "calculator.hpp"
+#include "tree.hpp"
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+namespace b3g {
+
+// xoshiro256** (Blackman and Vigna), seeded through splitmix64
+class Rng {
+      public:
+	explicit Rng(uint64_t seed);
+	uint64_t next();
+	double uniform();            // [0, 1)
+	uint32_t below(uint32_t n);  // [0, n)
+
+      private:
+	uint64_t s_[4];
+};
+
+struct Real {
+	double v = 0.0, backup = 0.0;
+	bool changed = false;
+	void set(double x)
+	{
+		if (!changed) {
+			backup = v;
+			changed = true;
+		}
+		v = x;
+	}
+	void accept() { changed = false; }
+	void reject()
+	{
+		if (changed)
+			v = backup;
+		changed = false;
+	}
+};
+
+struct RealVec {
+	std::vector<double> v, backup;
+	bool changed = false;
+	void set(size_t i, double x)
+	{
+		if (!changed) {
+			backup = v;
+			changed = true;
+		}
+		v[i] = x;
+	}
+	void accept() { changed = false; }
+	void reject()
+	{
+		if (changed)
+			v = backup;
+		changed = false;
+	}
+};
+
+enum OpKind : uint32_t {
+	kOpTreeScale = 0,
+	kOpSubtreeSlide,
+	kOpNarrowExchange,
+	kOpScaleKappa,
+	kOpScaleAlpha,
+	kOpScaleBirthRate,
+	kOpDeltaRates,
+	kOpDeltaFreqs,
+	kOpCount
+};
+
+struct OpStats {
+	uint64_t accepts = 0, rejects = 0, aborts = 0, prior_rejects = 0;
+	uint64_t window_accepts = 0, window_rejects = 0;
+	double tuning = 0.75;
+};
+
+struct McmcConfig {
+	uint32_t num_chains;
+	uint32_t num_categories;
+	uint32_t precision;
+	uint32_t model; // 0 HKY, 1 GTR
+	uint64_t seed;
+	double heat;          // beta_i = 1 / (1 + heat * i)
+	uint32_t swap_every;  // steps between swap attempts, 0 = never
+	uint32_t sample_every;
+	uint32_t tune_every;  // steps between operator tunings, 0 = never
+	int32_t device;
+	double weights[kOpCount];
+};
+
+struct Chain {
+	std::unique_ptr<DatedTree> tree;
+	std::unique_ptr<Calculator> calc;
+	Rng rng;
+	Real kappa, alpha, birth_rate;
+	RealVec rates, freqs;
+	double beta = 1.0;
+	double lnl_cache = 0.0, lnl_new = 0.0;
+	double prior_cache = 0.0, prior_new = 0.0;
+	bool launched = false;   // a device evaluation is pending
+	bool model_sent = false; // the device holds a not yet accepted model
+	bool alpha_sent = false;
+	// per-step state
+	uint32_t op = 0;
+	double hastings = 0.0;
+	int status = 0; // 0 pending, 1 abort, 2 prior reject
+	std::vector<uint32_t> internals, children;
+	std::vector<double> lengths;
+	explicit Chain(uint64_t seed) : rng(seed) {}
+};
+
+class Mcmc {
+      public:
+	Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
+	     const uint8_t *samples, const uint32_t *weights,
+	     const uint32_t *parents, const double *heights);
+
+	void set_parameters(double kappa, const double *rates,
+			    const double *freqs, double alpha,
+			    double birth_rate);
+	void run(uint64_t steps);
+	// cold-chain trace: 0 lnL, 1 prior, 2 posterior, 3 root height,
+	// 4 kappa or rates[0], 5 alpha, 6 tree length
+	const std::vector<double> &trace(uint32_t field) const
+	{
+		return trace_[field];
+	}
+	void op_stats(uint32_t op, uint64_t out[4], double *tuning) const;
+	uint64_t swaps_accepted() const { return swaps_accepted_; }
+	uint64_t swaps_tried() const { return swaps_tried_; }
+	uint64_t steps_done() const { return step_; }
+	// Full recompute of every chain from scratch against its cached value;
+	// returns the largest relative difference.  Between steps only.
+	double check_full_recompute();
+	void chain_state(uint32_t chain, uint32_t *parents, double *heights,
+			 double *lnl, double *beta) const;
+	uint32_t num_chains() const { return (uint32_t)chains_.size(); }
+
+      private:
+	void propose(Chain &ch);
+	double prior(const Chain &ch) const;
+	void sync_model(Chain &ch);
+	void launch(Chain &ch);
+	void finish(Chain &ch);
+	void swap_temperatures();
+	void tune();
+	void record();
+	double send_model(Chain &ch, bool mark_all);
+
+	McmcConfig cfg_;
+	std::vector<std::unique_ptr<Chain>> chains_;
+	OpStats ops_[kOpCount];
+	double weight_total_ = 0.0;
+	uint64_t step_ = 0;
+	uint64_t swaps_tried_ = 0, swaps_accepted_ = 0;
+	uint32_t tune_rounds_ = 0;
+	Rng swap_rng_;
+	std::vector<double> trace_[7];
+};
+
+} // namespace b3g

@@ -1,0 +1,154 @@
+// mcmc_abi.cpp -- C ABI of the native MCMC driver (include/b3g.h).
+#include "mcmc.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+namespace b3g {
+void set_last_error(const char *message);
+}
+
+namespace {
+
+template <typename F> b3g_status guarded(F &&f)
+{
+	try {
+		f();
+		b3g::set_last_error("");
+		return B3G_OK;
+	} catch (const b3g::Error &e) {
+		b3g::set_last_error(e.what());
+		return e.status;
+	} catch (const std::bad_alloc &) {
+		b3g::set_last_error("host allocation failed");
+		return B3G_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		b3g::set_last_error(e.what());
+		return B3G_ERR_STATE;
+	} catch (...) {
+		b3g::set_last_error("unknown error");
+		return B3G_ERR_STATE;
+	}
+}
+
+b3g::Mcmc *mcmc_of(b3g_mcmc *m)
+{
+	if (!m)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null mcmc");
+	return reinterpret_cast<b3g::Mcmc *>(m);
+}
+
+} // namespace
+
+extern "C" {
+
+B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
+				   uint32_t num_leaves, uint32_t num_patterns,
+				   const uint8_t *samples,
+				   const uint32_t *weights,
+				   const uint32_t *parents,
+				   const double *heights, b3g_mcmc **out)
+{
+	return guarded([&] {
+		if (!config || !samples || !weights || !parents || !heights || !out)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null argument");
+		*out = nullptr;
+		b3g::McmcConfig c{};
+		c.num_chains = config->num_chains;
+		c.num_categories = config->num_categories;
+		c.precision = config->precision;
+		c.model = config->model;
+		c.seed = config->seed;
+		c.heat = config->heat;
+		c.swap_every = config->swap_every;
+		c.sample_every = config->sample_every;
+		c.tune_every = config->tune_every;
+		c.device = config->device;
+		std::memcpy(c.weights, config->op_weights, sizeof(c.weights));
+		auto *m = new b3g::Mcmc(c, num_leaves, num_patterns, samples,
+					weights, parents, heights);
+		*out = reinterpret_cast<b3g_mcmc *>(m);
+	});
+}
+
+B3G_API void b3g_mcmc_destroy(b3g_mcmc *mcmc)
+{
+	delete reinterpret_cast<b3g::Mcmc *>(mcmc);
+}
+
+B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
+					   const double *rates,
+					   const double *frequencies,
+					   double alpha, double birth_rate)
+{
+	return guarded([&] {
+		mcmc_of(mcmc)->set_parameters(kappa, rates, frequencies, alpha,
+					      birth_rate);
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps)
+{
+	return guarded([&] { mcmc_of(mcmc)->run(steps); });
+}
+
+B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
+				  double *out, uint64_t capacity,
+				  uint64_t *count)
+{
+	return guarded([&] {
+		if (field > 6 || !count)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "bad trace field");
+		const auto &t = mcmc_of(mcmc)->trace(field);
+		*count = t.size();
+		if (out)
+			std::copy(t.begin(),
+				  t.begin() + std::min<uint64_t>(capacity, t.size()),
+				  out);
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
+					   uint64_t *counts, double *tuning)
+{
+	return guarded([&] {
+		if (op >= b3g::kOpCount || !counts || !tuning)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "bad operator");
+		mcmc_of(mcmc)->op_stats(op, counts, tuning);
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
+				  uint64_t *accepted)
+{
+	return guarded([&] {
+		if (!tried || !accepted)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*tried = mcmc_of(mcmc)->swaps_tried();
+		*accepted = mcmc_of(mcmc)->swaps_accepted();
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff)
+{
+	return guarded([&] {
+		if (!max_rel_diff)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*max_rel_diff = mcmc_of(mcmc)->check_full_recompute();
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_chain_state(b3g_mcmc *mcmc, uint32_t chain,
+					uint32_t *parents, double *heights,
+					double *lnl, double *beta)
+{
+	return guarded([&] {
+		b3g::Mcmc *m = mcmc_of(mcmc);
+		if (chain >= m->num_chains() || !parents || !heights || !lnl || !beta)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "bad chain or output");
+		m->chain_state(chain, parents, heights, lnl, beta);
+	});
+}
+
+} // extern "C"

@@ -1,0 +1,132 @@
+"""Python face of the native MCMC driver (``b3g_mcmc_*`` in include/b3g.h).
+
+The driver restates the step of b3's engine (crates/b3/src/mcmc.rs:314-393)
+in C++ around the device likelihood; this wrapper only configures it, runs
+it and reads its traces.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as nat
+from ._native import check, lib
+
+MODELS = {"hky": 0, "gtr": 1}
+OPERATORS = ["tree_scale", "subtree_slide", "narrow_exchange", "scale_kappa",
+             "scale_alpha", "scale_birth_rate", "delta_rates", "delta_frequencies"]
+TRACE_FIELDS = ["lnl", "prior", "posterior", "root_height", "kappa_or_rate0", "alpha",
+                "tree_length"]
+
+# the operator mix of the reference's config recipe for a Yule + GTR model
+# (python/aspartik/b3/config/__init__.py:660-730, 853-858)
+GTR_WEIGHTS = dict(tree_scale=3, subtree_slide=30, narrow_exchange=30, scale_alpha=1,
+                   scale_birth_rate=3, delta_rates=1, delta_frequencies=1)
+# branch-length scale and kappa moves only
+HKY_SCALE_KAPPA_WEIGHTS = dict(tree_scale=3, scale_kappa=1)
+
+
+@dataclass
+class McmcSettings:
+    model: str = "gtr"
+    precision: str = "f32"
+    num_categories: int = 4
+    num_chains: int = 1
+    seed: int = 4
+    heat: float = 0.0
+    swap_every: int = 0
+    sample_every: int = 10
+    tune_every: int = 1000
+    device: int = 0
+    weights: dict = field(default_factory=lambda: dict(GTR_WEIGHTS))
+
+
+class Mcmc:
+    def __init__(self, leaves: np.ndarray, weights: np.ndarray, parents: np.ndarray,
+                 heights: np.ndarray, settings: McmcSettings):
+        leaves = nat.u8(leaves)
+        L, P = leaves.shape
+        w = np.zeros(nat.OP_COUNT)
+        for name, val in settings.weights.items():
+            w[OPERATORS.index(name)] = val
+        cfg = nat.McmcConfig(settings.num_chains, settings.num_categories,
+                             nat.PRECISION_F64 if settings.precision == "f64"
+                             else nat.PRECISION_F32,
+                             MODELS[settings.model], settings.seed, settings.heat,
+                             settings.swap_every, settings.sample_every, settings.tune_every,
+                             settings.device, (ct.c_double * nat.OP_COUNT)(*w))
+        self._wts = nat.u32(weights)
+        self._par = nat.u32(parents)
+        self._hei = nat.f64(heights)
+        h = ct.c_void_p()
+        check(lib.b3g_mcmc_create(ct.byref(cfg), L, P, nat.as_ptr(leaves, ct.c_uint8),
+                                  nat.as_ptr(self._wts, ct.c_uint32),
+                                  nat.as_ptr(self._par, ct.c_uint32),
+                                  nat.as_ptr(self._hei, ct.c_double), ct.byref(h)))
+        self._h = h
+        self.settings = settings
+        self.num_nodes = self._par.size
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.b3g_mcmc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_parameters(self, kappa=2.0, rates=None, frequencies=None, alpha=0.5,
+                       birth_rate=1.0):
+        r = None if rates is None else nat.f64(rates)
+        f = None if frequencies is None else nat.f64(frequencies)
+        check(lib.b3g_mcmc_set_parameters(
+            self._h, float(kappa), None if r is None else nat.as_ptr(r, ct.c_double),
+            None if f is None else nat.as_ptr(f, ct.c_double), float(alpha),
+            float(birth_rate)))
+
+    def run(self, steps: int):
+        check(lib.b3g_mcmc_run(self._h, int(steps)))
+
+    def trace(self, name: str) -> np.ndarray:
+        fid = TRACE_FIELDS.index(name)
+        n = ct.c_uint64()
+        check(lib.b3g_mcmc_trace(self._h, fid, None, 0, ct.byref(n)))
+        out = np.empty(n.value)
+        check(lib.b3g_mcmc_trace(self._h, fid, nat.as_ptr(out, ct.c_double), n.value,
+                                 ct.byref(n)))
+        return out
+
+    def operator_stats(self) -> dict:
+        out = {}
+        for k, name in enumerate(OPERATORS):
+            counts = (ct.c_uint64 * 4)()
+            tuning = ct.c_double()
+            check(lib.b3g_mcmc_operator_stats(self._h, k, counts, ct.byref(tuning)))
+            out[name] = dict(accepts=counts[0], rejects=counts[1], aborts=counts[2],
+                             prior_rejects=counts[3], tuning=tuning.value)
+        return out
+
+    def swaps(self) -> tuple[int, int]:
+        t, a = ct.c_uint64(), ct.c_uint64()
+        check(lib.b3g_mcmc_swaps(self._h, ct.byref(t), ct.byref(a)))
+        return t.value, a.value
+
+    def check(self) -> float:
+        out = ct.c_double()
+        check(lib.b3g_mcmc_check(self._h, ct.byref(out)))
+        return out.value
+
+    def chain_state(self, chain: int):
+        parents = np.zeros(self.num_nodes, dtype=np.uint32)
+        heights = np.zeros(self.num_nodes)
+        lnl, beta = ct.c_double(), ct.c_double()
+        check(lib.b3g_mcmc_chain_state(self._h, chain, nat.as_ptr(parents, ct.c_uint32),
+                                       nat.as_ptr(heights, ct.c_double), ct.byref(lnl),
+                                       ct.byref(beta)))
+        return parents, heights, lnl.value, beta.value

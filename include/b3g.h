@@ -195,6 +195,90 @@ B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
 B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc);
 B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
 
+/* ---- native MCMC driver ---------------------------------------------------
+ * The caller side of the path: b3's MCMC step (crates/b3/src/mcmc.rs:
+ * 314-393) in C++ -- operator proposal, prior (reject at -inf before any
+ * likelihood work), device likelihood, Metropolis-Hastings, accept/reject
+ * of tree, parameters and calculator -- with the operators of
+ * python/aspartik/b3/operators (TreeScale, SubtreeSlide, BeastNarrowExchange,
+ * ScaleReal, DeltaExchange) and the priors of the reference's config
+ * recipe (Yule, LogNormal, SymmetricDirichlet).  Several chains run at once
+ * (replicates, or Metropolis-coupled temperatures beta_i = 1/(1 + heat*i));
+ * every chain's device work of a step is queued before any result is read.
+ * The model is HKY (kappa + frequencies) or GTR (6 exchangeabilities +
+ * frequencies), optionally with Gamma rate categories (shape alpha). */
+typedef struct b3g_mcmc b3g_mcmc;
+
+enum { B3G_MODEL_HKY = 0, B3G_MODEL_GTR = 1 };
+
+enum {
+	B3G_OP_TREE_SCALE = 0,
+	B3G_OP_SUBTREE_SLIDE = 1,
+	B3G_OP_NARROW_EXCHANGE = 2,
+	B3G_OP_SCALE_KAPPA = 3,
+	B3G_OP_SCALE_ALPHA = 4,
+	B3G_OP_SCALE_BIRTH_RATE = 5,
+	B3G_OP_DELTA_RATES = 6,
+	B3G_OP_DELTA_FREQUENCIES = 7,
+	B3G_OP_COUNT = 8
+};
+
+/* Trace fields of the cold chain, sampled every sample_every steps. */
+enum {
+	B3G_TRACE_LNL = 0,
+	B3G_TRACE_PRIOR = 1,
+	B3G_TRACE_POSTERIOR = 2,
+	B3G_TRACE_ROOT_HEIGHT = 3,
+	B3G_TRACE_KAPPA_OR_RATE0 = 4,
+	B3G_TRACE_ALPHA = 5,
+	B3G_TRACE_TREE_LENGTH = 6
+};
+
+typedef struct b3g_mcmc_config {
+	uint32_t num_chains;     /* 1..256 */
+	uint32_t num_categories; /* 1 = no Gamma */
+	uint32_t precision;      /* B3G_PRECISION_* */
+	uint32_t model;          /* B3G_MODEL_* */
+	uint64_t seed;
+	double heat;             /* 0 = independent replicates */
+	uint32_t swap_every;     /* steps between swap attempts, 0 = never */
+	uint32_t sample_every;   /* steps between trace samples, 0 = never */
+	uint32_t tune_every;     /* steps between operator tunings, 0 = never */
+	int32_t device;
+	double op_weights[B3G_OP_COUNT];
+} b3g_mcmc_config;
+
+/* parents[2L-1] (root: 0xFFFFFFFF) and heights[2L-1] give the start tree of
+ * every chain; samples/weights as for b3g_calculator_create/_set_weights. */
+B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
+				   uint32_t num_leaves, uint32_t num_patterns,
+				   const uint8_t *samples,
+				   const uint32_t *weights,
+				   const uint32_t *parents,
+				   const double *heights, b3g_mcmc **out);
+B3G_API void b3g_mcmc_destroy(b3g_mcmc *mcmc);
+/* Start values (rates/frequencies may be NULL to keep the defaults). */
+B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
+					   const double *rates,
+					   const double *frequencies,
+					   double alpha, double birth_rate);
+B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps);
+/* Copies up to `capacity` samples of a B3G_TRACE_* field; *count = all. */
+B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
+				  double *out, uint64_t capacity,
+				  uint64_t *count);
+/* counts = {accepts, rejects, aborts, prior rejects} of one operator. */
+B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
+					   uint64_t *counts, double *tuning);
+B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
+				  uint64_t *accepted);
+/* Re-evaluates every chain from scratch and returns the largest relative
+ * difference to its incrementally maintained log-likelihood. */
+B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff);
+B3G_API b3g_status b3g_mcmc_chain_state(b3g_mcmc *mcmc, uint32_t chain,
+					uint32_t *parents, double *heights,
+					double *lnl, double *beta);
+
 /* ---- allocation-free pruning --------------------------------------------
  * This entry point has no counterpart in the reference.
  *
