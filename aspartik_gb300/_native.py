@@ -136,6 +136,13 @@ SIGNATURES = {
     "b3g_calculator_span_begin": (ct.c_int, [_vp]),
     "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
     "b3g_prune_noalloc": (ct.c_int, [ct.POINTER(PruneBuffers), _vp]),
+    "b3g_batch_create": (ct.c_int, [ct.POINTER(_vp), ct.c_uint32, ct.POINTER(_vp)]),
+    "b3g_batch_destroy": (None, [_vp]),
+    "b3g_calculator_stage_lengths": (
+        ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
+    "b3g_batch_run": (ct.c_int, [_vp]),
+    "b3g_batch_log_likelihoods": (ct.c_int, [_vp, _f64p]),
+    "b3g_batch_last_ms": (ct.c_int, [_vp, _f32p]),
     "b3g_mcmc_create": (ct.c_int, [ct.POINTER(McmcConfig), ct.c_uint32, ct.c_uint32, _u8p,
                                    _u32p, _u32p, _f64p, ct.POINTER(_vp)]),
     "b3g_mcmc_destroy": (None, [_vp]),

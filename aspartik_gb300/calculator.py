@@ -201,4 +201,55 @@ class GpuCalculator:
         return ms.value
 
 
-__all__ = ["Calculator", "GpuCalculator", "B3GError"]
+def _stage_lengths(self, internals, children, lengths, clock_rate: float = 1.0) -> None:
+    """Stage a dirty-path evaluation for this calculator's batch (no launch)."""
+    internals = nat.u32(internals)
+    children = nat.u32(children).reshape(-1)
+    lengths = nat.f64(lengths).reshape(-1)
+    n = internals.size
+    if children.size != 2 * n or lengths.size != 2 * n:
+        raise ValueError("children and lengths need two values per internal")
+    check(lib.b3g_calculator_stage_lengths(
+        self._h, nat.as_ptr(internals, ct.c_uint32), nat.as_ptr(children, ct.c_uint32), n,
+        nat.as_ptr(lengths, ct.c_double), float(clock_rate)))
+
+
+GpuCalculator.stage_lengths = _stage_lengths
+
+
+class Batch:
+    """Many FP32 calculators evaluated by one graph-replayed launch."""
+
+    def __init__(self, members: list):
+        self.members = list(members)
+        arr = (ct.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        h = ct.c_void_p()
+        check(lib.b3g_batch_create(arr, len(self.members), ct.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.b3g_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self) -> None:
+        check(lib.b3g_batch_run(self._h))
+
+    def log_likelihoods(self) -> np.ndarray:
+        out = np.empty(len(self.members))
+        check(lib.b3g_batch_log_likelihoods(self._h, nat.as_ptr(out, ct.c_double)))
+        return out
+
+    def last_ms(self) -> float:
+        ms = ct.c_float()
+        check(lib.b3g_batch_last_ms(self._h, ct.byref(ms)))
+        return ms.value
+
+
+__all__ = ["Calculator", "GpuCalculator", "Batch", "B3GError"]

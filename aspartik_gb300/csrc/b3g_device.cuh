@@ -87,6 +87,45 @@ struct PruneParams {
 	double log_inv_c;
 };
 
+// One member of a batch (many calculators evaluated by one launch).  The
+// pointers are the member's own device store; written once per batch.
+struct MemberDesc {
+	const uint8_t *tips;
+	float *partials;     // FP32 chosen form
+	int32_t *scales;
+	float *ptab;
+	const uint8_t *stage; // the member's staged block (ops, pi, runs, lengths)
+	const ModelDev *model;
+	const uint32_t *weights;
+	double *site_lnl;
+	double *tile_sums;   // one per tile, owned by the batch
+	unsigned *ticket;    // tiles finished, owned by the batch
+	uint32_t off_pi, off_runs, off_in;
+	uint32_t ldp, C, L, tile;
+	double log_inv_c;
+};
+
+// Per step and member, written by the host before every batched launch.
+struct MemberStep {
+	uint32_t n;      // dirty entries (0: nothing to evaluate)
+	uint32_t n_runs;
+	uint32_t tips_smem;
+	uint32_t pad;
+	double clock_rate;
+};
+
+struct BatchParams {
+	const MemberDesc *members;
+	const MemberStep *steps;
+	double *lnl_out;     // [members]
+	unsigned *work_next; // work counter, zero before each launch
+	uint32_t num_members;
+	uint32_t smem_ops_bytes;  // shared memory reserved for ops + runs
+	uint32_t smem_tips_bytes; // shared memory reserved for a tip tile
+	uint32_t max_cols;
+	uint32_t narrow; // every member indexes with 32 bits
+};
+
 // Launchers (kernels4.cu).  Each returns the launch error.
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);
 cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
@@ -96,5 +135,12 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			       cudaStream_t s);
 cudaError_t launch_eigen(ModelDev *model, uint32_t states, cudaStream_t s);
+// Batched evaluation (FP32): transition tables of every member with work,
+// then one persistent pruning launch over all members' pattern tiles.
+// max_entries = largest member n * 2 * C.
+cudaError_t launch_ptab4_batch(const BatchParams &p, uint32_t max_entries,
+			       cudaStream_t s);
+cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
+				cudaStream_t s);
 
 } // namespace b3g

@@ -1,0 +1,44 @@
+// batch.hpp -- many calculators evaluated by one graph-replayed launch
+// (batch.cu).
+#pragma once
+
+#include "calculator.hpp"
+
+#include <vector>
+
+namespace b3g {
+
+class Batch {
+      public:
+	Batch(Calculator *const *members, uint32_t count);
+	~Batch();
+	Batch(const Batch &) = delete;
+	Batch &operator=(const Batch &) = delete;
+	// replays the step for every member that staged a proposal
+	void run();
+	// waits; out[i] = member i's log-likelihood, NaN if it had nothing
+	void log_likelihoods(double *out);
+	float last_ms();
+
+      private:
+	void release();
+	std::vector<Calculator *> members_;
+	std::vector<uint32_t> order_; // members by cost, descending
+	int device_ = -1;
+	cudaStream_t stream_ = nullptr;
+	cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+	MemberDesc *d_desc_ = nullptr;
+	MemberStep *d_steps_ = nullptr, *h_steps_ = nullptr;
+	double *d_lnl_ = nullptr, *h_lnl_ = nullptr;
+	unsigned *d_work_ = nullptr;
+	double *d_tile_sums_ = nullptr;
+	unsigned *d_tickets_ = nullptr;
+	cudaGraph_t graph_ = nullptr;
+	cudaGraphExec_t exec_ = nullptr;
+	BatchParams bp_{};
+	uint32_t max_entries_ = 0, ctas_ = 0;
+	bool ran_ = false;
+	std::vector<uint8_t> evaluated_;
+};
+
+} // namespace b3g

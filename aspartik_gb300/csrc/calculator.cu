@@ -273,6 +273,7 @@ void Calculator::upload_model()
 				   cudaMemcpyHostToDevice, stream_),
 		   "upload model");
 	check_cuda(cudaEventRecord(ev_model_free_, stream_), "event");
+	stream_dirty_ = true;
 }
 
 // The dirty list must name distinct internals, children must be valid node
@@ -451,6 +452,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read lnl");
 	have_result_ = true;
+	stream_dirty_ = true;
 	cat_valid_ = want_cat;
 }
 
@@ -493,10 +495,53 @@ void Calculator::propose_lengths(const uint32_t *internals,
 	if (!std::isfinite(clock_rate))
 		throw Error(B3G_ERR_NUMERIC, "non-finite clock rate");
 	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	if (batch_done_)
+		check_cuda(cudaEventSynchronize(batch_done_), "batch stage reuse");
 	stage_ops(internals, children, n);
 	std::memcpy(h_stage_ + off_pi_, model_host_.pi, S_ * sizeof(double));
 	std::memcpy(h_stage_ + off_in_, lengths, (size_t)n * 2 * sizeof(double));
+	staged_ = false;
 	launch(n, false, clock_rate, false);
+}
+
+void Calculator::stage_lengths(const uint32_t *internals,
+			       const uint32_t *children, uint32_t n,
+			       const double *lengths, double clock_rate)
+{
+	DeviceGuard g(device_);
+	if (!in_batch_)
+		throw Error(B3G_ERR_STATE,
+			    "stage_lengths needs the calculator to be in a batch");
+	if (!model_set_)
+		throw Error(B3G_ERR_STATE,
+			    "no substitution model set before stage_lengths");
+	if (n > 4096)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "batched lists hold at most 4,096 entries");
+	validate_lists(internals, children, n);
+	if (!lengths)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "null lengths");
+	for (size_t k = 0; k < (size_t)n * 2; ++k)
+		if (!std::isfinite(lengths[k]))
+			throw Error(B3G_ERR_NUMERIC, "non-finite edge length");
+	if (!std::isfinite(clock_rate))
+		throw Error(B3G_ERR_NUMERIC, "non-finite clock rate");
+	// the batch's previous copy of this staging buffer must be done, and
+	// so must this calculator's own last launch
+	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	if (batch_done_)
+		check_cuda(cudaEventSynchronize(batch_done_), "batch stage reuse");
+	stage_ops(internals, children, n);
+	std::memcpy(h_stage_ + off_pi_, model_host_.pi, S_ * sizeof(double));
+	std::memcpy(h_stage_ + off_in_, lengths, (size_t)n * 2 * sizeof(double));
+	staged_ = true;
+	staged_n_ = n;
+	staged_clock_ = clock_rate;
+	staged_tips_smem_ = (4ull * tip_children_ >= L_ &&
+			     (size_t)L_ * runs_tile_ <= 32u * 1024u)
+				    ? 1u
+				    : 0u;
+	have_result_ = false; // results come from the batch
 }
 
 void Calculator::likelihoods(double *out)
@@ -695,6 +740,7 @@ void Calculator::set_category_rates(const double *rates)
 				   stream_),
 		   "upload category rates");
 	check_cuda(cudaEventRecord(ev_model_free_, stream_), "event");
+	stream_dirty_ = true;
 }
 
 void Calculator::set_gamma(double alpha)

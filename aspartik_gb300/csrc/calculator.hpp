@@ -70,6 +70,12 @@ class Calculator {
 	float span_end();
 	uint64_t last_upload_bytes() const { return last_upload_bytes_; }
 
+	// Batched evaluation: validate and stage a dirty-path evaluation
+	// without launching; a Batch evaluates all staged members at once.
+	void stage_lengths(const uint32_t *internals, const uint32_t *children,
+			   uint32_t n, const double *lengths, double clock_rate);
+	friend class Batch;
+
       private:
 	void validate_lists(const uint32_t *internals,
 			    const uint32_t *children, uint32_t n);
@@ -137,6 +143,17 @@ class Calculator {
 	size_t off_pi_ = 0, off_runs_ = 0, off_in_ = 0;
 	uint32_t n_runs_ = 0;
 	uint64_t last_upload_bytes_ = 0;
+	// batch membership: staged proposal and the event after which the
+	// batch no longer reads this calculator's staging buffer
+	bool in_batch_ = false;
+	bool staged_ = false;
+	uint32_t staged_n_ = 0;
+	uint32_t staged_tips_smem_ = 0;
+	double staged_clock_ = 1.0;
+	cudaEvent_t batch_done_ = nullptr;
+	// work was queued on this calculator's own stream since a batch last
+	// synchronised with it (model uploads, eigen kernel, own proposals)
+	bool stream_dirty_ = false;
 	uint32_t num_sms_ = 1;
 	uint32_t runs_tile_ = 64;
 	bool use_runs_ = false;

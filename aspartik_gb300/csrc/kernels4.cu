@@ -513,234 +513,7 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 }
 
 // ---------------------------------------------------------------------------
-// Run-synchronous walk (FP32 chosen form).
-//
-// The one-thread-per-column walk above leaves the GPU with only
-// patterns x categories threads, about 14 warps per SM on the largest
-// workload, and it is latency-bound.  Here a block owns a tile of patterns
-// and walks the schedule run by run (a run is a sequence of mutually
-// independent entries, e.g. one level of the tree).  Inside a run its
-// (entry, category, pattern) items are spread over all threads of the block,
-// so a wide level keeps every thread busy; a __syncthreads() separates runs.
-// Blocks are persistent and take tiles blockIdx.x, + gridDim.x, ...
-//
-// Thread layout: column col = c * tile + pl (fixed per thread, patterns
-// fastest, so a warp touches 32 consecutive patterns of one category) and
-// group g; the block has cols * groups threads and group g handles entries
-// g, g + groups, ... of every run.
-
-// Tip codes come from the block's shared-memory tile (tip_row = tile) or
-// from global memory (tips_p = tips + p, tip_row = ldp); the schedule from
-// shared memory.
-template <typename Idx>
-__device__ __forceinline__ void run_item(const PruneParams &prm,
-					 const NodeOp *__restrict__ ops,
-					 const uint8_t *__restrict__ tips_p,
-					 uint32_t tip_row,
-					 const float4 *__restrict__ ptab,
-					 float4 *__restrict__ part,
-					 int32_t *__restrict__ scales, Idx stride,
-					 Idx col_off, uint32_t c, uint32_t i,
-					 float4 &y, int32_t &cnt)
-{
-	const NodeOp op = ops[i];
-	const float4 *tl = ptab + ((size_t)(2 * i) * prm.C + c) * 5;
-	const float4 *tr = tl + 5 * prm.C;
-	float4 a, b;
-	int32_t sa = 0, sb = 0;
-	if (op.left & kTipBit) {
-		a = tl[tips_p[(Idx)(op.left & ~kTipBit) * tip_row]];
-	} else {
-		const Idx ix = (Idx)op.left * stride + col_off;
-		const float4 x = part[ix];
-		sa = scales[ix];
-		a = v4_apply(tl, x);
-	}
-	if (op.right & kTipBit) {
-		b = tr[tips_p[(Idx)(op.right & ~kTipBit) * tip_row]];
-	} else {
-		const Idx ix = (Idx)op.right * stride + col_off;
-		const float4 x = part[ix];
-		sb = scales[ix];
-		b = v4_apply(tr, x);
-	}
-	y = v4_mul(a, b);
-	cnt = sa + sb + rescale_pow2(y);
-	const Idx ox = (Idx)op.out * stride + col_off;
-	part[ox] = y;
-	scales[ox] = cnt;
-}
-
-template <typename Idx>
-__global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
-{
-	const uint32_t tile = prm.tile, C = prm.C;
-	const uint32_t cols = tile * C;
-	const uint32_t groups = blockDim.x / cols;
-	const uint32_t tid = threadIdx.x;
-	const uint32_t col = tid % cols, g = tid / cols;
-	const uint32_t c = col / tile, pl = col - c * tile;
-	const Idx stride = (Idx)C * prm.ldp;
-	float4 *__restrict__ part = (float4 *)prm.partials;
-	const float4 *__restrict__ ptab = (const float4 *)prm.ptab;
-	int32_t *__restrict__ scales = prm.scales;
-	const uint32_t ntiles = prm.ldp / tile;
-
-	extern __shared__ double smem[];
-	double *s_dot = smem;                        // [cols] root pi . x
-	int32_t *s_cnt = (int32_t *)(smem + cols);   // [cols] root exponents
-	double *s_red = smem + cols + (cols + 1) / 2; // [2 * blockDim.x]
-	// schedule and run starts, staged once per block
-	NodeOp *s_ops = (NodeOp *)(s_red + 2 * blockDim.x);  // [n]
-	uint32_t *s_runs = (uint32_t *)(s_ops + prm.n);     // [n_runs + 1]
-	// tip codes of the current tile for every leaf: [L][tile]
-	uint8_t *s_tips = (uint8_t *)(s_runs + ((prm.n_runs + 4) & ~3u));
-	__shared__ unsigned s_last;
-
-	for (uint32_t k = tid; k < prm.n; k += blockDim.x)
-		s_ops[k] = prm.ops[k];
-	for (uint32_t k = tid; k <= prm.n_runs; k += blockDim.x)
-		s_runs[k] = prm.runs[k];
-
-	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
-
-	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const uint32_t p = t * tile + pl;
-		const Idx col_off = (Idx)c * prm.ldp + p;
-		const uint8_t *tips_p;
-		uint32_t tip_row;
-		if (prm.tips_smem) {
-			// 4-byte loads: rows start at multiples of 32 patterns
-			const uint32_t wpr = tile >> 2;
-			const uint32_t total = prm.num_leaves * wpr;
-			uint32_t *s_t32 = (uint32_t *)s_tips;
-			for (uint32_t k = tid; k < total; k += blockDim.x) {
-				const uint32_t leaf = k / wpr, w4 = k - leaf * wpr;
-				s_t32[k] = *(const uint32_t *)(prm.tips +
-							       (size_t)leaf * prm.ldp +
-							       t * tile + w4 * 4);
-			}
-			tips_p = s_tips + pl;
-			tip_row = tile;
-		} else {
-			tips_p = prm.tips + p;
-			tip_row = prm.ldp;
-		}
-		__syncthreads();
-		for (uint32_t r = 0; r < prm.n_runs; ++r) {
-			const uint32_t start = s_runs[r], end = s_runs[r + 1];
-			uint32_t i = start + g;
-			// two independent entries per iteration: all their loads
-			// are issued before either product
-			for (; i + groups < end; i += 2 * groups) {
-				float4 y0, y1;
-				int32_t c0, c1;
-				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
-					 stride, col_off, c, i, y0, c0);
-				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
-					 stride, col_off, c, i + groups, y1, c1);
-				if (i + groups == prm.n - 1) {
-					s_dot[col] = (double)prm.pi[0] * y1.x + (double)prm.pi[1] * y1.y +
-						     (double)prm.pi[2] * y1.z + (double)prm.pi[3] * y1.w;
-					s_cnt[col] = c1;
-				}
-			}
-			if (i < end) {
-				float4 y0;
-				int32_t c0;
-				run_item(prm, s_ops, tips_p, tip_row, ptab, part, scales,
-					 stride, col_off, c, i, y0, c0);
-				if (i == prm.n - 1) {
-					s_dot[col] = (double)prm.pi[0] * y0.x + (double)prm.pi[1] * y0.y +
-						     (double)prm.pi[2] * y0.z + (double)prm.pi[3] * y0.w;
-					s_cnt[col] = c0;
-				}
-			}
-			__syncthreads();
-		}
-		// root: category mixing per pattern (threads 0 .. tile-1)
-		double contrib = 0.0;
-		if (tid < tile) {
-			const uint32_t pp = t * tile + tid;
-			int32_t emax = INT32_MIN;
-			for (uint32_t k = 0; k < C; k++)
-				if (s_dot[k * tile + tid] > 0.0)
-					emax = max(emax, s_cnt[k * tile + tid]);
-			double site;
-			if (emax == INT32_MIN) {
-				site = -INFINITY;
-			} else {
-				double acc = 0.0;
-				for (uint32_t k = 0; k < C; k++)
-					acc += scalbn(s_dot[k * tile + tid],
-						      s_cnt[k * tile + tid] - emax);
-				site = log(acc) + (double)emax * 0.69314718055994530942 +
-				       prm.log_inv_c;
-			}
-			prm.site_lnl[pp] = site;
-			if (prm.cat_lnl)
-				for (uint32_t k = 0; k < C; k++)
-					prm.cat_lnl[(size_t)k * prm.ldp + pp] =
-						log(s_dot[k * tile + tid]) +
-						(double)s_cnt[k * tile + tid] *
-							0.69314718055994530942;
-			const uint32_t wgt = prm.weights[pp];
-			contrib = wgt ? site * (double)wgt : 0.0;
-		}
-		// tile sum in a fixed order (warp shuffles, then warps in order)
-		for (int off = 16; off > 0; off >>= 1)
-			contrib += __shfl_down_sync(0xffffffffu, contrib, off);
-		if ((tid & 31u) == 0 && tid < tile)
-			s_red[tid >> 5] = contrib;
-		__syncthreads();
-		if (tid == 0) {
-			double tsum = 0.0;
-			for (uint32_t w2 = 0; w2 < (tile + 31u) / 32u; w2++)
-				tsum += s_red[w2];
-			neumaier_add(cta_sum, cta_comp, tsum);
-		}
-		__syncthreads();
-	}
-
-	if (tid == 0) {
-		prm.block_sums[blockIdx.x] =
-			isfinite(cta_sum) ? cta_sum + cta_comp : cta_sum;
-		__threadfence();
-		const unsigned tk = atomicAdd(prm.ticket, 1u);
-		s_last = (tk == gridDim.x - 1u);
-	}
-	__syncthreads();
-	if (!s_last)
-		return;
-	// the last block folds the block sums in a fixed-shape tree
-	__threadfence();
-	const uint32_t nthr = blockDim.x;
-	double sum = 0.0, comp = 0.0;
-	for (uint32_t bix = tid; bix < gridDim.x; bix += nthr)
-		neumaier_add(sum, comp, __ldcg(prm.block_sums + bix));
-	double *s_sum = s_red;
-	double *s_comp = s_red + nthr;
-	s_sum[tid] = sum;
-	s_comp[tid] = comp;
-	__syncthreads();
-	uint32_t span = 1;
-	while (span < nthr)
-		span <<= 1;
-	for (uint32_t stride2 = span >> 1; stride2 > 0; stride2 >>= 1) {
-		if (tid < stride2 && tid + stride2 < nthr) {
-			double a = s_sum[tid], ac = s_comp[tid];
-			neumaier_merge(a, ac, s_sum[tid + stride2], s_comp[tid + stride2]);
-			s_sum[tid] = a;
-			s_comp[tid] = ac;
-		}
-		__syncthreads();
-	}
-	if (tid == 0) {
-		const double total = s_sum[0];
-		*prm.lnl_out = isfinite(total) ? total + s_comp[0] : total;
-		*prm.ticket = 0u;
-	}
-}
+#include "runs4.cuh"
 
 // ---------------------------------------------------------------------------
 // Eigensystem of a reversible Q (FP64; run when the model changes, not per
@@ -959,6 +732,32 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			return e;
 	}
 	kern<<<ctas, threads, smem, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_ptab4_batch(const BatchParams &p, uint32_t max_entries,
+			       cudaStream_t s)
+{
+	const dim3 grid((max_entries + 127u) / 128u, p.num_members);
+	ptab4_batch_kernel<<<grid, 128, 0, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
+				cudaStream_t s)
+{
+	const size_t smem = sizeof(double) * (p.max_cols + (p.max_cols + 1) / 2 +
+					      2 * 512) +
+			    p.smem_ops_bytes + p.smem_tips_bytes;
+	auto kern = p.narrow ? prune4_batch_kernel<uint32_t>
+			     : prune4_batch_kernel<size_t>;
+	if (smem > 48 * 1024) {
+		const cudaError_t e = cudaFuncSetAttribute(
+			kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess)
+			return e;
+	}
+	kern<<<ctas, 512, smem, s>>>(p);
 	return cudaGetLastError();
 }
 

@@ -113,6 +113,7 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		ch->calc = std::make_unique<Calculator>(cc, samples);
 		ch->calc->set_weights(weights);
 		ch->beta = 1.0 / (1.0 + cfg.heat * i);
+		ch->index = i;
 		ch->kappa.v = 2.0;
 		ch->alpha.v = 0.5;
 		ch->birth_rate.v = 1.0;
@@ -121,6 +122,13 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		chains_.push_back(std::move(ch));
 	}
 	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
+	if (cfg.precision == B3G_PRECISION_F32) {
+		std::vector<Calculator *> calcs;
+		for (auto &ch : chains_)
+			calcs.push_back(ch->calc.get());
+		batch_ = std::make_unique<Batch>(calcs.data(), (uint32_t)calcs.size());
+		batch_lnl_.assign(calcs.size(), 0.0);
+	}
 }
 
 double Mcmc::send_model(Chain &ch, bool mark_all)
@@ -382,9 +390,14 @@ void Mcmc::launch(Chain &ch)
 		return;
 	}
 	ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
-	ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
-				 (uint32_t)ch.internals.size(), ch.lengths.data(),
-				 1.0);
+	if (batch_)
+		ch.calc->stage_lengths(ch.internals.data(), ch.children.data(),
+				       (uint32_t)ch.internals.size(),
+				       ch.lengths.data(), 1.0);
+	else
+		ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
+					 (uint32_t)ch.internals.size(),
+					 ch.lengths.data(), 1.0);
 	ch.launched = true;
 }
 
@@ -394,7 +407,9 @@ void Mcmc::finish(Chain &ch)
 	OpStats &st = ops_[ch.op];
 	bool accept = false;
 	if (ch.status == 0) {
-		const double lnl = ch.launched ? ch.calc->log_likelihood() : ch.lnl_cache;
+		const double lnl = !ch.launched ? ch.lnl_cache
+				   : batch_    ? batch_lnl_[ch.index]
+					       : ch.calc->log_likelihood();
 		ch.lnl_new = lnl;
 		if (lnl != kNegInf && !std::isnan(lnl)) {
 			const double new_post = lnl + ch.prior_new;
@@ -523,9 +538,16 @@ void Mcmc::run(uint64_t steps)
 				ch->status = 2; // mcmc.rs:331-335
 		}
 		// every chain's device work is queued before any result is read
+		bool any = false;
 		for (auto &ch : chains_)
-			if (ch->status == 0)
+			if (ch->status == 0) {
 				launch(*ch);
+				any = any || ch->launched;
+			}
+		if (batch_ && any) {
+			batch_->run();
+			batch_->log_likelihoods(batch_lnl_.data());
+		}
 		for (auto &ch : chains_)
 			finish(*ch);
 		++step_;

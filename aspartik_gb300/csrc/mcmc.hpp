@@ -12,6 +12,7 @@
 // any result back, so their GPU work overlaps.
 #pragma once
 
+#include "batch.hpp"
 #include "calculator.hpp"
 #include "tree.hpp"
 
@@ -112,6 +113,7 @@ struct Chain {
 	Real kappa, alpha, birth_rate;
 	RealVec rates, freqs;
 	double beta = 1.0;
+	uint32_t index = 0;
 	double lnl_cache = 0.0, lnl_new = 0.0;
 	double prior_cache = 0.0, prior_new = 0.0;
 	bool launched = false;   // a device evaluation is pending
@@ -166,6 +168,10 @@ class Mcmc {
 
 	McmcConfig cfg_;
 	std::vector<std::unique_ptr<Chain>> chains_;
+	// FP32 chosen form: every chain's proposal of a step is evaluated by
+	// one graph replay of a batch
+	std::unique_ptr<Batch> batch_;
+	std::vector<double> batch_lnl_;
 	OpStats ops_[kOpCount];
 	double weight_total_ = 0.0;
 	uint64_t step_ = 0;

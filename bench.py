@@ -239,6 +239,43 @@ def cpu_oracle_eval(wl, num_threads: int, pattern_limit: int | None = None):
     return dt, P, calcs[0].num_threads(), lnl
 
 
+def mcmc_ess(wl, steps: int, device: int) -> dict:
+    """ESS per second of the cold chain, chosen FP32 form against the plain
+    FP64 form, same data, seed, moves and step count.  ESS is the minimum over
+    the lnL, root-height and first-exchangeability traces (Geyer 1992) after
+    10% burn-in; time is the wall time of the run."""
+    from aspartik_gb300.ess import min_ess
+    from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
+
+    out = {}
+    for precision in ("f32", "f64"):
+        s = McmcSettings(model="gtr", precision=precision,
+                         num_categories=wl["spec"]["categories"], seed=4, sample_every=10,
+                         weights=dict(GTR_WEIGHTS), device=device)
+        m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
+        m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
+                         alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
+        m.run(200)  # warm-up outside the timed region
+        t0 = time.perf_counter()
+        m.run(steps)
+        dt = time.perf_counter() - t0
+        traces = {k: m.trace(k)[20:] for k in ("lnl", "root_height", "kappa_or_rate0")}
+        e, per = min_ess(traces)
+        out[precision] = {"steps": steps, "seconds": round(dt, 3),
+                          "us_per_step": round(dt / steps * 1e6, 2),
+                          "ess_min": round(e, 2), "ess": {k: round(v, 2) for k, v in per.items()},
+                          "ess_per_s": round(e / dt, 3),
+                          "mean_lnl": float(np.mean(traces["lnl"][len(traces["lnl"]) // 10:])),
+                          "check_rel": m.check()}
+        m.close()
+    out["ess_per_s_ratio_chosen_vs_plain"] = round(
+        out["f32"]["ess_per_s"] / max(out["f64"]["ess_per_s"], 1e-12), 3)
+    out["note"] = ("same seed and moves (GTR+Gamma4, tree scale, subtree slide, narrow "
+                   "exchange, alpha/birth-rate scale, delta exchanges); no batching or "
+                   "delayed acceptance in this comparison")
+    return out
+
+
 def run_ours(args):
     world, rank, local = dist_setup()
     device = local
@@ -299,6 +336,8 @@ def run_ours(args):
     lnl64 = c64.log_likelihood()
     c64.close()
 
+    mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
@@ -348,6 +387,7 @@ def run_ours(args):
                        "us_per_eval": round(dms * 1e3 / len(paths), 3),
                        "mean_nodes": mean_path,
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
+        "mcmc": mcmc,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
@@ -405,6 +445,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--mcmc-steps", type=int, default=20000,
+                    help="MCMC steps per form for the ESS/s comparison (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -195,6 +195,32 @@ B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
 B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc);
 B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
 
+/* ---- batched evaluation ----------------------------------------------------
+ * Many calculators (chains: replicates or heated copies, each with its own
+ * alignment, tree and model) evaluated by one launch.  Members stage their
+ * proposals with b3g_calculator_stage_lengths (same arguments as
+ * b3g_calculator_propose_lengths, host work only); b3g_batch_run replays one
+ * CUDA graph that copies every member's staged block, builds all transition
+ * tables with one kernel and prunes every member's pattern tiles with one
+ * persistent kernel (tiles handed out by an atomic counter, costliest member
+ * first); b3g_batch_log_likelihoods waits and returns one value per member
+ * (NaN for members with nothing staged).  Members must use the FP32 chosen
+ * form and one device; a calculator belongs to at most one batch; accept and
+ * reject stay per member. */
+B3G_API b3g_status b3g_batch_create(b3g_calculator *const *members,
+				    uint32_t count, b3g_batch **out);
+B3G_API void b3g_batch_destroy(b3g_batch *batch);
+B3G_API b3g_status b3g_calculator_stage_lengths(b3g_calculator *calc,
+						const uint32_t *internals,
+						const uint32_t *children,
+						uint32_t n,
+						const double *lengths,
+						double clock_rate);
+B3G_API b3g_status b3g_batch_run(b3g_batch *batch);
+B3G_API b3g_status b3g_batch_log_likelihoods(b3g_batch *batch, double *out);
+/* Device time of the last replay (events inside the graph), ms. */
+B3G_API b3g_status b3g_batch_last_ms(b3g_batch *batch, float *ms);
+
 /* ---- native MCMC driver ---------------------------------------------------
  * The caller side of the path: b3's MCMC step (crates/b3/src/mcmc.rs:
  * 314-393) in C++ -- operator proposal, prior (reject at -inf before any
