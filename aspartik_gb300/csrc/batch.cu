@@ -130,7 +130,11 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		// capture one step as a graph
 		check_cuda(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal),
 			   "begin capture");
-		check_cuda(cudaEventRecord(ev0_, stream_), "event");
+		// external event-record nodes: the events are recorded each time
+		// the graph runs and can be waited on outside it
+		check_cuda(cudaEventRecordWithFlags(ev0_, stream_,
+						    cudaEventRecordExternal),
+			   "event");
 		check_cuda(cudaMemcpyAsync(d_steps_, h_steps_, sizeof(MemberStep) * M,
 					   cudaMemcpyHostToDevice, stream_),
 			   "steps copy");
@@ -150,11 +154,11 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double) * M,
 					   cudaMemcpyDeviceToHost, stream_),
 			   "lnl copy");
-		check_cuda(cudaEventRecord(ev1_, stream_), "event");
+		check_cuda(cudaEventRecordWithFlags(ev1_, stream_,
+						    cudaEventRecordExternal),
+			   "event");
 		check_cuda(cudaStreamEndCapture(stream_, &graph_), "end capture");
 		check_cuda(cudaGraphInstantiate(&exec_, graph_, 0), "instantiate");
-		for (Calculator *c : members_)
-			c->batch_done_ = ev1_;
 	} catch (...) {
 		release();
 		throw;
@@ -210,7 +214,8 @@ void Batch::run()
 {
 	check_cuda(cudaSetDevice(device_), "cudaSetDevice");
 	// the previous replay reads h_steps_: it must be done
-	check_cuda(cudaEventSynchronize(ev1_), "previous batch");
+	if (ran_)
+		check_cuda(cudaEventSynchronize(ev1_), "previous batch");
 	const uint32_t M = (uint32_t)members_.size();
 	for (uint32_t k = 0; k < M; ++k) {
 		Calculator *c = members_[order_[k]];
@@ -239,6 +244,9 @@ void Batch::run()
 			c->stream_dirty_ = false;
 		}
 	check_cuda(cudaGraphLaunch(exec_, stream_), "graph launch");
+	if (!ran_) // from now on members wait for the replay before restaging
+		for (Calculator *c : members_)
+			c->batch_done_ = ev1_;
 	ran_ = true;
 }
 
