@@ -239,6 +239,78 @@ def cpu_oracle_eval(wl, num_threads: int, pattern_limit: int | None = None):
     return dt, P, calcs[0].num_threads(), lnl
 
 
+def batched(device: int, steps: int, warmup: int, chains: int = 32, seed: int = 4) -> dict:
+    """Many chains in one launch: `chains` calculators with taxa uniform on
+    24..200 and sites log-uniform on 500..50,000 (i.i.d. random bases, as
+    Msa::random), GTR+Gamma4, each step one CUDA-graph replay evaluating every
+    chain.  Reports whole-tree evaluations (all chains, aggregate algorithmic
+    GB/s) and dirty-path evaluations (a random node's path in every chain)."""
+    from aspartik_gb300.calculator import Batch, Calculator
+
+    rng = np.random.default_rng(seed)
+    members, tops, whole = [], [], []
+    total_bytes, patterns = 0, 0
+    for _ in range(chains):
+        L = int(rng.integers(24, 201))
+        N = int(np.exp(rng.uniform(np.log(500), np.log(50000))))
+        tree = sim.yule_tree(L, rng, root_height=1.0)
+        leaves, weights, _ = sim.deduplicate(sim.random_dna(L, N, rng))
+        pi = sim.dirichlet([5.0] * 4, rng)
+        calc = Calculator.GB300(device, "f32").make4(leaves, leaves.shape[1], num_categories=4)
+        calc.set_weights(weights)
+        calc.set_reversible(rng.gamma(2.0, 1.0, size=6), pi)
+        calc.set_gamma(0.5)
+        top = schedule.Topology(tree.parents, tree.heights)
+        members.append(calc)
+        tops.append(top)
+        whole.append(top.full())
+        P = leaves.shape[1]
+        patterns += P
+        total_bytes += schedule.algorithmic_bytes(top, whole[-1][0], P, 4, 4, w=4, e_b=4, w_p=4)
+    batch = Batch(members)
+
+    def step(lists):
+        for calc, lst in zip(members, lists):
+            calc.stage_lengths(*lst, 1.0)
+        batch.run()
+        return batch.log_likelihoods()
+
+    for _ in range(warmup):
+        step(whole)
+    dev_ms = 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lnl = step(whole)
+        dev_ms += batch.last_ms()
+    wall = time.perf_counter() - t0
+    # dirty paths
+    paths = [[top.path(int(v)) for v in rng.integers(top.L, 2 * top.L - 1, size=8)]
+             for top in tops]
+    dsteps = max(steps, 50)
+    for k in range(warmup):
+        step([p[k % 8] for p in paths])
+    t0 = time.perf_counter()
+    dms = 0.0
+    for k in range(dsteps):
+        step([p[k % 8] for p in paths])
+        dms += batch.last_ms()
+    dwall = time.perf_counter() - t0
+    batch.close()
+    for m in members:
+        m.close()
+    return {"chains": chains, "patterns_total": patterns, "categories": 4,
+            "whole_tree": {"value": round(steps * total_bytes / (dev_ms * 1e-3) / 1e9, 2),
+                           "unit": "GB/s", "device_ms_per_step": round(dev_ms / steps, 4),
+                           "wall_ms_per_step": round(wall * 1e3 / steps, 4),
+                           "bytes_per_step": total_bytes,
+                           "finite": bool(np.isfinite(lnl).all())},
+            "dirty_path": {"device_us_per_step": round(dms * 1e3 / dsteps, 2),
+                           "wall_us_per_step": round(dwall * 1e6 / dsteps, 2),
+                           "chain_evaluations_per_s": round(chains * dsteps / dwall, 1)},
+            "launch": "one CUDA graph per step: staged copies, one transition kernel, one "
+                      "persistent pruning kernel, read-back"}
+
+
 def mcmc_ess(wl, steps: int, device: int) -> dict:
     """ESS per second of the cold chain, chosen FP32 form against the plain
     FP64 form, same data, seed, moves and step count.  ESS is the minimum over
@@ -337,6 +409,7 @@ def run_ours(args):
     c64.close()
 
     mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
+    batch = None if args.no_batch else batched(device, min(args.steps, 200), args.warmup)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -388,6 +461,7 @@ def run_ours(args):
                        "mean_nodes": mean_path,
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
+        "batched": batch,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
@@ -445,6 +519,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-chains leg")
     ap.add_argument("--mcmc-steps", type=int, default=20000,
                     help="MCMC steps per form for the ESS/s comparison (0 = skip)")
     args = ap.parse_args()
