@@ -97,6 +97,11 @@ class McmcConfig(ct.Structure):
         ("tune_every", ct.c_uint32),
         ("device", ct.c_int32),
         ("op_weights", ct.c_double * OP_COUNT),
+        ("da_pilot_steps", ct.c_uint32),
+        ("da_epochs", ct.c_uint32),
+        ("da_hidden", ct.c_uint32),
+        ("da_reserved", ct.c_uint32),
+        ("da_drift_limit", ct.c_double),
     ]
 
 
@@ -136,6 +141,18 @@ SIGNATURES = {
     "b3g_calculator_span_begin": (ct.c_int, [_vp]),
     "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
     "b3g_prune_noalloc": (ct.c_int, [ct.POINTER(PruneBuffers), _vp]),
+    "b3g_surrogate_create": (ct.c_int, [ct.c_uint32, ct.c_uint32, ct.c_uint64, ct.c_int32,
+                                        ct.POINTER(_vp)]),
+    "b3g_surrogate_destroy": (None, [_vp]),
+    "b3g_surrogate_num_params": (ct.c_uint32, [_vp]),
+    "b3g_surrogate_get_params": (ct.c_int, [_vp, _f32p]),
+    "b3g_surrogate_set_params": (ct.c_int, [_vp, _f32p]),
+    "b3g_surrogate_forward": (ct.c_int, [_vp, _f32p, ct.c_uint32, _f32p]),
+    "b3g_surrogate_loss_grad": (ct.c_int, [_vp, _f32p, _f32p, _f32p, ct.c_uint32, _f32p,
+                                           _f32p]),
+    "b3g_surrogate_train": (ct.c_int, [_vp, _f32p, _f32p, _f32p, ct.c_uint32, ct.c_uint32,
+                                       ct.c_uint32, ct.c_float, ct.c_uint64, _f32p]),
+    "b3g_surrogate_delta": (ct.c_int, [_vp, _f32p, _f32p, _f32p]),
     "b3g_batch_create": (ct.c_int, [ct.POINTER(_vp), ct.c_uint32, ct.POINTER(_vp)]),
     "b3g_batch_destroy": (None, [_vp]),
     "b3g_calculator_stage_lengths": (
@@ -154,6 +171,7 @@ SIGNATURES = {
     "b3g_mcmc_operator_stats": (ct.c_int, [_vp, ct.c_uint32, ct.POINTER(ct.c_uint64), _f64p]),
     "b3g_mcmc_swaps": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_check": (ct.c_int, [_vp, _f64p]),
+    "b3g_mcmc_da_stats": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), _f64p]),
     "b3g_mcmc_chain_state": (ct.c_int, [_vp, ct.c_uint32, _u32p, _f64p, _f64p, _f64p]),
 }
 

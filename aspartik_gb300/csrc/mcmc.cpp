@@ -246,6 +246,8 @@ void Mcmc::propose(Chain &ch)
 	ch.op = op;
 	ch.hastings = 0.0;
 	ch.status = 0;
+	ch.local = false;
+	ch.screened = false;
 	const double f = ops_[op].tuning;
 	auto scale_factor = [&]() {
 		// sample_range(f, 1 / f, Uniform(0, 1)) (operators/_util.py)
@@ -294,8 +296,13 @@ void Mcmc::propose(Chain &ch)
 		const uint32_t gp = t.parent_of(parent);
 		const uint32_t uncle = t.other_child(gp, parent);
 		if (t.height(uncle) < t.height(parent)) {
-			if (!t.swap_parents(node, uncle))
+			features(ch, parent, ch.feat_old);
+			if (!t.swap_parents(node, uncle)) {
 				ch.status = 1;
+			} else {
+				features(ch, parent, ch.feat_new);
+				ch.local = true;
+			}
 		} else {
 			ch.status = 1;
 		}
@@ -310,6 +317,7 @@ void Mcmc::propose(Chain &ch)
 		const uint32_t parent = t.parent_of(node);
 		const uint32_t gp = t.parent_of(parent);
 		const uint32_t sibling = t.other_child(parent, node);
+		features(ch, parent, ch.feat_old);
 		// distribution Uniform(-0.5, 0.5) times the tuning factor
 		const double delta = (ch.rng.uniform() - 0.5) * f;
 		const double old_h = t.height(parent);
@@ -362,6 +370,8 @@ void Mcmc::propose(Chain &ch)
 			}
 		}
 		t.set_height(parent, new_h);
+		features(ch, parent, ch.feat_new);
+		ch.local = true;
 		break;
 	}
 	default:
@@ -401,7 +411,99 @@ void Mcmc::launch(Chain &ch)
 	ch.launched = true;
 }
 
-// Metropolis-Hastings and finalize_step (mcmc.rs:337-393).
+// Surrogate inputs around `center` (see kDaInputs).
+void Mcmc::features(const Chain &ch, uint32_t center, float *out) const
+{
+	const DatedTree &t = *ch.tree;
+	auto lg = [](double x) { return (float)std::log(std::max(x, 1e-12)); };
+	const uint32_t p = t.parent_of(center);
+	out[0] = p != kTombstone ? lg(t.edge_length(center)) : 0.0f;
+	out[1] = lg(t.edge_length(t.left(center)));
+	out[2] = lg(t.edge_length(t.right(center)));
+	out[3] = out[4] = 0.0f;
+	if (p != kTombstone) {
+		out[3] = lg(t.edge_length(t.other_child(p, center)));
+		if (t.parent_of(p) != kTombstone)
+			out[4] = lg(t.edge_length(p));
+	}
+	for (uint32_t k = 0; k < 6; ++k)
+		out[5 + k] = cfg_.model == 1 ? lg(ch.rates.v[k])
+					     : (k == 0 ? lg(ch.kappa.v) : 0.0f);
+	for (uint32_t k = 0; k < 3; ++k)
+		out[11 + k] = (float)ch.freqs.v[k];
+}
+
+// Stage one of delayed acceptance (Christen and Fox, "Markov chain Monte
+// Carlo using an approximation", J. Comput. Graph. Stat. 14(4), 2005): the
+// proposal passes with probability min(1, r*), r* its MH ratio with the
+// surrogate difference in place of the exact log-likelihood difference.
+void Mcmc::screen(Chain &ch)
+{
+	float xn[kDaInputs], xo[kDaInputs];
+	for (uint32_t k = 0; k < kDaInputs; ++k) {
+		xn[k] = (ch.feat_new[k] - in_mean_[k]) * in_scale_[k];
+		xo[k] = (ch.feat_old[k] - in_mean_[k]) * in_scale_[k];
+	}
+	ch.da_delta = out_scale_ * (double)surrogate_->delta(xn, xo);
+	const double log_r1 =
+		ch.beta * (ch.da_delta + ch.prior_new - ch.prior_cache) + ch.hastings;
+	if (log_r1 > std::log(ch.rng.uniform())) {
+		ch.screened = true;
+	} else {
+		ch.status = 3;
+		++da_.stage1_rejects;
+	}
+}
+
+void Mcmc::train_surrogate()
+{
+	const size_t n = pilot_delta_.size();
+	if (n < 64) { // too few pairs: stay with the exact chain
+		da_.fallback = 1;
+		return;
+	}
+	for (uint32_t k = 0; k < kDaInputs; ++k) {
+		double s = 0.0, s2 = 0.0;
+		for (size_t i = 0; i < n; ++i) {
+			const double a = pilot_old_[i * kDaInputs + k];
+			const double b = pilot_new_[i * kDaInputs + k];
+			s += a + b;
+			s2 += a * a + b * b;
+		}
+		const double mean = s / (2.0 * n);
+		const double var = std::max(s2 / (2.0 * n) - mean * mean, 0.0);
+		in_mean_[k] = (float)mean;
+		in_scale_[k] = var > 1e-20 ? (float)(1.0 / std::sqrt(var)) : 0.0f;
+	}
+	double m = 0.0, m2 = 0.0;
+	for (const float d : pilot_delta_) {
+		m += d;
+		m2 += (double)d * d;
+	}
+	const double dvar = m2 / n - (m / n) * (m / n);
+	out_scale_ = dvar > 1e-12 ? std::sqrt(dvar) : 1.0;
+	std::vector<float> xo(pilot_old_.size()), xn(pilot_new_.size()), dl(n);
+	for (size_t i = 0; i < n; ++i) {
+		for (uint32_t k = 0; k < kDaInputs; ++k) {
+			xo[i * kDaInputs + k] =
+				(pilot_old_[i * kDaInputs + k] - in_mean_[k]) * in_scale_[k];
+			xn[i * kDaInputs + k] =
+				(pilot_new_[i * kDaInputs + k] - in_mean_[k]) * in_scale_[k];
+		}
+		dl[i] = (float)(pilot_delta_[i] / out_scale_);
+	}
+	surrogate_ = std::make_unique<Mlp>(kDaInputs, cfg_.da_hidden, cfg_.seed ^ 0xDAu,
+					   cfg_.device);
+	da_.train_loss = surrogate_->train(xn.data(), xo.data(), dl.data(),
+					   (uint32_t)n, cfg_.da_epochs, 512, 1e-3f,
+					   cfg_.seed ^ 0x7Au);
+	da_active_ = true;
+	drift_.assign(200, 0.0);
+	drift_pos_ = 0;
+}
+
+// Metropolis-Hastings and finalize_step (mcmc.rs:337-393); for a screened
+// proposal, stage two of delayed acceptance: min(1, r / r*).
 void Mcmc::finish(Chain &ch)
 {
 	OpStats &st = ops_[ch.op];
@@ -411,11 +513,44 @@ void Mcmc::finish(Chain &ch)
 				   : batch_    ? batch_lnl_[ch.index]
 					       : ch.calc->log_likelihood();
 		ch.lnl_new = lnl;
+		if (ch.launched)
+			++da_.exact_evaluations;
 		if (lnl != kNegInf && !std::isnan(lnl)) {
-			const double new_post = lnl + ch.prior_new;
-			const double old_post = ch.lnl_cache + ch.prior_cache;
-			const double ratio = ch.beta * (new_post - old_post) + ch.hastings;
-			accept = ratio > std::log(ch.rng.uniform());
+			const double dlnl = lnl - ch.lnl_cache;
+			if (ch.screened) {
+				const double err = dlnl - ch.da_delta;
+				accept = ch.beta * err > std::log(ch.rng.uniform());
+				++(accept ? da_.stage2_accepts : da_.stage2_rejects);
+				// drift of the screen: RMS of the last window of errors
+				drift_[drift_pos_++ % drift_.size()] = err * err;
+				if (drift_pos_ >= drift_.size()) {
+					double s = 0.0;
+					for (const double e2 : drift_)
+						s += e2;
+					da_.drift_rms = std::sqrt(s / drift_.size());
+					if (cfg_.da_drift_limit > 0.0 &&
+					    da_.drift_rms > cfg_.da_drift_limit) {
+						da_active_ = false; // back to the exact chain
+						da_.fallback = 1;
+					}
+				}
+			} else {
+				const double new_post = lnl + ch.prior_new;
+				const double old_post = ch.lnl_cache + ch.prior_cache;
+				const double ratio =
+					ch.beta * (new_post - old_post) + ch.hastings;
+				accept = ratio > std::log(ch.rng.uniform());
+			}
+			// pilot pairs for the surrogate
+			if (ch.local && cfg_.da_pilot_steps && !surrogate_ &&
+			    da_.fallback == 0 && std::isfinite(dlnl)) {
+				pilot_old_.insert(pilot_old_.end(), ch.feat_old,
+						  ch.feat_old + kDaInputs);
+				pilot_new_.insert(pilot_new_.end(), ch.feat_new,
+						  ch.feat_new + kDaInputs);
+				pilot_delta_.push_back((float)dlnl);
+				++da_.pilot_pairs;
+			}
 		}
 	}
 	if (ch.status == 1)
@@ -436,7 +571,7 @@ void Mcmc::finish(Chain &ch)
 		ch.lnl_cache = ch.lnl_new;
 		ch.prior_cache = ch.prior_new;
 	} else {
-		if (ch.status == 0) {
+		if (ch.status == 0 || ch.status == 3) {
 			++st.rejects;
 			++st.window_rejects;
 		}
@@ -536,6 +671,8 @@ void Mcmc::run(uint64_t steps)
 			ch->prior_new = prior(*ch);
 			if (ch->prior_new == kNegInf)
 				ch->status = 2; // mcmc.rs:331-335
+			else if (da_active_ && ch->local)
+				screen(*ch);
 		}
 		// every chain's device work is queued before any result is read
 		bool any = false;
@@ -551,6 +688,8 @@ void Mcmc::run(uint64_t steps)
 		for (auto &ch : chains_)
 			finish(*ch);
 		++step_;
+		if (cfg_.da_pilot_steps && step_ == cfg_.da_pilot_steps && !surrogate_)
+			train_surrogate();
 		if (cfg_.swap_every && step_ % cfg_.swap_every == 0)
 			swap_temperatures();
 		if (cfg_.tune_every && step_ % cfg_.tune_every == 0)

@@ -14,6 +14,7 @@
 
 #include "batch.hpp"
 #include "calculator.hpp"
+#include "mlp.hpp"
 #include "tree.hpp"
 
 #include <cstdint>
@@ -104,6 +105,23 @@ struct McmcConfig {
 	uint32_t tune_every;  // steps between operator tunings, 0 = never
 	int32_t device;
 	double weights[kOpCount];
+	// delayed acceptance (0 pilot steps: off)
+	uint32_t da_pilot_steps;
+	uint32_t da_epochs;
+	uint32_t da_hidden;
+	double da_drift_limit;
+};
+
+// Inputs of the surrogate: 5 branch lengths around the node a tree move
+// changes (its parent edge, its two child edges, its sibling's edge and its
+// parent's edge, log scale) and 9 model parameters (log exchangeabilities
+// or log kappa, three frequencies).
+constexpr uint32_t kDaInputs = 14;
+
+struct DaStats {
+	uint64_t pilot_pairs = 0, stage1_rejects = 0, stage2_accepts = 0,
+		 stage2_rejects = 0, exact_evaluations = 0, fallback = 0;
+	double train_loss = 0.0, drift_rms = 0.0;
 };
 
 struct Chain {
@@ -122,7 +140,11 @@ struct Chain {
 	// per-step state
 	uint32_t op = 0;
 	double hastings = 0.0;
-	int status = 0; // 0 pending, 1 abort, 2 prior reject
+	int status = 0; // 0 pending, 1 abort, 2 prior reject, 3 stage-1 reject
+	bool local = false;   // a tree move around one node (surrogate inputs)
+	bool screened = false; // passed stage one of delayed acceptance
+	double da_delta = 0.0; // surrogate f(x_new) - f(x_old)
+	float feat_old[kDaInputs], feat_new[kDaInputs];
 	std::vector<uint32_t> internals, children;
 	std::vector<double> lengths;
 	explicit Chain(uint64_t seed) : rng(seed) {}
@@ -145,6 +167,7 @@ class Mcmc {
 		return trace_[field];
 	}
 	void op_stats(uint32_t op, uint64_t out[4], double *tuning) const;
+	const DaStats &da_stats() const { return da_; }
 	uint64_t swaps_accepted() const { return swaps_accepted_; }
 	uint64_t swaps_tried() const { return swaps_tried_; }
 	uint64_t steps_done() const { return step_; }
@@ -165,6 +188,9 @@ class Mcmc {
 	void tune();
 	void record();
 	double send_model(Chain &ch, bool mark_all);
+	void features(const Chain &ch, uint32_t center, float *out) const;
+	void screen(Chain &ch);
+	void train_surrogate();
 
 	McmcConfig cfg_;
 	std::vector<std::unique_ptr<Chain>> chains_;
@@ -179,6 +205,17 @@ class Mcmc {
 	uint32_t tune_rounds_ = 0;
 	Rng swap_rng_;
 	std::vector<double> trace_[7];
+
+	// delayed acceptance: pilot pairs, the trained surrogate, input and
+	// output normalisation, the drift window of (exact - surrogate)
+	std::unique_ptr<Mlp> surrogate_;
+	bool da_active_ = false;
+	std::vector<float> pilot_old_, pilot_new_, pilot_delta_;
+	float in_mean_[kDaInputs] = {}, in_scale_[kDaInputs] = {};
+	double out_scale_ = 1.0;
+	std::vector<double> drift_;
+	size_t drift_pos_ = 0;
+	DaStats da_;
 };
 
 } // namespace b3g

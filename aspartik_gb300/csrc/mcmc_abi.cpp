@@ -66,6 +66,18 @@ B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
 		c.tune_every = config->tune_every;
 		c.device = config->device;
 		std::memcpy(c.weights, config->op_weights, sizeof(c.weights));
+		if (config->da_reserved != 0)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "da_reserved must be 0");
+		if (config->da_pilot_steps &&
+		    (config->da_hidden < 32 || config->da_hidden % 32 ||
+		     config->da_hidden > 1024 || config->da_epochs < 1))
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "delayed acceptance needs da_hidden a multiple "
+					 "of 32 in 32..1024 and da_epochs >= 1");
+		c.da_pilot_steps = config->da_pilot_steps;
+		c.da_epochs = config->da_epochs;
+		c.da_hidden = config->da_hidden;
+		c.da_drift_limit = config->da_drift_limit;
 		auto *m = new b3g::Mcmc(c, num_leaves, num_patterns, samples,
 					weights, parents, heights);
 		*out = reinterpret_cast<b3g_mcmc *>(m);
@@ -127,6 +139,24 @@ B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
 		*tried = mcmc_of(mcmc)->swaps_tried();
 		*accepted = mcmc_of(mcmc)->swaps_accepted();
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_da_stats(b3g_mcmc *mcmc, uint64_t *counts,
+				     double *values)
+{
+	return guarded([&] {
+		if (!counts || !values)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		const b3g::DaStats &d = mcmc_of(mcmc)->da_stats();
+		counts[0] = d.pilot_pairs;
+		counts[1] = d.stage1_rejects;
+		counts[2] = d.stage2_accepts;
+		counts[3] = d.stage2_rejects;
+		counts[4] = d.exact_evaluations;
+		counts[5] = d.fallback;
+		values[0] = d.train_loss;
+		values[1] = d.drift_rms;
 	});
 }
 

@@ -1,0 +1,520 @@
+// mlp.cu -- training and inference kernels of the delayed-acceptance
+// surrogate (see mlp.hpp).
+//
+// Layers are stored flat, layer l as W_l [out][in] row-major followed by
+// b_l [out].  Hidden layers use GELU in its tanh form (Hendrycks and
+// Gimpel, "Gaussian Error Linear Units", 2016):
+//     gelu(x) = x/2 (1 + tanh(u)),  u = sqrt(2/pi) (x + 0.044715 x^3).
+// Products go through one shared-memory tiled FP32 GEMM kernel with
+// optional transposes; Adam (Kingma and Ba, 2015) updates the parameters.
+#include "calculator.hpp"
+#include "mlp.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+
+namespace b3g {
+namespace {
+
+constexpr float kGeluC = 0.7978845608028654f; // sqrt(2 / pi)
+constexpr float kGeluA = 0.044715f;
+
+__device__ __forceinline__ float gelu(float x)
+{
+	const float u = kGeluC * (x + kGeluA * x * x * x);
+	return 0.5f * x * (1.0f + tanhf(u));
+}
+
+__device__ __forceinline__ float gelu_grad(float x)
+{
+	const float u = kGeluC * (x + kGeluA * x * x * x);
+	const float t = tanhf(u);
+	return 0.5f * (1.0f + t) +
+	       0.5f * x * (1.0f - t * t) * kGeluC * (1.0f + 3.0f * kGeluA * x * x);
+}
+
+// C[M][N] = sum_k A'(m, k) B'(k, n) (+ bias[n]); A'(m, k) = TA ? A[k][m] :
+// A[m][k] with row stride lda, B'(k, n) = TB ? B[n][k] : B[k][n] with row
+// stride ldb.  With `act` the GELU of C goes to Cact and C itself to C.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) gemm_kernel(const float *__restrict__ A,
+						    const float *__restrict__ B,
+						    const float *__restrict__ bias,
+						    float *__restrict__ C,
+						    float *__restrict__ Cact,
+						    uint32_t M, uint32_t N, uint32_t K,
+						    uint32_t lda, uint32_t ldb)
+{
+	constexpr int T = 16;
+	__shared__ float sa[T][T + 1];
+	__shared__ float sb[T][T + 1];
+	const uint32_t tx = threadIdx.x, ty = threadIdx.y;
+	const uint32_t m = blockIdx.y * T + ty;
+	const uint32_t n = blockIdx.x * T + tx;
+	float acc = 0.0f;
+	for (uint32_t k0 = 0; k0 < K; k0 += T) {
+		// A' tile rows m, columns k0 + tx
+		{
+			const uint32_t mm = blockIdx.y * T + ty, kk = k0 + tx;
+			float v = 0.0f;
+			if (mm < M && kk < K)
+				v = TA ? A[(size_t)kk * lda + mm] : A[(size_t)mm * lda + kk];
+			sa[ty][tx] = v;
+		}
+		// B' tile rows k0 + ty, columns n
+		{
+			const uint32_t kk = k0 + ty, nn = blockIdx.x * T + tx;
+			float v = 0.0f;
+			if (kk < K && nn < N)
+				v = TB ? B[(size_t)nn * ldb + kk] : B[(size_t)kk * ldb + nn];
+			sb[ty][tx] = v;
+		}
+		__syncthreads();
+#pragma unroll
+		for (int k = 0; k < T; ++k)
+			acc = fmaf(sa[ty][k], sb[k][tx], acc);
+		__syncthreads();
+	}
+	if (m < M && n < N) {
+		if (bias)
+			acc += bias[n];
+		C[(size_t)m * N + n] = acc;
+		if (Cact)
+			Cact[(size_t)m * N + n] = gelu(acc);
+	}
+}
+
+// dZ = dA * gelu'(Z)
+__global__ void gelu_backward_kernel(const float *__restrict__ dA,
+				     const float *__restrict__ Z,
+				     float *__restrict__ dZ, uint32_t count)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < count)
+		dZ[i] = dA[i] * gelu_grad(Z[i]);
+}
+
+// db[o] = sum_n dZ[n][o], summed in row order
+__global__ void column_sum_kernel(const float *__restrict__ dZ,
+				  float *__restrict__ db, uint32_t rows,
+				  uint32_t cols)
+{
+	const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+	if (o >= cols)
+		return;
+	float s = 0.0f;
+	for (uint32_t n = 0; n < rows; ++n)
+		s += dZ[(size_t)n * cols + o];
+	db[o] = s;
+}
+
+// pair objective: rows 0..n-1 hold f(x_new), rows n..2n-1 f(x_old)
+__global__ void pair_loss_kernel(const float *__restrict__ y,
+				 const float *__restrict__ delta,
+				 float *__restrict__ dy, float *__restrict__ loss,
+				 uint32_t n)
+{
+	__shared__ float s[256];
+	float acc = 0.0f;
+	for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+		const float r = y[i] - y[n + i] - delta[i];
+		dy[i] = 2.0f * r / n;
+		dy[n + i] = -2.0f * r / n;
+		acc += r * r;
+	}
+	s[threadIdx.x] = acc;
+	__syncthreads();
+	for (uint32_t st = blockDim.x / 2; st > 0; st >>= 1) {
+		if (threadIdx.x < st)
+			s[threadIdx.x] += s[threadIdx.x + st];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+		*loss = s[0] / n;
+}
+
+__global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g,
+			    float *__restrict__ m, float *__restrict__ v,
+			    uint32_t count, float lr, float b1, float b2,
+			    float c1, float c2, float eps)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= count)
+		return;
+	const float gi = g[i];
+	const float mi = b1 * m[i] + (1.0f - b1) * gi;
+	const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+	m[i] = mi;
+	v[i] = vi;
+	p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// rows of the dataset gathered by index: out[r] = src[idx[r]]
+__global__ void gather_rows_kernel(const float *__restrict__ src,
+				   const uint32_t *__restrict__ idx,
+				   float *__restrict__ out, uint32_t rows,
+				   uint32_t cols)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= rows * cols)
+		return;
+	const uint32_t r = i / cols, c = i - r * cols;
+	out[i] = src[(size_t)idx[r] * cols + c];
+}
+
+// f(x_new) - f(x_old) for one pair in one block of `hidden` threads: each
+// thread owns one unit of every hidden layer, activations live in shared
+// memory.  pair = [x_new (in), x_old (in)], result in pair[2 * in].
+__global__ void mlp_delta_kernel(const float *__restrict__ params,
+				 float *__restrict__ pair, uint32_t in,
+				 uint32_t hidden)
+{
+	extern __shared__ float sh[];
+	float *a = sh;               // [2][hidden]
+	float *b = sh + 2 * hidden;  // [2][hidden]
+	const uint32_t j = threadIdx.x;
+	for (uint32_t k = j; k < 2 * in; k += blockDim.x)
+		a[k] = pair[k];
+	__syncthreads();
+	const float *W = params;
+	uint32_t width = in;
+	for (int layer = 0; layer < 3; ++layer) {
+		const float *bias = W + (size_t)hidden * width;
+		const float *w = W + (size_t)j * width;
+		float z0 = bias[j], z1 = bias[j];
+		for (uint32_t k = 0; k < width; ++k) {
+			const float wk = w[k];
+			z0 = fmaf(wk, a[k], z0);
+			z1 = fmaf(wk, a[width + k], z1);
+		}
+		__syncthreads();
+		b[j] = gelu(z0);
+		b[hidden + j] = gelu(z1);
+		__syncthreads();
+		for (uint32_t k = j; k < 2 * hidden; k += blockDim.x)
+			a[k] = b[k];
+		__syncthreads();
+		W = bias + hidden;
+		width = hidden;
+	}
+	// output unit: W [1][hidden], b [1]
+	__shared__ float s0[32], s1[32];
+	float p0 = W[j] * a[j], p1 = W[j] * a[hidden + j];
+	for (int off = 16; off > 0; off >>= 1) {
+		p0 += __shfl_down_sync(0xffffffffu, p0, off);
+		p1 += __shfl_down_sync(0xffffffffu, p1, off);
+	}
+	if ((j & 31u) == 0) {
+		s0[j >> 5] = p0;
+		s1[j >> 5] = p1;
+	}
+	__syncthreads();
+	if (j == 0) {
+		float y0 = 0.0f, y1 = 0.0f;
+		for (uint32_t w2 = 0; w2 < (hidden + 31) / 32; ++w2) {
+			y0 += s0[w2];
+			y1 += s1[w2];
+		}
+		pair[2 * in] = y0 - y1; // the biases cancel
+	}
+}
+
+dim3 gemm_grid(uint32_t M, uint32_t N)
+{
+	return dim3((N + 15) / 16, (M + 15) / 16);
+}
+
+} // namespace
+
+Mlp::Mlp(uint32_t in_dim, uint32_t hidden, uint64_t seed, int device)
+    : in_(in_dim), hidden_(hidden), device_(device)
+{
+	if (in_dim < 1 || in_dim > hidden || hidden < 32 || hidden > 1024 ||
+	    hidden % 32 != 0)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "surrogate: 1 <= inputs <= 256, hidden a multiple of 32 "
+			    "in 32..1024");
+	check_cuda(cudaSetDevice(device), "cudaSetDevice");
+	dims_[0] = in_dim;
+	dims_[1] = dims_[2] = dims_[3] = hidden;
+	dims_[4] = 1;
+	uint32_t off = 0;
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		w_off_[l] = off;
+		off += dims_[l + 1] * dims_[l];
+		b_off_[l] = off;
+		off += dims_[l + 1];
+	}
+	n_params_ = off;
+	// uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases
+	std::vector<float> p(n_params_, 0.0f);
+	std::mt19937_64 gen(seed);
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		const float r = 1.0f / std::sqrt(static_cast<float>(dims_[l]));
+		std::uniform_real_distribution<float> u(-r, r);
+		for (uint32_t k = 0; k < dims_[l + 1] * dims_[l]; ++k)
+			p[w_off_[l] + k] = u(gen);
+	}
+	check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+	const size_t bytes = sizeof(float) * n_params_;
+	check_cuda(cudaMalloc(&d_params_, bytes), "surrogate params");
+	check_cuda(cudaMalloc(&d_grad_, bytes), "surrogate grads");
+	check_cuda(cudaMalloc(&d_m_, bytes), "adam m");
+	check_cuda(cudaMalloc(&d_v_, bytes), "adam v");
+	check_cuda(cudaMemcpy(d_params_, p.data(), bytes, cudaMemcpyHostToDevice), "params");
+	check_cuda(cudaMemset(d_m_, 0, bytes), "adam m");
+	check_cuda(cudaMemset(d_v_, 0, bytes), "adam v");
+	check_cuda(cudaMalloc(&d_pair_, sizeof(float) * (2 * in_ + 4)), "pair");
+	check_cuda(cudaHostAlloc((void **)&h_pair_, sizeof(float) * (2 * in_ + 4),
+				 cudaHostAllocDefault),
+		   "pinned pair");
+}
+
+Mlp::~Mlp()
+{
+	cudaSetDevice(device_);
+	if (stream_)
+		cudaStreamSynchronize(stream_);
+	cudaFree(d_params_);
+	cudaFree(d_grad_);
+	cudaFree(d_m_);
+	cudaFree(d_v_);
+	cudaFree(d_x_);
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		cudaFree(d_z_[l]);
+		cudaFree(d_a_[l]);
+		cudaFree(d_da_[l]);
+	}
+	cudaFree(d_dy_);
+	cudaFree(d_delta_);
+	cudaFree(d_loss_);
+	cudaFree(d_pair_);
+	cudaFreeHost(h_pair_);
+	if (stream_)
+		cudaStreamDestroy(stream_);
+}
+
+void Mlp::ensure_batch(uint32_t rows)
+{
+	if (rows <= cap_)
+		return;
+	cudaFree(d_x_);
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		cudaFree(d_z_[l]);
+		cudaFree(d_a_[l]);
+		cudaFree(d_da_[l]);
+	}
+	cudaFree(d_dy_);
+	cudaFree(d_delta_);
+	cudaFree(d_loss_);
+	cap_ = rows;
+	check_cuda(cudaMalloc(&d_x_, sizeof(float) * rows * in_), "inputs");
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		const size_t sz = sizeof(float) * rows * dims_[l + 1];
+		check_cuda(cudaMalloc(&d_z_[l], sz), "z");
+		check_cuda(cudaMalloc(&d_a_[l], sz), "a");
+		check_cuda(cudaMalloc(&d_da_[l], sz), "da");
+	}
+	d_y_ = d_z_[kLayers - 1];
+	check_cuda(cudaMalloc(&d_dy_, sizeof(float) * rows), "dy");
+	check_cuda(cudaMalloc(&d_delta_, sizeof(float) * rows), "delta");
+	check_cuda(cudaMalloc(&d_loss_, sizeof(float)), "loss");
+}
+
+void Mlp::forward_device(uint32_t rows)
+{
+	const float *in = d_x_;
+	for (uint32_t l = 0; l < kLayers; ++l) {
+		const uint32_t I = dims_[l], O = dims_[l + 1];
+		const bool act = l + 1 < kLayers;
+		gemm_kernel<false, true><<<gemm_grid(rows, O), dim3(16, 16), 0, stream_>>>(
+			in, d_params_ + w_off_[l], d_params_ + b_off_[l], d_z_[l],
+			act ? d_a_[l] : nullptr, rows, O, I, I, I);
+		in = act ? d_a_[l] : d_z_[l];
+	}
+	check_cuda(cudaGetLastError(), "surrogate forward");
+}
+
+void Mlp::backward_device(uint32_t rows)
+{
+	// d_dy_ holds dL/dy for every row
+	const float *dz = d_dy_;
+	for (int l = kLayers - 1; l >= 0; --l) {
+		const uint32_t I = dims_[l], O = dims_[l + 1];
+		const float *a_prev = l == 0 ? d_x_ : d_a_[l - 1];
+		// dW = dZ^T a_prev, db = column sums of dZ
+		gemm_kernel<true, false><<<gemm_grid(O, I), dim3(16, 16), 0, stream_>>>(
+			dz, a_prev, nullptr, d_grad_ + w_off_[l], nullptr, O, I, rows, O, I);
+		column_sum_kernel<<<(O + 127) / 128, 128, 0, stream_>>>(
+			dz, d_grad_ + b_off_[l], rows, O);
+		if (l == 0)
+			break;
+		// dA_prev = dZ W, then through GELU into dZ_prev
+		float *da_prev = d_da_[l - 1];
+		gemm_kernel<false, false><<<gemm_grid(rows, I), dim3(16, 16), 0, stream_>>>(
+			dz, d_params_ + w_off_[l], nullptr, da_prev, nullptr, rows, I, O, O, I);
+		const uint32_t count = rows * I;
+		gelu_backward_kernel<<<(count + 255) / 256, 256, 0, stream_>>>(
+			da_prev, d_z_[l - 1], da_prev, count);
+		dz = da_prev;
+	}
+	check_cuda(cudaGetLastError(), "surrogate backward");
+}
+
+void Mlp::get_params(float *out)
+{
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	check_cuda(cudaMemcpy(out, d_params_, sizeof(float) * n_params_,
+			      cudaMemcpyDeviceToHost),
+		   "read params");
+}
+
+void Mlp::set_params(const float *in)
+{
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	check_cuda(cudaMemcpy(d_params_, in, sizeof(float) * n_params_,
+			      cudaMemcpyHostToDevice),
+		   "write params");
+	check_cuda(cudaMemset(d_m_, 0, sizeof(float) * n_params_), "adam m");
+	check_cuda(cudaMemset(d_v_, 0, sizeof(float) * n_params_), "adam v");
+	adam_t_ = 0;
+}
+
+void Mlp::forward(const float *x, uint32_t n, float *out)
+{
+	check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+	ensure_batch(n);
+	check_cuda(cudaMemcpyAsync(d_x_, x, sizeof(float) * n * in_,
+				   cudaMemcpyHostToDevice, stream_),
+		   "inputs");
+	forward_device(n);
+	check_cuda(cudaMemcpyAsync(out, d_y_, sizeof(float) * n,
+				   cudaMemcpyDeviceToHost, stream_),
+		   "outputs");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+}
+
+float Mlp::loss_grad(const float *x_new, const float *x_old,
+		     const float *delta, uint32_t n, float *grad)
+{
+	check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+	ensure_batch(2 * n);
+	check_cuda(cudaMemcpyAsync(d_x_, x_new, sizeof(float) * n * in_,
+				   cudaMemcpyHostToDevice, stream_),
+		   "inputs");
+	check_cuda(cudaMemcpyAsync(d_x_ + (size_t)n * in_, x_old,
+				   sizeof(float) * n * in_, cudaMemcpyHostToDevice,
+				   stream_),
+		   "inputs");
+	check_cuda(cudaMemcpyAsync(d_delta_, delta, sizeof(float) * n,
+				   cudaMemcpyHostToDevice, stream_),
+		   "deltas");
+	forward_device(2 * n);
+	pair_loss_kernel<<<1, 256, 0, stream_>>>(d_y_, d_delta_, d_dy_, d_loss_, n);
+	backward_device(2 * n);
+	float loss = 0.0f;
+	check_cuda(cudaMemcpyAsync(&loss, d_loss_, sizeof(float),
+				   cudaMemcpyDeviceToHost, stream_),
+		   "loss");
+	if (grad)
+		check_cuda(cudaMemcpyAsync(grad, d_grad_, sizeof(float) * n_params_,
+					   cudaMemcpyDeviceToHost, stream_),
+			   "grads");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	return loss;
+}
+
+float Mlp::train(const float *x_new, const float *x_old, const float *delta,
+		 uint32_t n, uint32_t epochs, uint32_t batch, float lr,
+		 uint64_t seed)
+{
+	if (n < 1 || batch < 1)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "empty training set");
+	check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+	batch = std::min(batch, n);
+	ensure_batch(2 * batch);
+	// the whole data set on the device once: rows [x_new; x_old], deltas
+	float *d_xn = nullptr, *d_xo = nullptr, *d_dl = nullptr;
+	uint32_t *d_idx = nullptr, *h_idx = nullptr;
+	check_cuda(cudaMalloc(&d_xn, sizeof(float) * n * in_), "train x_new");
+	check_cuda(cudaMalloc(&d_xo, sizeof(float) * n * in_), "train x_old");
+	check_cuda(cudaMalloc(&d_dl, sizeof(float) * n), "train deltas");
+	check_cuda(cudaMalloc(&d_idx, sizeof(uint32_t) * batch), "indices");
+	check_cuda(cudaHostAlloc((void **)&h_idx, sizeof(uint32_t) * batch,
+				 cudaHostAllocDefault),
+		   "pinned indices");
+	check_cuda(cudaMemcpy(d_xn, x_new, sizeof(float) * n * in_, cudaMemcpyHostToDevice), "x_new");
+	check_cuda(cudaMemcpy(d_xo, x_old, sizeof(float) * n * in_, cudaMemcpyHostToDevice), "x_old");
+	check_cuda(cudaMemcpy(d_dl, delta, sizeof(float) * n, cudaMemcpyHostToDevice), "deltas");
+	std::vector<uint32_t> order(n);
+	std::iota(order.begin(), order.end(), 0u);
+	std::mt19937_64 gen(seed);
+	const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+	double epoch_loss = 0.0;
+	for (uint32_t e = 0; e < epochs; ++e) {
+		std::shuffle(order.begin(), order.end(), gen);
+		epoch_loss = 0.0;
+		uint32_t batches = 0;
+		for (uint32_t s = 0; s + batch <= n; s += batch) {
+			check_cuda(cudaStreamSynchronize(stream_), "sync");
+			std::memcpy(h_idx, order.data() + s, sizeof(uint32_t) * batch);
+			check_cuda(cudaMemcpyAsync(d_idx, h_idx, sizeof(uint32_t) * batch,
+						   cudaMemcpyHostToDevice, stream_),
+				   "indices");
+			const uint32_t cnt = batch * in_;
+			gather_rows_kernel<<<(cnt + 255) / 256, 256, 0, stream_>>>(
+				d_xn, d_idx, d_x_, batch, in_);
+			gather_rows_kernel<<<(cnt + 255) / 256, 256, 0, stream_>>>(
+				d_xo, d_idx, d_x_ + (size_t)batch * in_, batch, in_);
+			gather_rows_kernel<<<(batch + 255) / 256, 256, 0, stream_>>>(
+				d_dl, d_idx, d_delta_, batch, 1);
+			forward_device(2 * batch);
+			pair_loss_kernel<<<1, 256, 0, stream_>>>(d_y_, d_delta_, d_dy_,
+								 d_loss_, batch);
+			backward_device(2 * batch);
+			++adam_t_;
+			const float c1 = 1.0f - std::pow(b1, (float)adam_t_);
+			const float c2 = 1.0f - std::pow(b2, (float)adam_t_);
+			adam_kernel<<<(n_params_ + 255) / 256, 256, 0, stream_>>>(
+				d_params_, d_grad_, d_m_, d_v_, n_params_, lr, b1, b2,
+				c1, c2, eps);
+			float loss = 0.0f;
+			check_cuda(cudaMemcpyAsync(&loss, d_loss_, sizeof(float),
+						   cudaMemcpyDeviceToHost, stream_),
+				   "loss");
+			check_cuda(cudaStreamSynchronize(stream_), "sync");
+			epoch_loss += loss;
+			++batches;
+		}
+		epoch_loss /= std::max(1u, batches);
+	}
+	cudaFree(d_xn);
+	cudaFree(d_xo);
+	cudaFree(d_dl);
+	cudaFree(d_idx);
+	cudaFreeHost(h_idx);
+	check_cuda(cudaGetLastError(), "training");
+	return static_cast<float>(epoch_loss);
+}
+
+float Mlp::delta(const float *x_new, const float *x_old)
+{
+	std::memcpy(h_pair_, x_new, sizeof(float) * in_);
+	std::memcpy(h_pair_ + in_, x_old, sizeof(float) * in_);
+	check_cuda(cudaMemcpyAsync(d_pair_, h_pair_, sizeof(float) * 2 * in_,
+				   cudaMemcpyHostToDevice, stream_),
+		   "pair");
+	const size_t smem = sizeof(float) * 4 * std::max(hidden_, in_);
+	mlp_delta_kernel<<<1, hidden_, smem, stream_>>>(d_params_, d_pair_, in_, hidden_);
+	check_cuda(cudaGetLastError(), "surrogate inference");
+	check_cuda(cudaMemcpyAsync(h_pair_ + 2 * in_, d_pair_ + 2 * in_, sizeof(float),
+				   cudaMemcpyDeviceToHost, stream_),
+		   "delta");
+	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	return h_pair_[2 * in_];
+}
+
+} // namespace b3g

@@ -42,6 +42,11 @@ class McmcSettings:
     tune_every: int = 1000
     device: int = 0
     weights: dict = field(default_factory=lambda: dict(GTR_WEIGHTS))
+    # delayed acceptance (0 pilot steps: off)
+    da_pilot_steps: int = 0
+    da_epochs: int = 20
+    da_hidden: int = 256
+    da_drift_limit: float = 0.0
 
 
 class Mcmc:
@@ -57,7 +62,9 @@ class Mcmc:
                              else nat.PRECISION_F32,
                              MODELS[settings.model], settings.seed, settings.heat,
                              settings.swap_every, settings.sample_every, settings.tune_every,
-                             settings.device, (ct.c_double * nat.OP_COUNT)(*w))
+                             settings.device, (ct.c_double * nat.OP_COUNT)(*w),
+                             settings.da_pilot_steps, settings.da_epochs, settings.da_hidden,
+                             0, settings.da_drift_limit)
         self._wts = nat.u32(weights)
         self._par = nat.u32(parents)
         self._hei = nat.f64(heights)
@@ -116,6 +123,16 @@ class Mcmc:
         t, a = ct.c_uint64(), ct.c_uint64()
         check(lib.b3g_mcmc_swaps(self._h, ct.byref(t), ct.byref(a)))
         return t.value, a.value
+
+    def da_stats(self) -> dict:
+        counts = (ct.c_uint64 * 6)()
+        values = (ct.c_double * 2)()
+        check(lib.b3g_mcmc_da_stats(self._h, counts, values))
+        keys = ["pilot_pairs", "stage1_rejects", "stage2_accepts", "stage2_rejects",
+                "exact_evaluations", "fallback"]
+        out = {k: int(v) for k, v in zip(keys, counts)}
+        out["train_loss"], out["drift_rms"] = values[0], values[1]
+        return out
 
     def check(self) -> float:
         out = ct.c_double()

@@ -272,6 +272,20 @@ typedef struct b3g_mcmc_config {
 	uint32_t tune_every;     /* steps between operator tunings, 0 = never */
 	int32_t device;
 	double op_weights[B3G_OP_COUNT];
+	/* Delayed acceptance (no counterpart in the reference): after
+	 * da_pilot_steps exact steps a surrogate (14 inputs: 5 branch lengths
+	 * around the moved node and 9 model parameters; da_hidden units per
+	 * hidden layer) is trained for da_epochs on the pilot's tree-move pairs
+	 * and screens later subtree-slide and narrow-exchange proposals; the
+	 * exact likelihood stays the second-stage judge, so the target
+	 * distribution is unchanged.  Screening stops for good when the RMS of
+	 * (exact - surrogate) over the last 200 screened proposals exceeds
+	 * da_drift_limit (0: never).  da_pilot_steps = 0 turns it off. */
+	uint32_t da_pilot_steps;
+	uint32_t da_epochs;
+	uint32_t da_hidden;
+	uint32_t da_reserved; /* must be 0 */
+	double da_drift_limit;
 } b3g_mcmc_config;
 
 /* parents[2L-1] (root: 0xFFFFFFFF) and heights[2L-1] give the start tree of
@@ -298,12 +312,50 @@ B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
 					   uint64_t *counts, double *tuning);
 B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
 				  uint64_t *accepted);
+/* counts = {pilot pairs, stage-1 rejects, stage-2 accepts, stage-2 rejects,
+ * exact evaluations, fallback (1 if screening stopped)};
+ * values = {final training loss, last drift RMS}. */
+B3G_API b3g_status b3g_mcmc_da_stats(b3g_mcmc *mcmc, uint64_t *counts,
+				     double *values);
 /* Re-evaluates every chain from scratch and returns the largest relative
  * difference to its incrementally maintained log-likelihood. */
 B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff);
 B3G_API b3g_status b3g_mcmc_chain_state(b3g_mcmc *mcmc, uint32_t chain,
 					uint32_t *parents, double *heights,
 					double *lnl, double *beta);
+
+/* ---- delayed-acceptance surrogate ------------------------------------------
+ * No counterpart in the reference.  A fully connected network
+ * inputs -> hidden -> hidden -> hidden -> 1 with GELU, FP32, trained and
+ * evaluated by this library's own CUDA kernels.  Parameters are flat: layer
+ * by layer, W [out][in] row-major then b [out].  The training objective is
+ * mean_n (f(x_new,n) - f(x_old,n) - delta_n)^2 (Adam). */
+typedef struct b3g_surrogate b3g_surrogate;
+B3G_API b3g_status b3g_surrogate_create(uint32_t inputs, uint32_t hidden,
+					uint64_t seed, int32_t device,
+					b3g_surrogate **out);
+B3G_API void b3g_surrogate_destroy(b3g_surrogate *s);
+B3G_API uint32_t b3g_surrogate_num_params(const b3g_surrogate *s);
+B3G_API b3g_status b3g_surrogate_get_params(b3g_surrogate *s, float *out);
+B3G_API b3g_status b3g_surrogate_set_params(b3g_surrogate *s,
+					    const float *in);
+/* f(x) for n rows x[n][inputs]. */
+B3G_API b3g_status b3g_surrogate_forward(b3g_surrogate *s, const float *x,
+					 uint32_t n, float *out);
+/* Loss of the pair objective and its gradient (flat, parameter order). */
+B3G_API b3g_status b3g_surrogate_loss_grad(b3g_surrogate *s,
+					   const float *x_new,
+					   const float *x_old,
+					   const float *delta, uint32_t n,
+					   float *loss, float *grad);
+B3G_API b3g_status b3g_surrogate_train(b3g_surrogate *s, const float *x_new,
+				       const float *x_old, const float *delta,
+				       uint32_t n, uint32_t epochs,
+				       uint32_t batch, float lr, uint64_t seed,
+				       float *final_loss);
+/* f(x_new) - f(x_old) for one pair (fused single-block kernel). */
+B3G_API b3g_status b3g_surrogate_delta(b3g_surrogate *s, const float *x_new,
+				       const float *x_old, float *out);
 
 /* ---- allocation-free pruning --------------------------------------------
  * This entry point has no counterpart in the reference.
