@@ -110,7 +110,7 @@ struct MemberStep {
 	uint32_t n;      // dirty entries (0: nothing to evaluate)
 	uint32_t n_runs;
 	uint32_t tips_smem;
-	uint32_t pad;
+	uint32_t tile; // patterns per tile for this step (divides ldp)
 	double clock_rate;
 };
 

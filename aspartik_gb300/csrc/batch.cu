@@ -105,8 +105,10 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 			max_ops = std::max<uint32_t>(
 				max_ops, c->I_ * sizeof(NodeOp) +
 						 ((c->I_ + 4) & ~3u) * sizeof(uint32_t));
-			max_tips = std::max<uint32_t>(max_tips, c->L_ * c->runs_tile_);
-			max_cols = std::max<uint32_t>(max_cols, c->runs_tile_ * c->C_);
+			// a step may use tiles of up to 128 patterns (pick_tile); a
+			// tile's columns never exceed one 512-thread block
+			max_tips = std::max<uint32_t>(max_tips, c->L_ * 128u);
+			max_cols = 512u;
 			max_entries_ = std::max<uint32_t>(max_entries_, c->I_ * 2 * c->C_);
 			if ((uint64_t)c->L_ * 2 * c->C_ * c->ldp_ >= (1ull << 31))
 				narrow = false;
@@ -226,16 +228,17 @@ void Batch::run()
 			check_cuda(cudaEventSynchronize(c->ev_stage_free_), "member stage");
 			s.n = c->staged_n_;
 			s.n_runs = c->n_runs_;
+			s.tile = c->staged_tile_;
 			s.tips_smem = c->staged_tips_smem_;
 			s.clock_rate = c->staged_clock_;
 			c->staged_ = false;
 		} else {
 			s.n = 0;
 			s.n_runs = 0;
+			s.tile = c->runs_tile_;
 			s.tips_smem = 0;
 			s.clock_rate = 1.0;
 		}
-		s.pad = 0;
 	}
 	// members' own streams may still hold model uploads or eigen kernels
 	for (Calculator *c : members_)

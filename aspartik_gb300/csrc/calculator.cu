@@ -434,12 +434,12 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	if (use_runs_ && n <= 4096) {
 		pp.runs = reinterpret_cast<const uint32_t *>(d_stage_ + off_runs_);
 		pp.n_runs = n_runs_;
-		pp.tile = runs_tile_;
+		pp.tile = pick_tile(n);
 		pp.tips_smem = (4ull * tip_children_ >= L_ &&
-				(size_t)L_ * runs_tile_ <= 32u * 1024u)
+				(size_t)L_ * pp.tile <= 32u * 1024u)
 				       ? 1u
 				       : 0u;
-		const uint32_t tiles = ldp_ / runs_tile_;
+		const uint32_t tiles = ldp_ / pp.tile;
 		const uint32_t ctas = std::min(tiles, 2 * num_sms_);
 		check_cuda(launch_prune4_runs(pp, ctas, stream_), "pruning kernel");
 	} else {
@@ -537,8 +537,9 @@ void Calculator::stage_lengths(const uint32_t *internals,
 	staged_ = true;
 	staged_n_ = n;
 	staged_clock_ = clock_rate;
+	staged_tile_ = pick_tile(n);
 	staged_tips_smem_ = (4ull * tip_children_ >= L_ &&
-			     (size_t)L_ * runs_tile_ <= 32u * 1024u)
+			     (size_t)L_ * staged_tile_ <= 32u * 1024u)
 				    ? 1u
 				    : 0u;
 	have_result_ = false; // results come from the batch

@@ -149,6 +149,15 @@ class Calculator {
 	bool staged_ = false;
 	uint32_t staged_n_ = 0;
 	uint32_t staged_tips_smem_ = 0;
+	uint32_t staged_tile_ = 64;
+	// patterns per tile of the run-synchronous walk for the staged list:
+	// path-like lists (runs of one entry) take 128 so that one entry fills
+	// a 512-thread block
+	uint32_t pick_tile(uint32_t n) const
+	{
+		const bool narrow_runs = 2 * n_runs_ > n;
+		return (narrow_runs && 128 * C_ <= 512) ? 128u : runs_tile_;
+	}
 	double staged_clock_ = 1.0;
 	cudaEvent_t batch_done_ = nullptr;
 	// work was queued on this calculator's own stream since a batch last

@@ -170,28 +170,81 @@ __device__ void transition4(const ModelDev *__restrict__ m, double d,
 	}
 }
 
+// FP32 chosen form: P(t) in single precision from the FP64 eigensystem
+// (the decomposition of Q is the only FP64 work of this step; on GB300 FP64
+// issues at 1/64 of the FP32 rate).  The shortcut tests stay in FP64.
+__device__ void transition4f(const ModelDev *__restrict__ m, double d,
+			     float P[16])
+{
+	if (m->shortcuts && d > 20.0) {
+		for (int i = 0; i < 4; i++)
+			for (int j = 0; j < 4; j++)
+				P[i * 4 + j] = (float)m->pi[j];
+		return;
+	}
+	if (m->shortcuts && d < 1e-10) {
+		for (int i = 0; i < 4; i++)
+			for (int j = 0; j < 4; j++)
+				P[i * 4 + j] = i == j ? 1.0f : (float)(m->Q[i * 4 + j] * d);
+		return;
+	}
+	const float df = (float)d;
+	float e[4];
+	for (int k = 0; k < 4; k++)
+		e[k] = expf((float)m->lambda[k] * df);
+	for (int i = 0; i < 4; i++) {
+		const float t0 = (float)m->V[i * 4 + 0] * e[0];
+		const float t1 = (float)m->V[i * 4 + 1] * e[1];
+		const float t2 = (float)m->V[i * 4 + 2] * e[2];
+		const float t3 = (float)m->V[i * 4 + 3] * e[3];
+		for (int j = 0; j < 4; j++) {
+			float s = t0 * (float)m->Vinv[0 * 4 + j];
+			s = fmaf(t1, (float)m->Vinv[1 * 4 + j], s);
+			s = fmaf(t2, (float)m->Vinv[2 * 4 + j], s);
+			s = fmaf(t3, (float)m->Vinv[3 * 4 + j], s);
+			P[i * 4 + j] = s;
+		}
+	}
+}
+
 template <typename R>
-__global__ void __launch_bounds__(128) ptab4_kernel(PtabParams prm)
+__global__ void __launch_bounds__(32) ptab4_kernel(PtabParams prm)
 {
 	const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
 	if (id >= prm.n * 2u * prm.C)
 		return;
 	const uint32_t c = id % prm.C;
 	const uint32_t es = id / prm.C; // dirty index * 2 + side
-	double P[16];
-	if (prm.matrices) {
-		const double *src = prm.matrices + (size_t)id * 16;
-		for (int k = 0; k < 16; k++)
-			P[k] = src[k];
-	} else {
-		const double d = prm.lengths[es] *
-				 (prm.clock_rate * prm.model->cat_rates[c]);
-		transition4(prm.model, d, P);
-	}
 	R *out = (R *)prm.ptab + (size_t)id * 20;
-	for (int k = 0; k < 4; k++)
-		for (int j = 0; j < 4; j++)
-			out[k * 4 + j] = (R)P[j * 4 + k];
+	if constexpr (sizeof(R) == 4) {
+		float P[16];
+		if (prm.matrices) {
+			const double *src = prm.matrices + (size_t)id * 16;
+			for (int k = 0; k < 16; k++)
+				P[k] = (float)src[k];
+		} else {
+			const double d = prm.lengths[es] *
+					 (prm.clock_rate * prm.model->cat_rates[c]);
+			transition4f(prm.model, d, P);
+		}
+		for (int k = 0; k < 4; k++)
+			for (int j = 0; j < 4; j++)
+				out[k * 4 + j] = P[j * 4 + k];
+	} else {
+		double P[16];
+		if (prm.matrices) {
+			const double *src = prm.matrices + (size_t)id * 16;
+			for (int k = 0; k < 16; k++)
+				P[k] = src[k];
+		} else {
+			const double d = prm.lengths[es] *
+					 (prm.clock_rate * prm.model->cat_rates[c]);
+			transition4(prm.model, d, P);
+		}
+		for (int k = 0; k < 4; k++)
+			for (int j = 0; j < 4; j++)
+				out[k * 4 + j] = (R)P[j * 4 + k];
+	}
 	for (int j = 0; j < 4; j++)
 		out[16 + j] = (R)1.0;
 }
@@ -673,11 +726,12 @@ cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
 	const uint32_t total = p.n * 2u * p.C;
 	if (total == 0)
 		return cudaSuccess;
-	const uint32_t blocks = (total + 127u) / 128u;
+	// one warp per block spreads the (mostly FP64/exp) work over many SMs
+	const uint32_t blocks = (total + 31u) / 32u;
 	if (f32)
-		ptab4_kernel<float><<<blocks, 128, 0, s>>>(p);
+		ptab4_kernel<float><<<blocks, 32, 0, s>>>(p);
 	else
-		ptab4_kernel<double><<<blocks, 128, 0, s>>>(p);
+		ptab4_kernel<double><<<blocks, 32, 0, s>>>(p);
 	return cudaGetLastError();
 }
 
@@ -738,8 +792,8 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 cudaError_t launch_ptab4_batch(const BatchParams &p, uint32_t max_entries,
 			       cudaStream_t s)
 {
-	const dim3 grid((max_entries + 127u) / 128u, p.num_members);
-	ptab4_batch_kernel<<<grid, 128, 0, s>>>(p);
+	const dim3 grid((max_entries + 31u) / 32u, p.num_members);
+	ptab4_batch_kernel<<<grid, 32, 0, s>>>(p);
 	return cudaGetLastError();
 }
 

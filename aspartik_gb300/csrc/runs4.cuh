@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 // ---------------------------------------------------------------------------
 // Batched evaluation: many calculators (chains) in one launch.
 
-__global__ void __launch_bounds__(128) ptab4_batch_kernel(BatchParams bp)
+__global__ void __launch_bounds__(32) ptab4_batch_kernel(BatchParams bp)
 {
 	const uint32_t m = blockIdx.y;
 	const MemberStep st = bp.steps[m];
@@ -305,12 +305,12 @@ __global__ void __launch_bounds__(128) ptab4_batch_kernel(BatchParams bp)
 	const uint32_t c = id % C, es = id / C;
 	const double *lengths = (const double *)(md.stage + md.off_in);
 	const double d = lengths[es] * (st.clock_rate * md.model->cat_rates[c]);
-	double P[16];
-	transition4(md.model, d, P);
+	float P[16];
+	transition4f(md.model, d, P);
 	float *out = md.ptab + (size_t)id * 20;
 	for (int k = 0; k < 4; k++)
 		for (int j = 0; j < 4; j++)
-			out[k * 4 + j] = (float)P[j * 4 + k];
+			out[k * 4 + j] = P[j * 4 + k];
 	for (int j = 0; j < 4; j++)
 		out[16 + j] = 1.0f;
 }
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 		for (uint32_t m = 0; m < M; ++m) {
 			s_prefix[m] = acc;
 			if (bp.steps[m].n)
-				acc += bp.members[m].ldp / bp.members[m].tile;
+				acc += bp.members[m].ldp / bp.steps[m].tile;
 		}
 		s_prefix[M] = acc;
 	}
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 			a.ldp = md.ldp;
 			a.C = md.C;
 			a.L = md.L;
-			a.tile = md.tile;
+			a.tile = st.tile;
 			a.n = st.n;
 			a.n_runs = st.n_runs;
 			a.tips_smem = st.tips_smem;
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 		}
 		const double tsum =
 			tile_walk<Idx>(a, t, s_dot, s_cnt, s_red, s_ops, s_runs, s_tips);
-		const uint32_t tiles = md.ldp / md.tile;
+		const uint32_t tiles = md.ldp / a.tile;
 		if (tid == 0) {
 			md.tile_sums[t] = tsum;
 			__threadfence();
