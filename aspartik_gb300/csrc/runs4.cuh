@@ -115,7 +115,69 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 		tip_row = a.ldp;
 	}
 	__syncthreads();
-	for (uint32_t r = 0; r < a.n_runs; ++r) {
+	if (a.n_runs == a.n) {
+		// A path (every run one entry, e.g. the ancestors of a node whose
+		// height changed): each entry needs only the previous entry's
+		// result and clean inputs, so one thread per column walks it alone
+		// with no barrier, takes the previous result from registers and
+		// prefetches the clean children two entries ahead into L1.
+		if (g == 0) {
+			float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+			int32_t cnt = 0;
+			uint32_t prev_out = 0xFFFFFFFFu;
+			auto prefetch = [&](uint32_t j) {
+				if (j >= a.n)
+					return;
+				const NodeOp o = s_ops[j];
+				for (const uint32_t id : {o.left, o.right})
+					if (!(id & kTipBit) && id != prev_out) {
+						const float4 *ptr =
+							a.part + ((Idx)id * stride + col_off);
+						asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+					}
+			};
+			prefetch(0);
+			prefetch(1);
+			for (uint32_t i = 0; i < a.n; ++i) {
+				prefetch(i + 2);
+				const NodeOp op = s_ops[i];
+				const float4 *tl = a.ptab + ((size_t)(2 * i) * C + c) * 5;
+				const float4 *tr = tl + 5 * C;
+				float4 ca, cb;
+				int32_t sa = 0, sb = 0;
+				if (op.left & kTipBit) {
+					ca = tl[tips_p[(Idx)(op.left & ~kTipBit) * tip_row]];
+				} else if (op.left == prev_out) {
+					ca = v4_apply(tl, y);
+					sa = cnt;
+				} else {
+					const Idx ix = (Idx)op.left * stride + col_off;
+					sa = a.scales[ix];
+					ca = v4_apply(tl, a.part[ix]);
+				}
+				if (op.right & kTipBit) {
+					cb = tr[tips_p[(Idx)(op.right & ~kTipBit) * tip_row]];
+				} else if (op.right == prev_out) {
+					cb = v4_apply(tr, y);
+					sb = cnt;
+				} else {
+					const Idx ix = (Idx)op.right * stride + col_off;
+					sb = a.scales[ix];
+					cb = v4_apply(tr, a.part[ix]);
+				}
+				y = v4_mul(ca, cb);
+				cnt = sa + sb + rescale_pow2(y);
+				const Idx ox = (Idx)op.out * stride + col_off;
+				a.part[ox] = y;
+				a.scales[ox] = cnt;
+				prev_out = op.out;
+			}
+			s_dot[col] = root_dot4(a.pi, y);
+			s_cnt[col] = cnt;
+		}
+		__syncthreads();
+	}
+	for (uint32_t r = 0; r < a.n_runs && a.n_runs != a.n; ++r) {
 		const uint32_t start = s_runs[r], end = s_runs[r + 1];
 		if (worker) {
 			uint32_t i = start + g;
