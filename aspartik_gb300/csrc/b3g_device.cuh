@@ -82,6 +82,7 @@ struct PruneParams {
 	const uint32_t *runs;
 	uint32_t n_runs;
 	uint32_t tile; // patterns per tile
+	uint32_t ptab_smem; // stage the transition tables in shared memory
 	double scale_threshold;
 	double scale_mult;
 	double log_inv_c;
@@ -124,7 +125,11 @@ struct BatchParams {
 	uint32_t smem_tips_bytes; // shared memory reserved for a tip tile
 	uint32_t max_cols;
 	uint32_t narrow; // every member indexes with 32 bits
+	uint32_t smem_ptab_bytes; // shared memory reserved for staged tables
 };
+
+// Transition tables of one list fit shared memory at most this large.
+constexpr uint32_t kPtabSmemBytes = 32u * 1024u;
 
 // Launchers (kernels4.cu).  Each returns the launch error.
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);

@@ -125,6 +125,7 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		bp_.smem_ops_bytes = (max_ops + 15u) & ~15u;
 		bp_.smem_tips_bytes = std::min<uint32_t>(max_tips, 32u * 1024u);
 		bp_.max_cols = max_cols;
+		bp_.smem_ptab_bytes = kPtabSmemBytes;
 		bp_.narrow = narrow ? 1u : 0u;
 		ctas_ = 2 * members_[0]->num_sms_;
 		evaluated_.assign(M, 0);

@@ -439,6 +439,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 				(size_t)L_ * pp.tile <= 32u * 1024u)
 				       ? 1u
 				       : 0u;
+		pp.ptab_smem = (size_t)n * 2 * C_ * 5 * 16 <= kPtabSmemBytes ? 1u : 0u;
 		const uint32_t tiles = ldp_ / pp.tile;
 		const uint32_t ctas = std::min(tiles, 2 * num_sms_);
 		check_cuda(launch_prune4_runs(pp, ctas, stream_), "pruning kernel");

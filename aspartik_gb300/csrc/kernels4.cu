@@ -777,6 +777,8 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 		      sizeof(NodeOp) * p.n + sizeof(uint32_t) * ((p.n_runs + 4) & ~3u);
 	if (p.tips_smem)
 		smem += (size_t)p.num_leaves * p.tile;
+	if (p.ptab_smem)
+		smem += 16 + (size_t)p.n * 2 * p.C * 5 * sizeof(float4);
 	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
 	auto kern = narrow ? prune4_runs_kernel<uint32_t> : prune4_runs_kernel<size_t>;
 	if (smem > 48 * 1024) {
@@ -802,7 +804,7 @@ cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
 {
 	const size_t smem = sizeof(double) * (p.max_cols + (p.max_cols + 1) / 2 +
 					      2 * 512) +
-			    p.smem_ops_bytes + p.smem_tips_bytes;
+			    p.smem_ops_bytes + p.smem_tips_bytes + 16 + p.smem_ptab_bytes;
 	auto kern = p.narrow ? prune4_batch_kernel<uint32_t>
 			     : prune4_batch_kernel<size_t>;
 	if (smem > 48 * 1024) {

@@ -298,6 +298,9 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	NodeOp *s_ops = (NodeOp *)(s_red + 2 * blockDim.x);
 	uint32_t *s_runs = (uint32_t *)(s_ops + prm.n);
 	uint8_t *s_tips = (uint8_t *)(s_runs + ((prm.n_runs + 4) & ~3u));
+	float4 *s_ptab = (float4 *)(((uintptr_t)s_tips +
+				     (prm.tips_smem ? prm.num_leaves * prm.tile : 0u) + 15) &
+				    ~(uintptr_t)15);
 	__shared__ unsigned s_last;
 
 	for (uint32_t k = tid; k < prm.n; k += blockDim.x)
@@ -322,6 +325,13 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	a.n_runs = prm.n_runs;
 	a.tips_smem = prm.tips_smem;
 	a.log_inv_c = prm.log_inv_c;
+	if (prm.ptab_smem) {
+		// every table row of the list, once per block (one load latency)
+		const uint32_t rows = prm.n * 2 * prm.C * 5;
+		for (uint32_t k = tid; k < rows; k += blockDim.x)
+			s_ptab[k] = a.ptab[k];
+		a.ptab = s_ptab;
+	}
 
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
 	const uint32_t ntiles = prm.ldp / prm.tile;
@@ -397,6 +407,8 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 	double *s_red = smem + bp.max_cols + (bp.max_cols + 1) / 2;
 	NodeOp *s_ops = (NodeOp *)(s_red + 2 * blockDim.x);
 	uint8_t *s_tips = (uint8_t *)s_ops + bp.smem_ops_bytes;
+	float4 *s_ptab = (float4 *)(((uintptr_t)s_tips + bp.smem_tips_bytes + 15) &
+				    ~(uintptr_t)15);
 
 	if (tid == 0) {
 		uint32_t acc = 0;
@@ -458,6 +470,14 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 				s_ops[k] = g_ops[k];
 			for (uint32_t k = tid; k <= st.n_runs; k += blockDim.x)
 				s_runs[k] = g_runs[k];
+			// a small list's tables in shared memory (see the single-
+			// calculator kernel)
+			const uint32_t rows = st.n * 2 * md.C * 5;
+			if (rows * sizeof(float4) <= bp.smem_ptab_bytes) {
+				for (uint32_t k = tid; k < rows; k += blockDim.x)
+					s_ptab[k] = ((const float4 *)md.ptab)[k];
+				a.ptab = s_ptab;
+			}
 			cur = m;
 			__syncthreads();
 		}
