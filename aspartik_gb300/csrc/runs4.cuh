@@ -125,21 +125,25 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 			float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
 			int32_t cnt = 0;
 			uint32_t prev_out = 0xFFFFFFFFu;
-			auto prefetch = [&](uint32_t j) {
-				if (j >= a.n)
-					return;
+			// every input that does not come from this walk, requested
+			// at once: one memory latency for the whole path
+			for (uint32_t j = 0; j < a.n && j < 64; ++j) {
 				const NodeOp o = s_ops[j];
-				for (const uint32_t id : {o.left, o.right})
-					if (!(id & kTipBit) && id != prev_out) {
-						const float4 *ptr =
-							a.part + ((Idx)id * stride + col_off);
-						asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
-					}
-			};
-			prefetch(0);
-			prefetch(1);
+				const uint32_t own = j ? s_ops[j - 1].out : 0xFFFFFFFFu;
+				for (const uint32_t id : {o.left, o.right}) {
+					const void *ptr;
+					if (id & kTipBit) {
+						if (a.tips_smem) // already on chip
+							continue;
+						ptr = tips_p + (Idx)(id & ~kTipBit) * tip_row;
+					} else if (id != own)
+						ptr = a.part + ((Idx)id * stride + col_off);
+					else
+						continue;
+					asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+				}
+			}
 			for (uint32_t i = 0; i < a.n; ++i) {
-				prefetch(i + 2);
 				const NodeOp op = s_ops[i];
 				const float4 *tl = a.ptab + ((size_t)(2 * i) * C + c) * 5;
 				const float4 *tr = tl + 5 * C;
