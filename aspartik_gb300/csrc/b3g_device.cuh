@@ -31,8 +31,9 @@ struct NodeOp {
 	uint32_t pad;
 };
 
-// Substitution model resident on the device.  Written by the host
-// (eigensystem given) or by eigen_kernel (device decomposition).
+// Substitution model resident on the device, written by the host (the
+// eigensystem is given or decomposed on the host); matrices row-major with
+// row stride `states`.
 struct ModelDev {
 	double V[kMaxStates * kMaxStates];
 	double Vinv[kMaxStates * kMaxStates];
@@ -40,12 +41,8 @@ struct ModelDev {
 	double Q[kMaxStates * kMaxStates];
 	double pi[kMaxStates];
 	double cat_rates[kMaxCategories];
-	double rates_in[kMaxStates * (kMaxStates - 1) / 2]; // eigen_kernel input
-	double pi_in[kMaxStates];                           // eigen_kernel input
 	uint32_t shortcuts;
 	uint32_t states;
-	uint32_t jacobi_sweeps; // written by eigen_kernel
-	uint32_t status;        // 0 ok, 1 Jacobi did not converge
 };
 
 struct PtabParams {
@@ -131,6 +128,30 @@ struct BatchParams {
 // Transition tables of one list fit shared memory at most this large.
 constexpr uint32_t kPtabSmemBytes = 32u * 1024u;
 
+// Fused single-launch evaluation of a short list (FP32 chosen form, four
+// states, four categories): the schedule, the edge lengths and the root
+// frequencies travel in the kernel parameters, so the launch needs no
+// upload, no transition kernel and no read-back copy.
+constexpr uint32_t kDirectMax = 48; // entries
+struct DirectParams {
+	const uint8_t *tips;
+	void *partials;
+	int32_t *scales;
+	const uint32_t *weights;
+	const ModelDev *model;
+	double *site_lnl;   // [ldp]
+	double *block_sums; // [gridDim.x]
+	unsigned *ticket;   // zero between launches
+	double *lnl_out;    // device copy of the result
+	double *lnl_host;   // host-mapped pinned word, written by the last block
+	uint32_t n, ldp, L, pad0;
+	double clock_rate;
+	double log_inv_c;
+	double pi[4];
+	NodeOp ops[kDirectMax];
+	double lengths[2 * kDirectMax]; // [n][2] time lengths
+};
+
 // Launchers (kernels4.cu).  Each returns the launch error.
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);
 cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
@@ -139,7 +160,10 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 // pattern tiles.  Needs p.runs; block sums sized for `ctas`.
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			       cudaStream_t s);
-cudaError_t launch_eigen(ModelDev *model, uint32_t states, cudaStream_t s);
+// Fused short-list evaluation: `ctas` persistent blocks over ldp / 128
+// pattern tiles; needs p.n <= kDirectMax and block sums sized for `ctas`.
+cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,
+				 cudaStream_t s);
 // Batched evaluation (FP32): transition tables of every member with work,
 // then one persistent pruning launch over all members' pattern tiles.
 // max_entries = largest member n * 2 * C.

@@ -113,6 +113,11 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 			runs_tile_ = t;
 	}
 	use_runs_ = f32_ && runs_tile_ * C_ <= 512;
+	// fused single-launch evaluation of short lists (B3G_DIRECT=0 turns
+	// it off, e.g. to time the two-kernel path)
+	use_direct_ = f32_ && S_ == 4 && C_ == 4;
+	if (const char *env = std::getenv("B3G_DIRECT"))
+		use_direct_ = use_direct_ && std::atoi(env) != 0;
 
 	selectors_.assign(I_, 0);
 	stamp_.assign(2 * L_ - 1, 0);
@@ -167,9 +172,12 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		check_cuda(cudaHostAlloc((void **)&h_model_, sizeof(ModelDev),
 					 cudaHostAllocDefault),
 			   "pinned model");
+		// mapped: the fused short-list kernel writes the result here
 		check_cuda(cudaHostAlloc((void **)&h_lnl_, sizeof(double),
-					 cudaHostAllocDefault),
+					 cudaHostAllocMapped),
 			   "pinned lnl");
+		check_cuda(cudaHostGetDevicePointer((void **)&d_lnl_host_, h_lnl_, 0),
+			   "mapped lnl");
 
 		// tips: single bases -> 0..3, everything else -> unknown (4)
 		// (cpu4.rs:117-124); padded patterns are unknown too
@@ -374,6 +382,11 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 			bool want_cat)
 {
+	if (use_direct_ && !matrices_mode && !want_cat && n > 0 &&
+	    n <= kDirectMax) {
+		launch_direct(n, clock_rate);
+		return;
+	}
 	const size_t in_bytes =
 		matrices_mode ? (size_t)n * 2 * C_ * S_ * S_ * sizeof(double)
 			      : (size_t)n * 2 * sizeof(double);
@@ -385,6 +398,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	TimingSlot &slot = ring_[ring_next_ % kRing];
 	if (slot.pending)
 		harvest(slot); // recorded kRing proposals ago: long complete
+	slot.direct = false;
 	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
 
 	PtabParams pt{};
@@ -455,6 +469,50 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	have_result_ = true;
 	stream_dirty_ = true;
 	cat_valid_ = want_cat;
+}
+
+// One launch for a short FP32 list: the staged schedule, the lengths and
+// the root frequencies go into the kernel parameters (nothing is uploaded),
+// the kernel builds its transition tables in shared memory and writes the
+// result into the mapped pinned word that log_likelihood() reads.
+void Calculator::launch_direct(uint32_t n, double clock_rate)
+{
+	DirectParams dp;
+	dp.tips = d_tips_;
+	dp.partials = d_partials_;
+	dp.scales = d_scales_;
+	dp.weights = d_weights_;
+	dp.model = d_model_;
+	dp.site_lnl = d_site_;
+	dp.block_sums = d_block_sums_;
+	dp.ticket = d_ticket_;
+	dp.lnl_out = d_lnl_;
+	dp.lnl_host = d_lnl_host_;
+	dp.n = n;
+	dp.ldp = ldp_;
+	dp.L = L_;
+	dp.pad0 = 0;
+	dp.clock_rate = clock_rate;
+	dp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
+	std::memcpy(dp.pi, h_stage_ + off_pi_, 4 * sizeof(double));
+	std::memcpy(dp.ops, h_stage_, (size_t)n * sizeof(NodeOp));
+	std::memcpy(dp.lengths, h_stage_ + off_in_, (size_t)n * 2 * sizeof(double));
+	// bytes that reach the device with the launch
+	last_upload_bytes_ = (uint64_t)n * (sizeof(NodeOp) + 2 * sizeof(double)) +
+			     4 * sizeof(double);
+	TimingSlot &slot = ring_[ring_next_ % kRing];
+	if (slot.pending)
+		harvest(slot);
+	slot.direct = true;
+	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
+	const uint32_t ctas = std::min(ldp_ / 128u, 2 * num_sms_);
+	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
+	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
+	slot.pending = true;
+	++ring_next_;
+	have_result_ = true;
+	stream_dirty_ = true;
+	cat_valid_ = false;
 }
 
 void Calculator::propose_matrices(const uint32_t *internals,
@@ -587,8 +645,12 @@ void Calculator::harvest(TimingSlot &s)
 {
 	check_cuda(cudaEventSynchronize(s.k1), "timing sync");
 	float t = 0.0f, p = 0.0f;
-	check_cuda(cudaEventElapsedTime(&t, s.k0, s.kmid), "elapsed");
-	check_cuda(cudaEventElapsedTime(&p, s.kmid, s.k1), "elapsed");
+	if (s.direct) { // one fused kernel: all of it counts as pruning
+		check_cuda(cudaEventElapsedTime(&p, s.k0, s.k1), "elapsed");
+	} else {
+		check_cuda(cudaEventElapsedTime(&t, s.k0, s.kmid), "elapsed");
+		check_cuda(cudaEventElapsedTime(&p, s.kmid, s.k1), "elapsed");
+	}
 	acc_transition_ms_ += t;
 	acc_prune_ms_ += p;
 	++acc_count_;
@@ -602,6 +664,11 @@ void Calculator::last_timing(float *transition_ms, float *prune_ms)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
 	TimingSlot &s = ring_[(ring_next_ - 1) % kRing];
 	check_cuda(cudaEventSynchronize(s.k1), "sync");
+	if (s.direct) {
+		*transition_ms = 0.0f;
+		check_cuda(cudaEventElapsedTime(prune_ms, s.k0, s.k1), "elapsed");
+		return;
+	}
 	check_cuda(cudaEventElapsedTime(transition_ms, s.k0, s.kmid), "elapsed");
 	check_cuda(cudaEventElapsedTime(prune_ms, s.kmid, s.k1), "elapsed");
 }
@@ -713,14 +780,18 @@ void Calculator::set_reversible(const double *rates, const double *pi,
 		psum += pi[k];
 	}
 	(void)psum;
-	std::memcpy(model_host_.rates_in, rates, nr * sizeof(double));
-	std::memcpy(model_host_.pi_in, pi, S_ * sizeof(double));
+	// decomposed on the host in FP64: a one-block Jacobi kernel measured
+	// about 410 us per model on this GPU (its FP64 pipe issues at 1/64 of
+	// the FP32 rate), the host takes a few microseconds
+	const int sweeps = reversible_eigen((int)S_, rates, pi, model_host_.V,
+					    model_host_.Vinv, model_host_.lambda,
+					    model_host_.Q);
+	if (sweeps < 0)
+		throw Error(B3G_ERR_NUMERIC,
+			    "eigen decomposition of Q did not converge");
 	std::memcpy(model_host_.pi, pi, S_ * sizeof(double));
 	model_host_.shortcuts = shortcuts ? 1u : 0u;
 	upload_model();
-	check_cuda(launch_eigen(d_model_, S_, stream_), "eigen kernel");
-	// the host copy of the decomposition is not needed: the device keeps
-	// V, V^-1, lambda and Q; pi is mirrored for the root reduction
 	model_set_ = true;
 }
 
@@ -732,8 +803,7 @@ void Calculator::set_category_rates(const double *rates)
 	for (uint32_t c = 0; c < C_; ++c)
 		if (!std::isfinite(rates[c]) || rates[c] < 0.0)
 			throw Error(B3G_ERR_NUMERIC, "bad category rate");
-	// the device model may hold a decomposition written by eigen_kernel;
-	// update only the category rates in place
+	// update only the category rates of the device model in place
 	std::memcpy(model_host_.cat_rates, rates, C_ * sizeof(double));
 	check_cuda(cudaEventSynchronize(ev_model_free_), "model staging");
 	std::memcpy(h_model_->cat_rates, rates, C_ * sizeof(double));

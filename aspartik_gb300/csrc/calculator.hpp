@@ -83,6 +83,7 @@ class Calculator {
 		       uint32_t n);
 	void launch(uint32_t n, bool matrices_mode, double clock_rate,
 		    bool want_cat);
+	void launch_direct(uint32_t n, double clock_rate);
 	void upload_model();
 	void release();
 
@@ -114,6 +115,7 @@ class Calculator {
 	struct TimingSlot {
 		cudaEvent_t k0 = nullptr, kmid = nullptr, k1 = nullptr;
 		bool pending = false;
+		bool direct = false; // fused launch: k0 .. k1, no kmid
 	};
 	TimingSlot ring_[kRing];
 	uint64_t ring_next_ = 0;
@@ -139,6 +141,7 @@ class Calculator {
 	unsigned char *h_stage_ = nullptr;
 	ModelDev *h_model_ = nullptr;
 	double *h_lnl_ = nullptr;
+	double *d_lnl_host_ = nullptr; // device view of h_lnl_
 	size_t stage_bytes_ = 0;
 	size_t off_pi_ = 0, off_runs_ = 0, off_in_ = 0;
 	uint32_t n_runs_ = 0;
@@ -166,6 +169,7 @@ class Calculator {
 	uint32_t num_sms_ = 1;
 	uint32_t runs_tile_ = 64;
 	bool use_runs_ = false;
+	bool use_direct_ = false;
 };
 
 } // namespace b3g

@@ -160,4 +160,94 @@ void gamma_categories(double alpha, int k, double *rates)
 		rates[i] = rates[i] / mean;
 }
 
+
+// Reversible Q from exchangeabilities and frequencies, normalised to mean
+// rate 1 (GTR::update_matrices, crates/b3/src/substitution.rs:502-555), and
+// its eigensystem through the symmetric matrix B = Pi^1/2 Q Pi^-1/2: cyclic
+// Jacobi rotations (Golub & Van Loan, Matrix Computations, 4th ed., sec.
+// 8.5) until the off-diagonal norm is below 1e-17 of the total.  Then
+// Q = V diag(lambda) V^-1 with V = Pi^-1/2 U and V^-1 = U^T Pi^1/2.
+int reversible_eigen(int n, const double *rates, const double *pi, double *V,
+		     double *Vinv, double *lambda, double *Q)
+{
+	double sq[kHostMaxStates];
+	double B[kHostMaxStates * kHostMaxStates];
+	double U[kHostMaxStates * kHostMaxStates];
+	int k = 0;
+	for (int a = 0; a < n; a++) {
+		Q[a * n + a] = 0.0;
+		for (int b = a + 1; b < n; b++, k++) {
+			Q[a * n + b] = rates[k] * pi[b];
+			Q[b * n + a] = rates[k] * pi[a];
+		}
+	}
+	double scale = 0.0;
+	for (int a = 0; a < n; a++) {
+		double rsum = 0.0;
+		for (int b = 0; b < n; b++)
+			if (b != a)
+				rsum += Q[a * n + b];
+		Q[a * n + a] = -rsum;
+		scale += rsum * pi[a];
+	}
+	for (int a = 0; a < n; a++) {
+		sq[a] = std::sqrt(pi[a]);
+		for (int b = 0; b < n; b++)
+			Q[a * n + b] /= scale;
+	}
+	for (int a = 0; a < n; a++)
+		for (int b = 0; b < n; b++) {
+			B[a * n + b] = 0.5 * (Q[a * n + b] * sq[a] / sq[b] +
+					      Q[b * n + a] * sq[b] / sq[a]);
+			U[a * n + b] = a == b ? 1.0 : 0.0;
+		}
+	int sweep = 0;
+	for (; sweep < 50; ++sweep) {
+		double off = 0.0, tot = 0.0;
+		for (int a = 0; a < n; a++)
+			for (int b = 0; b < n; b++) {
+				const double b2 = B[a * n + b] * B[a * n + b];
+				tot += b2;
+				if (a != b)
+					off += b2;
+			}
+		if (off <= 1e-34 * tot)
+			break;
+		for (int p = 0; p < n - 1; p++)
+			for (int q = p + 1; q < n; q++) {
+				const double apq = B[p * n + q];
+				if (apq == 0.0)
+					continue;
+				const double theta = (B[q * n + q] - B[p * n + p]) / (2.0 * apq);
+				const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+						 (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+				const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+				for (int r = 0; r < n; r++) { // B J
+					const double bp = B[r * n + p], bq = B[r * n + q];
+					B[r * n + p] = c * bp - s * bq;
+					B[r * n + q] = s * bp + c * bq;
+				}
+				for (int r = 0; r < n; r++) { // J^T (B J)
+					const double bp = B[p * n + r], bq = B[q * n + r];
+					B[p * n + r] = c * bp - s * bq;
+					B[q * n + r] = s * bp + c * bq;
+				}
+				B[p * n + q] = B[q * n + p] = 0.0;
+				for (int r = 0; r < n; r++) { // U J
+					const double up = U[r * n + p], uq = U[r * n + q];
+					U[r * n + p] = c * up - s * uq;
+					U[r * n + q] = s * up + c * uq;
+				}
+			}
+	}
+	for (int i = 0; i < n; i++) {
+		lambda[i] = B[i * n + i];
+		for (int j = 0; j < n; j++) {
+			V[i * n + j] = U[i * n + j] / sq[i];
+			Vinv[j * n + i] = U[i * n + j] * sq[i];
+		}
+	}
+	return sweep < 50 ? sweep : -1;
+}
+
 } // namespace b3g

@@ -14,4 +14,11 @@ void gamma_categories(double alpha, int k, double *rates);
 void hky_eigen(double kappa, const double *pi, double *V, double *Vinv,
 	       double *lambda, double *Q);
 
+constexpr int kHostMaxStates = 20;
+// Reversible model of n <= kHostMaxStates states from upper-triangle
+// exchangeabilities and frequencies: normalised Q and its eigensystem, all
+// row-major.  Returns the Jacobi sweeps taken, or -1 without convergence.
+int reversible_eigen(int n, const double *rates, const double *pi, double *V,
+		     double *Vinv, double *lambda, double *Q);
+
 } // namespace b3g

@@ -12,7 +12,8 @@
 //                  patterns and the last block to finish folds the block
 //                  sums with Neumaier compensation (no atomics on doubles,
 //                  deterministic order).
-//   eigen_kernel   FP64 symmetric Jacobi decomposition of a reversible Q.
+//   prune4_runs_kernel / prune4_direct_kernel / prune4_batch_kernel
+//                  FP32 walks of pattern tiles (runs4.cuh).
 //
 // The arithmetic restates the reference's CPU pruner
 // (crates/b3/src/calculator/cpu4.rs:170-433): tip-tip nodes are products of
@@ -173,8 +174,10 @@ __device__ void transition4(const ModelDev *__restrict__ m, double d,
 // FP32 chosen form: P(t) in single precision from the FP64 eigensystem
 // (the decomposition of Q is the only FP64 work of this step; on GB300 FP64
 // issues at 1/64 of the FP32 rate).  The shortcut tests stay in FP64.
-__device__ void transition4f(const ModelDev *__restrict__ m, double d,
-			     float P[16])
+// eig: V (16), Vinv (16) and lambda (4) of a four-state model, in FP32.
+__device__ void transition4f_eig(const ModelDev *__restrict__ m,
+				 const float *__restrict__ eig, double d,
+				 float P[16])
 {
 	if (m->shortcuts && d > 20.0) {
 		for (int i = 0; i < 4; i++)
@@ -191,20 +194,33 @@ __device__ void transition4f(const ModelDev *__restrict__ m, double d,
 	const float df = (float)d;
 	float e[4];
 	for (int k = 0; k < 4; k++)
-		e[k] = expf((float)m->lambda[k] * df);
+		e[k] = expf(eig[32 + k] * df);
 	for (int i = 0; i < 4; i++) {
-		const float t0 = (float)m->V[i * 4 + 0] * e[0];
-		const float t1 = (float)m->V[i * 4 + 1] * e[1];
-		const float t2 = (float)m->V[i * 4 + 2] * e[2];
-		const float t3 = (float)m->V[i * 4 + 3] * e[3];
+		const float t0 = eig[i * 4 + 0] * e[0];
+		const float t1 = eig[i * 4 + 1] * e[1];
+		const float t2 = eig[i * 4 + 2] * e[2];
+		const float t3 = eig[i * 4 + 3] * e[3];
 		for (int j = 0; j < 4; j++) {
-			float s = t0 * (float)m->Vinv[0 * 4 + j];
-			s = fmaf(t1, (float)m->Vinv[1 * 4 + j], s);
-			s = fmaf(t2, (float)m->Vinv[2 * 4 + j], s);
-			s = fmaf(t3, (float)m->Vinv[3 * 4 + j], s);
+			float s = t0 * eig[16 + 0 * 4 + j];
+			s = fmaf(t1, eig[16 + 1 * 4 + j], s);
+			s = fmaf(t2, eig[16 + 2 * 4 + j], s);
+			s = fmaf(t3, eig[16 + 3 * 4 + j], s);
 			P[i * 4 + j] = s;
 		}
 	}
+}
+
+__device__ void transition4f(const ModelDev *__restrict__ m, double d,
+			     float P[16])
+{
+	float eig[36];
+	for (int k = 0; k < 16; k++) {
+		eig[k] = (float)m->V[k];
+		eig[16 + k] = (float)m->Vinv[k];
+	}
+	for (int k = 0; k < 4; k++)
+		eig[32 + k] = (float)m->lambda[k];
+	transition4f_eig(m, eig, d, P);
 }
 
 template <typename R>
@@ -577,148 +593,6 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 // element of B and of the accumulated rotations U.  Then Q = V L V^-1 with
 // V = D^-1/2 U and V^-1 = U^T D^1/2.  One block of m x m threads, m = n
 // rounded up to even (the extra index is a dummy that never rotates).
-
-constexpr int kEigMax = kMaxStates; // even
-
-__global__ void __launch_bounds__(kEigMax *kEigMax) eigen_kernel(ModelDev *mdl)
-{
-	__shared__ double B[kEigMax][kEigMax + 1];
-	__shared__ double U[kEigMax][kEigMax + 1];
-	__shared__ double Qs[kEigMax][kEigMax];
-	__shared__ double cs[kEigMax], sn[kEigMax], sq[kEigMax];
-	__shared__ int partner[kEigMax], order[kEigMax];
-	__shared__ double s_off, s_tot;
-
-	const int n = (int)mdl->states;
-	const int m = (n + 1) & ~1;
-	const int i = threadIdx.y, j = threadIdx.x; // element (i, j)
-	const bool live = i < n && j < n;
-	const int tid = i * blockDim.x + j;
-
-	// Q_ij = r_ij pi_j, rows summing to zero, normalised to mean rate 1
-	if (tid == 0) {
-		int k = 0;
-		for (int a = 0; a < n; a++) {
-			Qs[a][a] = 0.0;
-			for (int b = a + 1; b < n; b++, k++) {
-				Qs[a][b] = mdl->rates_in[k] * mdl->pi_in[b];
-				Qs[b][a] = mdl->rates_in[k] * mdl->pi_in[a];
-			}
-		}
-		double scale = 0.0;
-		for (int a = 0; a < n; a++) {
-			double rsum = 0.0;
-			for (int b = 0; b < n; b++)
-				if (b != a)
-					rsum += Qs[a][b];
-			Qs[a][a] = -rsum;
-			scale += rsum * mdl->pi_in[a];
-		}
-		for (int a = 0; a < n; a++) {
-			sq[a] = sqrt(mdl->pi_in[a]);
-			for (int b = 0; b < n; b++)
-				Qs[a][b] /= scale;
-		}
-		for (int a = 0; a < m; a++)
-			order[a] = a;
-	}
-	__syncthreads();
-	if (i < m && j < m) {
-		double b = 0.0;
-		if (live)
-			b = 0.5 * (Qs[i][j] * sq[i] / sq[j] + Qs[j][i] * sq[j] / sq[i]);
-		B[i][j] = b;
-		U[i][j] = i == j ? 1.0 : 0.0;
-	}
-	__syncthreads();
-
-	int sweep = 0;
-	for (; sweep < 40; ++sweep) {
-		// off-diagonal and total squared norms, summed in a fixed order
-		if (tid == 0) {
-			double off = 0.0, tot = 0.0;
-			for (int a = 0; a < n; a++)
-				for (int b = 0; b < n; b++) {
-					const double b2 = B[a][b] * B[a][b];
-					tot += b2;
-					if (a != b)
-						off += b2;
-				}
-			s_off = off;
-			s_tot = tot;
-		}
-		__syncthreads();
-		if (s_off <= 1e-34 * s_tot)
-			break;
-		for (int round = 0; round < m - 1; ++round) {
-			// rotation of every pair of this round, by thread (k, 0)
-			if (j == 0 && i < m / 2) {
-				int p = order[i], q = order[m - 1 - i];
-				if (p > q) {
-					const int t = p;
-					p = q;
-					q = t;
-				}
-				double c = 1.0, s = 0.0;
-				const double apq = B[p][q];
-				if (q < n && apq != 0.0) {
-					const double theta = (B[q][q] - B[p][p]) / (2.0 * apq);
-					const double t = (theta >= 0.0 ? 1.0 : -1.0) /
-							 (fabs(theta) + sqrt(theta * theta + 1.0));
-					c = 1.0 / sqrt(t * t + 1.0);
-					s = t * c;
-				}
-				// new row/column k = c * k + coef * partner
-				partner[p] = q;
-				partner[q] = p;
-				cs[p] = c;
-				cs[q] = c;
-				sn[p] = -s;
-				sn[q] = s;
-			}
-			__syncthreads();
-			double rb = 0.0;
-			if (i < m && j < m)
-				rb = cs[i] * B[i][j] + sn[i] * B[partner[i]][j];
-			__syncthreads();
-			if (i < m && j < m)
-				B[i][j] = rb;
-			__syncthreads();
-			double cb = 0.0, cu = 0.0;
-			if (i < m && j < m) {
-				cb = cs[j] * B[i][j] + sn[j] * B[i][partner[j]];
-				cu = cs[j] * U[i][j] + sn[j] * U[i][partner[j]];
-			}
-			__syncthreads();
-			if (i < m && j < m) {
-				B[i][j] = cb;
-				U[i][j] = cu;
-			}
-			// next round: keep order[0], rotate order[1..m-1]
-			if (tid == 0) {
-				const int last = order[m - 1];
-				for (int a = m - 1; a > 1; --a)
-					order[a] = order[a - 1];
-				order[1] = last;
-			}
-			__syncthreads();
-		}
-	}
-	if (live) {
-		if (i == j)
-			mdl->lambda[i] = B[i][i];
-		mdl->V[i * n + j] = U[i][j] / sq[i];
-		mdl->Vinv[j * n + i] = U[i][j] * sq[i];
-		mdl->Q[i * n + j] = Qs[i][j];
-	}
-	if (tid == 0) {
-		for (int a = 0; a < n; a++)
-			mdl->pi[a] = mdl->pi_in[a];
-		mdl->jacobi_sweeps = (uint32_t)sweep;
-		mdl->status = sweep < 40 ? 0u : 1u;
-	}
-}
-
 } // namespace
 
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
@@ -817,11 +691,18 @@ cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
 	return cudaGetLastError();
 }
 
-cudaError_t launch_eigen(ModelDev *model, uint32_t states, cudaStream_t s)
+cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,
+				 cudaStream_t s)
 {
-	const uint32_t m = (states + 1) & ~1u;
-	eigen_kernel<<<1, dim3(m, m), 0, s>>>(model);
+	if (p.n == 0 || p.n > kDirectMax || p.ldp % 128u)
+		return cudaErrorInvalidValue;
+	const bool narrow = (uint64_t)p.L * 2 * 4 * p.ldp < (1ull << 31);
+	if (narrow)
+		prune4_direct_kernel<uint32_t><<<ctas, 512, 0, s>>>(p);
+	else
+		prune4_direct_kernel<size_t><<<ctas, 512, 0, s>>>(p);
 	return cudaGetLastError();
 }
+
 
 } // namespace b3g

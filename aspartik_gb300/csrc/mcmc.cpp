@@ -122,7 +122,9 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		chains_.push_back(std::move(ch));
 	}
 	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
-	if (cfg.precision == B3G_PRECISION_F32) {
+	// several FP32 chains share one batched launch per step; a single
+	// chain launches its own (short lists take the fused one-kernel path)
+	if (cfg.precision == B3G_PRECISION_F32 && chains_.size() > 1) {
 		std::vector<Calculator *> calcs;
 		for (auto &ch : chains_)
 			calcs.push_back(ch->calc.get());

@@ -70,17 +70,19 @@ __device__ __forceinline__ void run_item(const NodeOp *__restrict__ ops,
 	scales[ox] = cnt;
 }
 
-__device__ __forceinline__ double root_dot4(const double *pi, const float4 &y)
+// Root: frequency-weighted sum of the partial vector, in FP32 (the FP64
+// pipe runs at 1/64 of the FP32 rate on this part, and the root mixing of
+// every pattern sits on the critical path of a short dirty list).
+__device__ __forceinline__ float root_dot4(const float *pi, const float4 &y)
 {
-	return (double)pi[0] * y.x + (double)pi[1] * y.y + (double)pi[2] * y.z +
-	       (double)pi[3] * y.w;
+	return fmaf(pi[3], y.w, fmaf(pi[2], y.z, fmaf(pi[1], y.y, pi[0] * y.x)));
 }
 
 // One pattern tile t: every run of the schedule, then the category mixing
 // of the root.  Returns the tile's weighted site sum in thread 0.  Ends with
 // the block synchronised.  s_dot/s_cnt hold tile * C entries, s_red 32.
 template <typename Idx>
-__device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
+__device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			    int32_t *s_cnt, double *s_red,
 			    const NodeOp *s_ops, const uint32_t *s_runs,
 			    uint8_t *s_tips)
@@ -96,6 +98,10 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 	const uint32_t p = t * tile + pl;
 	const Idx col_off = (Idx)c * a.ldp + p;
 
+	__shared__ float s_pi[4];
+	if (tid < 4)
+		s_pi[tid] = (float)a.pi[tid];
+	const bool serial = groups == 1;
 	const uint8_t *tips_p;
 	uint32_t tip_row;
 	if (a.tips_smem) {
@@ -115,73 +121,59 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 		tip_row = a.ldp;
 	}
 	__syncthreads();
-	if (a.n_runs == a.n) {
-		// A path (every run one entry, e.g. the ancestors of a node whose
-		// height changed): each entry needs only the previous entry's
-		// result and clean inputs, so one thread per column walks it alone
-		// with no barrier, takes the previous result from registers and
-		// prefetches the clean children two entries ahead into L1.
-		if (g == 0) {
-			float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-			int32_t cnt = 0;
-			uint32_t prev_out = 0xFFFFFFFFu;
-			// every input that does not come from this walk, requested
-			// at once: one memory latency for the whole path
-			for (uint32_t j = 0; j < a.n && j < 64; ++j) {
-				const NodeOp o = s_ops[j];
-				const uint32_t own = j ? s_ops[j - 1].out : 0xFFFFFFFFu;
-				for (const uint32_t id : {o.left, o.right}) {
-					const void *ptr;
-					if (id & kTipBit) {
-						if (a.tips_smem) // already on chip
-							continue;
-						ptr = tips_p + (Idx)(id & ~kTipBit) * tip_row;
-					} else if (id != own)
-						ptr = a.part + ((Idx)id * stride + col_off);
-					else
-						continue;
-					asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
-				}
+	if (serial) {
+		// One thread per column (tile * C == blockDim.x) walks the whole
+		// list in order, with no barrier: a child that is the output of
+		// one of the two previous entries comes from registers, any other
+		// listed child from memory (written earlier by this thread).  The
+		// walk is issue-bound (about 700 cycles an entry at 16 warps per
+		// SM), so clean inputs are loaded plainly: staging them ahead in
+		// shared memory was measured to gain nothing.
+		float4 y0 = make_float4(0.f, 0.f, 0.f, 0.f), y1 = y0;
+		int32_t c0 = 0, c1 = 0;
+		uint32_t o0 = 0xFFFFFFFFu, o1 = 0xFFFFFFFFu;
+		auto input = [&](uint32_t id, const float4 *tb, float4 &v,
+				 int32_t &sc) {
+			if (id & kTipBit) {
+				v = tb[tips_p[(Idx)(id & ~kTipBit) * tip_row]];
+				sc = 0;
+			} else if (id == o0) {
+				v = v4_apply(tb, y0);
+				sc = c0;
+			} else if (id == o1) {
+				v = v4_apply(tb, y1);
+				sc = c1;
+			} else {
+				const Idx ix = (Idx)id * stride + col_off;
+				sc = a.scales[ix];
+				v = v4_apply(tb, a.part[ix]);
 			}
-			for (uint32_t i = 0; i < a.n; ++i) {
-				const NodeOp op = s_ops[i];
-				const float4 *tl = a.ptab + ((size_t)(2 * i) * C + c) * 5;
-				const float4 *tr = tl + 5 * C;
-				float4 ca, cb;
-				int32_t sa = 0, sb = 0;
-				if (op.left & kTipBit) {
-					ca = tl[tips_p[(Idx)(op.left & ~kTipBit) * tip_row]];
-				} else if (op.left == prev_out) {
-					ca = v4_apply(tl, y);
-					sa = cnt;
-				} else {
-					const Idx ix = (Idx)op.left * stride + col_off;
-					sa = a.scales[ix];
-					ca = v4_apply(tl, a.part[ix]);
-				}
-				if (op.right & kTipBit) {
-					cb = tr[tips_p[(Idx)(op.right & ~kTipBit) * tip_row]];
-				} else if (op.right == prev_out) {
-					cb = v4_apply(tr, y);
-					sb = cnt;
-				} else {
-					const Idx ix = (Idx)op.right * stride + col_off;
-					sb = a.scales[ix];
-					cb = v4_apply(tr, a.part[ix]);
-				}
-				y = v4_mul(ca, cb);
-				cnt = sa + sb + rescale_pow2(y);
-				const Idx ox = (Idx)op.out * stride + col_off;
-				a.part[ox] = y;
-				a.scales[ox] = cnt;
-				prev_out = op.out;
-			}
-			s_dot[col] = root_dot4(a.pi, y);
-			s_cnt[col] = cnt;
+		};
+		for (uint32_t i = 0; i < a.n; ++i) {
+			const NodeOp op = s_ops[i];
+			const float4 *tl = a.ptab + ((size_t)(2 * i) * C + c) * 5;
+			const float4 *tr = tl + 5 * C;
+			float4 ca, cb;
+			int32_t sa, sb;
+			input(op.left, tl, ca, sa);
+			input(op.right, tr, cb, sb);
+			float4 y = v4_mul(ca, cb);
+			const int32_t cnt = sa + sb + rescale_pow2(y);
+			const Idx ox = (Idx)op.out * stride + col_off;
+			a.part[ox] = y;
+			a.scales[ox] = cnt;
+			y1 = y0;
+			c1 = c0;
+			o1 = o0;
+			y0 = y;
+			c0 = cnt;
+			o0 = op.out;
 		}
+		s_dot[col] = root_dot4(s_pi, y0);
+		s_cnt[col] = c0;
 		__syncthreads();
 	}
-	for (uint32_t r = 0; r < a.n_runs && a.n_runs != a.n; ++r) {
+	for (uint32_t r = 0; r < a.n_runs && !serial; ++r) {
 		const uint32_t start = s_runs[r], end = s_runs[r + 1];
 		if (worker) {
 			uint32_t i = start + g;
@@ -196,7 +188,7 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 					      a.scales, C, stride, col_off, c,
 					      i + groups, y1, c1);
 				if (i + groups == a.n - 1) {
-					s_dot[col] = root_dot4(a.pi, y1);
+					s_dot[col] = root_dot4(s_pi, y1);
 					s_cnt[col] = c1;
 				}
 			}
@@ -206,7 +198,7 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 				run_item<Idx>(s_ops, tips_p, tip_row, a.ptab, a.part,
 					      a.scales, C, stride, col_off, c, i, y0, c0);
 				if (i == a.n - 1) {
-					s_dot[col] = root_dot4(a.pi, y0);
+					s_dot[col] = root_dot4(s_pi, y0);
 					s_cnt[col] = c0;
 				}
 			}
@@ -219,24 +211,27 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 		const uint32_t pp = t * tile + tid;
 		int32_t emax = INT32_MIN;
 		for (uint32_t k = 0; k < C; k++)
-			if (s_dot[k * tile + tid] > 0.0)
+			if (s_dot[k * tile + tid] > 0.f)
 				emax = max(emax, s_cnt[k * tile + tid]);
 		double site;
 		if (emax == INT32_MIN) {
 			site = -INFINITY;
 		} else {
-			double acc = 0.0;
+			// categories mixed in FP32 at the largest exponent; only
+			// the exact exponent term and the constant join in FP64
+			float acc = 0.f;
 			for (uint32_t k = 0; k < C; k++)
-				acc += scalbn(s_dot[k * tile + tid],
+				acc += ldexpf(s_dot[k * tile + tid],
 					      s_cnt[k * tile + tid] - emax);
-			site = log(acc) + (double)emax * 0.69314718055994530942 +
-			       a.log_inv_c;
+			site = (double)logf(acc) +
+			       fma((double)emax, 0.69314718055994530942,
+				   a.log_inv_c);
 		}
 		a.site_lnl[pp] = site;
 		if (a.cat_lnl)
 			for (uint32_t k = 0; k < C; k++)
 				a.cat_lnl[(size_t)k * a.ldp + pp] =
-					log(s_dot[k * tile + tid]) +
+					log((double)s_dot[k * tile + tid]) +
 					(double)s_cnt[k * tile + tid] *
 						0.69314718055994530942;
 		const uint32_t wgt = a.weights[pp];
@@ -256,35 +251,29 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, double *s_dot,
 	return tsum;
 }
 
-// Fold `count` compensated-free partial sums at `sums` with Neumaier
-// compensation in a fixed-shape tree (threads of the block); the result is
-// returned in thread 0.  Uses 2 * blockDim.x doubles at s_red.
+// Sum `count` doubles at `sums` in a fixed order: strided per thread,
+// then a warp-shuffle tree and the warps' sums in a second tree.  The
+// result is returned in thread 0; s_red holds blockDim.x / 32 doubles.
+// Pairwise FP64 over a few hundred block sums loses nothing at the FP32
+// form's accuracy, and keeps the serial tail of the launch to ~14
+// dependent FP64 adds (the pipe runs at 1/64 of the FP32 rate here).
 __device__ double block_fold(const double *sums, uint32_t count, double *s_red)
 {
-	const uint32_t tid = threadIdx.x, nthr = blockDim.x;
-	double sum = 0.0, comp = 0.0;
-	for (uint32_t k = tid; k < count; k += nthr)
-		neumaier_add(sum, comp, __ldcg(sums + k));
-	double *s_sum = s_red;
-	double *s_comp = s_red + nthr;
-	s_sum[tid] = sum;
-	s_comp[tid] = comp;
+	const uint32_t tid = threadIdx.x, nwarps = blockDim.x >> 5;
+	double sum = 0.0;
+	for (uint32_t k = tid; k < count; k += blockDim.x)
+		sum += __ldcg(sums + k);
+	for (int off = 16; off > 0; off >>= 1)
+		sum += __shfl_down_sync(0xffffffffu, sum, off);
+	if ((tid & 31u) == 0)
+		s_red[tid >> 5] = sum;
 	__syncthreads();
-	uint32_t span = 1;
-	while (span < nthr)
-		span <<= 1;
-	for (uint32_t stride2 = span >> 1; stride2 > 0; stride2 >>= 1) {
-		if (tid < stride2 && tid + stride2 < nthr) {
-			double x = s_sum[tid], xc = s_comp[tid];
-			neumaier_merge(x, xc, s_sum[tid + stride2], s_comp[tid + stride2]);
-			s_sum[tid] = x;
-			s_comp[tid] = xc;
-		}
-		__syncthreads();
-	}
 	double total = 0.0;
-	if (tid == 0)
-		total = isfinite(s_sum[0]) ? s_sum[0] + s_comp[0] : s_sum[0];
+	if (tid < 32) {
+		total = tid < nwarps ? s_red[tid] : 0.0;
+		for (int off = 16; off > 0; off >>= 1)
+			total += __shfl_down_sync(0xffffffffu, total, off);
+	}
 	__syncthreads();
 	return total;
 }
@@ -341,7 +330,8 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	const uint32_t ntiles = prm.ldp / prm.tile;
 	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 		const double tsum =
-			tile_walk<Idx>(a, t, s_dot, s_cnt, s_red, s_ops, s_runs, s_tips);
+			tile_walk<Idx>(a, t, (float *)s_dot, s_cnt, s_red, s_ops,
+				       s_runs, s_tips);
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
 	}
@@ -360,6 +350,95 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	const double total = block_fold(prm.block_sums, gridDim.x, s_red);
 	if (tid == 0) {
 		*prm.lnl_out = total;
+		*prm.ticket = 0u;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Fused evaluation of a short list in one launch (FP32, four states, four
+// categories, 128-pattern tiles: one thread per column, serial walk).  Every
+// block converts the device eigensystem to FP32, builds the list's
+// transition tables in shared memory with the same arithmetic as the
+// transition kernels (so results match a two-kernel evaluation bit for
+// bit), walks its tiles, and the last block writes the root lnL to the
+// device and to the host-mapped word.
+template <typename Idx>
+__global__ void __launch_bounds__(512, 2)
+prune4_direct_kernel(const __grid_constant__ DirectParams prm)
+{
+	constexpr uint32_t kC = 4, kTile = 128, kCols = kTile * kC;
+	__shared__ float4 s_tab[kDirectMax * 2 * kC * 5];
+	__shared__ float s_eig[36];
+	__shared__ double s_rate[kC];
+	__shared__ float s_dot[kCols];
+	__shared__ int32_t s_cnt[kCols];
+	__shared__ double s_red[32];
+	__shared__ unsigned s_last;
+	const uint32_t tid = threadIdx.x;
+	const ModelDev *m = prm.model;
+	if (tid < 16)
+		s_eig[tid] = (float)m->V[tid];
+	else if (tid < 32)
+		s_eig[tid] = (float)m->Vinv[tid - 16];
+	else if (tid < 36)
+		s_eig[tid] = (float)m->lambda[tid - 32];
+	else if (tid < 40)
+		s_rate[tid - 36] = prm.clock_rate * m->cat_rates[tid - 36];
+	__syncthreads();
+	if (tid < prm.n * 2 * kC) {
+		// table (entry, side, category), laid out as ptab4_kernel's
+		const uint32_t c = tid % kC, es = tid / kC;
+		float P[16];
+		transition4f_eig(m, s_eig, prm.lengths[es] * s_rate[c], P);
+		float *out = reinterpret_cast<float *>(s_tab + tid * 5);
+		for (int k = 0; k < 4; k++)
+			for (int j = 0; j < 4; j++)
+				out[k * 4 + j] = P[j * 4 + k];
+		for (int j = 0; j < 4; j++)
+			out[16 + j] = 1.0f;
+	}
+	__syncthreads();
+
+	TileArgs a;
+	a.tips = prm.tips;
+	a.part = (float4 *)prm.partials;
+	a.scales = prm.scales;
+	a.ptab = s_tab;
+	a.pi = prm.pi;
+	a.weights = prm.weights;
+	a.site_lnl = prm.site_lnl;
+	a.cat_lnl = nullptr;
+	a.ldp = prm.ldp;
+	a.C = kC;
+	a.L = prm.L;
+	a.tile = kTile;
+	a.n = prm.n;
+	a.n_runs = 0; // the serial walk needs no runs
+	a.tips_smem = 0;
+	a.log_inv_c = prm.log_inv_c;
+	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
+	const uint32_t ntiles = prm.ldp / kTile;
+	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const double tsum = tile_walk<Idx>(a, t, s_dot, s_cnt, s_red,
+						   prm.ops, nullptr, nullptr);
+		if (tid == 0)
+			neumaier_add(cta_sum, cta_comp, tsum);
+	}
+	if (tid == 0) {
+		prm.block_sums[blockIdx.x] =
+			isfinite(cta_sum) ? cta_sum + cta_comp : cta_sum;
+		__threadfence();
+		const unsigned tk = atomicAdd(prm.ticket, 1u);
+		s_last = (tk == gridDim.x - 1u);
+	}
+	__syncthreads();
+	if (!s_last)
+		return;
+	__threadfence();
+	const double total = block_fold(prm.block_sums, gridDim.x, s_red);
+	if (tid == 0) {
+		*prm.lnl_out = total;
+		*prm.lnl_host = total;
 		*prm.ticket = 0u;
 	}
 }
@@ -486,7 +565,8 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 			__syncthreads();
 		}
 		const double tsum =
-			tile_walk<Idx>(a, t, s_dot, s_cnt, s_red, s_ops, s_runs, s_tips);
+			tile_walk<Idx>(a, t, (float *)s_dot, s_cnt, s_red, s_ops,
+				       s_runs, s_tips);
 		const uint32_t tiles = md.ldp / a.tile;
 		if (tid == 0) {
 			md.tile_sums[t] = tsum;

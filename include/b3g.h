@@ -139,8 +139,8 @@ B3G_API b3g_status b3g_calculator_set_eigen(b3g_calculator *calc,
 					    int shortcuts);
 /* Reversible model from symmetric exchangeabilities in upper-triangle
  * row-major order (AC, AG, AT, CG, CT, GT for DNA: GTR::update_matrices,
- * substitution.rs:502-555) and frequencies.  Q is normalised to mean rate 1
- * and decomposed on the device in FP64 (symmetric Jacobi). */
+ * substitution.rs:502-555) and frequencies.  Q is normalised to mean rate 1,
+ * decomposed on the host in FP64 (symmetric Jacobi) and uploaded. */
 B3G_API b3g_status b3g_calculator_set_reversible(b3g_calculator *calc,
 						 const double *rates,
 						 const double *frequencies,
