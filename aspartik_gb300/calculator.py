@@ -50,6 +50,15 @@ class Calculator:
                              precision=self.precision, scale_ln=self.scale_ln,
                              num_categories=num_categories)
 
+    def make20(self, samples: np.ndarray, num_patterns: int,
+               num_categories: int = 1) -> "GpuCalculator":
+        """20-state (protein) counterpart of ``make4``; the reference has no
+        20-state calculator.  ``samples`` are state indices 0..19, any other
+        code is unknown; at most 8 categories."""
+        return GpuCalculator(samples, num_patterns, device=self.device,
+                             precision=self.precision, scale_ln=self.scale_ln,
+                             num_categories=num_categories, num_states=20)
+
 
 class GpuCalculator:
     """A device-resident pruning store for one alignment and one chain."""

@@ -160,6 +160,11 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 // pattern tiles.  Needs p.runs; block sums sized for `ctas`.
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			       cudaStream_t s);
+// 20-state path (prune20.cuh): transition tables [n][2][C][21][20] computed
+// in FP64, then one thread per (pattern, category) column walks the list;
+// blocks of 32 patterns x C (C <= 8) categories.
+cudaError_t launch_ptab20(const PtabParams &p, bool f32, cudaStream_t s);
+cudaError_t launch_prune20(const PruneParams &p, bool f32, cudaStream_t s);
 // Fused short-list evaluation: `ctas` persistent blocks over ldp / 128
 // pattern tiles; needs p.n <= kDirectMax and block sums sized for `ctas`.
 cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,

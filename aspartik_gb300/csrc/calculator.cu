@@ -63,9 +63,12 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_leaves must be >= 2");
 	if (cfg.num_patterns < 1)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_patterns must be >= 1");
-	if (cfg.num_states != 4)
+	if (cfg.num_states != 4 && cfg.num_states != 20)
 		throw Error(B3G_ERR_INVALID_ARGUMENT,
-			    "num_states must be 4 for this calculator");
+			    "num_states must be 4 (DNA) or 20 (protein)");
+	if (cfg.num_states == 20 && cfg.num_categories > 8)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "20-state calculators take at most 8 categories");
 	if (cfg.num_categories < 1 || cfg.num_categories > kMaxCategories)
 		throw Error(B3G_ERR_INVALID_ARGUMENT,
 			    "num_categories must be in 1..16");
@@ -112,7 +115,7 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		if (t == 32 || t == 64 || t == 128)
 			runs_tile_ = t;
 	}
-	use_runs_ = f32_ && runs_tile_ * C_ <= 512;
+	use_runs_ = f32_ && S_ == 4 && runs_tile_ * C_ <= 512;
 	// fused single-launch evaluation of short lists (B3G_DIRECT=0 turns
 	// it off, e.g. to time the two-kernel path)
 	use_direct_ = f32_ && S_ == 4 && C_ == 4;
@@ -179,16 +182,21 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		check_cuda(cudaHostGetDevicePointer((void **)&d_lnl_host_, h_lnl_, 0),
 			   "mapped lnl");
 
-		// tips: single bases -> 0..3, everything else -> unknown (4)
-		// (cpu4.rs:117-124); padded patterns are unknown too
-		std::vector<uint8_t> tips((size_t)L_ * ldp_, 4);
+		// DNA: single bases -> 0..3, everything else -> unknown (4)
+		// (cpu4.rs:117-124).  Protein: states 0..19 as given, anything
+		// else -> unknown (20).  Padded patterns are unknown too.
+		std::vector<uint8_t> tips((size_t)L_ * ldp_, (uint8_t)S_);
 		for (uint32_t l = 0; l < L_; ++l)
 			for (uint32_t p = 0; p < P_; ++p) {
-				uint8_t code = samples[(size_t)l * P_ + p];
-				uint8_t s = code == 1 ? 0 : code == 2 ? 1
-							   : code == 4 ? 2
-							   : code == 8 ? 3
-								       : 4;
+				const uint8_t code = samples[(size_t)l * P_ + p];
+				uint8_t s;
+				if (S_ == 4)
+					s = code == 1 ? 0 : code == 2 ? 1
+						   : code == 4 ? 2
+						   : code == 8 ? 3
+							       : 4;
+				else
+					s = code < S_ ? code : (uint8_t)S_;
 				tips[(size_t)l * ldp_ + p] = s;
 			}
 		check_cuda(cudaMemcpy(d_tips_, tips.data(), tips.size(),
@@ -401,6 +409,10 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	slot.direct = false;
 	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
 
+	if (S_ == 20) {
+		launch20(n, matrices_mode, clock_rate, want_cat, slot);
+		return;
+	}
 	PtabParams pt{};
 	pt.lengths = matrices_mode
 			     ? nullptr
@@ -460,6 +472,57 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	} else {
 		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
 	}
+	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
+	slot.pending = true;
+	++ring_next_;
+	check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
+				   cudaMemcpyDeviceToHost, stream_),
+		   "read lnl");
+	have_result_ = true;
+	stream_dirty_ = true;
+	cat_valid_ = want_cat;
+}
+
+// 20-state list: table kernel, then the column walk (prune20.cuh).
+void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
+			  bool want_cat, TimingSlot &slot)
+{
+	PtabParams pt{};
+	pt.lengths = matrices_mode
+			     ? nullptr
+			     : reinterpret_cast<const double *>(d_stage_ + off_in_);
+	pt.matrices = matrices_mode
+			      ? reinterpret_cast<const double *>(d_stage_ + off_in_)
+			      : nullptr;
+	pt.model = d_model_;
+	pt.clock_rate = clock_rate;
+	pt.n = n;
+	pt.C = C_;
+	pt.ptab = d_ptab_;
+	check_cuda(launch_ptab20(pt, f32_, stream_), "transition kernel");
+	check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+	PruneParams pp{};
+	pp.tips = d_tips_;
+	pp.partials = d_partials_;
+	pp.scales = d_scales_;
+	pp.ops = reinterpret_cast<const NodeOp *>(d_stage_);
+	pp.ptab = d_ptab_;
+	pp.pi = reinterpret_cast<const double *>(d_stage_ + off_pi_);
+	pp.weights = d_weights_;
+	pp.site_lnl = d_site_;
+	pp.cat_lnl = want_cat ? d_cat_ : nullptr;
+	pp.block_sums = d_block_sums_;
+	pp.ticket = d_ticket_;
+	pp.lnl_out = d_lnl_;
+	pp.n = n;
+	pp.ldp = ldp_;
+	pp.C = C_;
+	pp.scale_ln = scale_ln_;
+	pp.num_leaves = L_;
+	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
+	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
+	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
+	check_cuda(launch_prune20(pp, f32_, stream_), "pruning kernel");
 	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
 	slot.pending = true;
 	++ring_next_;

@@ -84,6 +84,9 @@ class Calculator {
 	void launch(uint32_t n, bool matrices_mode, double clock_rate,
 		    bool want_cat);
 	void launch_direct(uint32_t n, double clock_rate);
+	struct TimingSlot;
+	void launch20(uint32_t n, bool matrices_mode, double clock_rate,
+		      bool want_cat, TimingSlot &slot);
 	void upload_model();
 	void release();
 

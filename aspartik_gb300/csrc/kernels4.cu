@@ -585,14 +585,8 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 #include "runs4.cuh"
 
 // ---------------------------------------------------------------------------
-// Eigensystem of a reversible Q (FP64; run when the model changes, not per
-// step).  Parallel cyclic Jacobi on the symmetric B = D^1/2 Q D^-1/2,
-// D = diag(pi): in every round the indices form disjoint pairs in the
-// round-robin ("chess tournament") order of Brent and Luk, all pairs are
-// rotated at once (disjoint rotations commute), and one thread owns one
-// element of B and of the accumulated rotations U.  Then Q = V L V^-1 with
-// V = D^-1/2 U and V^-1 = U^T D^1/2.  One block of m x m threads, m = n
-// rounded up to even (the extra index is a dummy that never rotates).
+#include "prune20.cuh"
+
 } // namespace
 
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s)
@@ -689,6 +683,37 @@ cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
 	}
 	kern<<<ctas, 512, smem, s>>>(p);
 	return cudaGetLastError();
+}
+
+cudaError_t launch_ptab20(const PtabParams &p, bool f32, cudaStream_t s)
+{
+	const uint32_t tables = p.n * 2u * p.C;
+	if (f32)
+		ptab20_kernel<float><<<tables, kS20 * kS20, 0, s>>>(p);
+	else
+		ptab20_kernel<double><<<tables, kS20 * kS20, 0, s>>>(p);
+	return cudaGetLastError();
+}
+
+template <typename R, bool kPow2>
+static cudaError_t launch_prune20_t(const PruneParams &p, cudaStream_t s)
+{
+	const dim3 block(32, p.C), grid(p.ldp / 32);
+	const size_t smem = sizeof(double) * (2 * (size_t)block.x * block.y + 32);
+	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
+	if (narrow)
+		prune20_kernel<R, kPow2, uint32_t><<<grid, block, smem, s>>>(p);
+	else
+		prune20_kernel<R, kPow2, size_t><<<grid, block, smem, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_prune20(const PruneParams &p, bool f32, cudaStream_t s)
+{
+	if (p.C == 0 || p.C > 8 || p.ldp % 32u)
+		return cudaErrorInvalidValue;
+	return f32 ? launch_prune20_t<float, true>(p, s)
+		   : launch_prune20_t<double, false>(p, s);
 }
 
 cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,

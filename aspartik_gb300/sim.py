@@ -166,10 +166,11 @@ def random_dna(num_sequences: int, num_sites: int, rng: np.random.Generator) -> 
     return DNA_CODES[rng.integers(0, 4, size=(num_sequences, num_sites))]
 
 
-def deduplicate(msa: np.ndarray):
+def deduplicate(msa: np.ndarray, dna: bool = True):
     """Site-pattern compression (likelihood/mod.rs:74-132): unique columns in
     first-occurrence order, their counts, the pattern of every site, and the
-    leaf-major pattern matrix with gaps (code 0) mapped to 0b1111."""
+    leaf-major pattern matrix.  For DNA (IUPAC codes) gaps (code 0) map to
+    0b1111; for protein state indices (dna=False) codes are kept as given."""
     msa = np.ascontiguousarray(msa, dtype=np.uint8)
     L, N = msa.shape
     cols = np.ascontiguousarray(msa.T)
@@ -180,7 +181,8 @@ def deduplicate(msa: np.ndarray):
     rank = np.empty_like(order)
     rank[order] = np.arange(order.size)
     leaves = msa[:, first[order]].copy()
-    leaves[leaves == 0] = 0x0F
+    if dna:
+        leaves[leaves == 0] = 0x0F
     weights = counts[order].astype(np.uint32)
     site_to_pattern = rank[inverse.reshape(-1)].astype(np.uint32)
     return leaves, weights, site_to_pattern

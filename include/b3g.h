@@ -67,7 +67,7 @@ enum {
 typedef struct b3g_config {
 	uint32_t num_leaves;     /* L >= 2 */
 	uint32_t num_patterns;   /* P >= 1, site patterns after deduplication */
-	uint32_t num_states;     /* 4 (DNA) */
+	uint32_t num_states;     /* 4 (DNA) or 20 (protein, <= 8 categories) */
 	uint32_t num_categories; /* C in 1..16 rate categories */
 	uint32_t precision;      /* B3G_PRECISION_* */
 	uint32_t scale_ln;       /* FP64 form: rescale threshold e^-scale_ln;
@@ -91,7 +91,9 @@ B3G_API const char *b3g_version(void);
  * cuda_partials/mod.rs:171-284).  `samples` is the leaf-major
  * [num_leaves][num_patterns] array of 4-bit IUPAC codes that `deduplicate`
  * produces (likelihood/mod.rs:74-132); single bases map to states 0..3 and
- * every other code to "unknown" (cpu4.rs:117-124).  Partials start zeroed. */
+ * every other code to "unknown" (cpu4.rs:117-124).  With num_states = 20
+ * (no reference counterpart) the samples are state indices 0..19 and any
+ * other value is unknown.  Partials start zeroed. */
 B3G_API b3g_status b3g_calculator_create(const b3g_config *config,
 					 const uint8_t *samples,
 					 b3g_calculator **out);

@@ -5,7 +5,8 @@ site likelihood is the sum, over every assignment of states to the internal
 nodes, of pi(root state) times the product over edges of P(t)[parent state,
 child state], with P(t) = expm(Q t) from scipy.  Tips with a single-base
 code fix the child state; any other code is "unknown" and contributes 1, as
-calculator/cpu4.rs:117-124 maps them.  Sums run in numpy's longdouble.
+calculator/cpu4.rs:117-124 maps them.  With S != 4 states the codes are
+state indices and a code >= S is unknown.  Sums run in numpy's longdouble.
 """
 
 from __future__ import annotations
@@ -17,6 +18,12 @@ from scipy.linalg import expm
 
 TOMBSTONE = 0xFFFFFFFF
 _CODE_STATE = {1: 0, 2: 1, 4: 2, 8: 3}
+
+
+def _state(code, S):
+    if S == 4:
+        return _CODE_STATE.get(int(code))
+    return int(code) if int(code) < S else None
 
 
 def site_log_likelihoods(parents, heights, leaves, Q, pi, cat_rates=None,
@@ -51,8 +58,9 @@ def site_log_likelihoods(parents, heights, leaves, Q, pi, cat_rates=None,
                 w = w * mats[v][state[parents[v]], state[v]]
             for leaf in range(L):
                 Pm = mats[leaf][state[parents[leaf]]]
-                col = np.array([Pm[_CODE_STATE[c]] if c in _CODE_STATE else 1.0
-                                for c in leaves[leaf]], dtype=np.longdouble)
+                col = np.array([Pm[st] if st is not None else 1.0
+                                for st in (_state(c, S) for c in leaves[leaf])],
+                               dtype=np.longdouble)
                 w = w * col
             cat_lik += w
         total += cat_lik / len(cats)

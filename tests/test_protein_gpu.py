@@ -1,0 +1,120 @@
+"""20-state (protein) GPU path against the generic-S oracle.
+
+Tolerances (relative, on the log-likelihood): FP64 plain form 1e-10, FP32
+chosen form 1e-6.  Dirty-path evaluations must equal a fresh whole-tree
+evaluation bit for bit in the FP64 form.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import generic as G
+from oracle import oracle as O
+from tests.cases import protein_case
+from tests.test_gpu_parity import F32_TOL, F64_TOL, lists_and_lengths
+from tests.test_oracle import random_move
+
+pytestmark = pytest.mark.gpu
+
+
+def make20(c, precision, K, scale_ln=30):
+    from aspartik_gb300.calculator import Calculator
+
+    g = Calculator.GB300(0, precision).with_scale(scale_ln).make20(
+        c.leaves, c.leaves.shape[1], num_categories=K)
+    g.set_weights(c.weights)
+    return g
+
+
+def whole(tree):
+    tree.mark_all_edges_updated()
+    return lists_and_lengths(tree)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", F64_TOL), ("f32", F32_TOL)])
+@pytest.mark.parametrize("K,alpha", [(1, None), (4, 1.0), (3, 0.4)])
+def test_whole_tree_matches_generic_oracle(precision, tol, K, alpha):
+    c = protein_case(32, 600, seed=30 + K, alpha=alpha, num_categories=K, gaps=0.03)
+    model = O.reversible(c.rates, c.pi)
+    cats = O.gamma_categories(alpha, K) if alpha else None
+    want_site = G.site_log_likelihoods(c.leaves, c.tree.parents, c.tree.heights, model, cats)
+    want = float(want_site @ c.weights.astype(np.float64))
+    g = make20(c, precision, K)
+    g.set_reversible(c.rates, c.pi)
+    if K > 1:
+        g.set_gamma(alpha)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    g.propose_lengths(*whole(tree), 1.0)
+    assert g.log_likelihood() == pytest.approx(want, rel=tol)
+    np.testing.assert_allclose(g.site_log_likelihoods(), want_site,
+                               rtol=1e-9 if precision == "f64" else 2e-5)
+    g.close()
+
+
+def test_calculator_level_matrices_match_oracle():
+    """propose() with explicit matrices (calculator level, one category)."""
+    c = protein_case(16, 300, seed=41, alpha=None, num_categories=1)
+    model = O.reversible(c.rates, c.pi)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    internals, children, lengths = whole(tree)
+    mats = np.array([[model.transition(d) for d in pair] for pair in lengths])
+    want = G.prune(c.leaves, internals, children, mats, c.pi)
+    for precision, rtol in (("f64", 1e-10), ("f32", 1e-5)):
+        g = make20(c, precision, 1)
+        g.propose(internals, children, mats.reshape(len(internals), 2, 1, 20, 20), c.pi)
+        np.testing.assert_allclose(g.likelihoods(), want, rtol=rtol)
+        g.close()
+
+
+def test_dirty_paths_equal_full_recompute(rng):
+    c = protein_case(48, 800, seed=43, alpha=1.0, num_categories=4, gaps=0.02)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    g64, g32 = make20(c, "f64", 4), make20(c, "f32", 4)
+    for g in (g64, g32):
+        g.set_reversible(c.rates, c.pi)
+        g.set_gamma(1.0)
+        g.propose_lengths(*whole(tree), 1.0)
+        g.accept()
+    tree.accept()
+    for step in range(12):
+        random_move(tree, rng)
+        inc = lists_and_lengths(tree)
+        for g in (g64, g32):
+            g.propose_lengths(*inc, 1.0)
+        d64, d32 = g64.log_likelihood(), g32.log_likelihood()
+        fresh = make20(c, "f64", 4)
+        fresh.set_reversible(c.rates, c.pi)
+        fresh.set_gamma(1.0)
+        fresh.propose_lengths(*whole(O.DatedTree(np.array(tree.parents),
+                                                 np.array(tree.heights))), 1.0)
+        assert d64 == fresh.log_likelihood(), step  # bit-identical
+        assert d32 == pytest.approx(d64, rel=F32_TOL), step
+        fresh.close()
+        if rng.random() < 0.5:
+            tree.accept()
+            g64.accept()
+            g32.accept()
+        else:
+            tree.reject()
+            g64.reject()
+            g32.reject()
+    g64.close()
+    g32.close()
+
+
+def test_protein_workload_forms_agree():
+    """128 taxa x 5,000 sites, 20 states, Gamma4 alpha = 1: the FP32 chosen
+    form within 1e-6 of the FP64 plain form."""
+    c = protein_case(128, 5000, seed=4, alpha=1.0, num_categories=4)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    lists = whole(tree)
+    out = {}
+    for precision in ("f64", "f32"):
+        g = make20(c, precision, 4)
+        g.set_reversible(c.rates, c.pi)
+        g.set_gamma(1.0)
+        g.propose_lengths(*lists, 1.0)
+        out[precision] = g.log_likelihood()
+        g.close()
+    assert np.isfinite(out["f64"])
+    assert out["f32"] == pytest.approx(out["f64"], rel=F32_TOL)
