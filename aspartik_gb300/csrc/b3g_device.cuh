@@ -160,6 +160,35 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 // pattern tiles.  Needs p.runs; block sums sized for `ctas`.
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			       cudaStream_t s);
+// 20-state tensor-core path (prune20tc.cuh), FP32 chosen form.
+struct Tc20Params {
+	const uint8_t *tips;
+	float *partials;
+	int32_t *scales;
+	const NodeOp *ops;
+	const float *tab;    // [n][2][C][21][20] tip rows
+	const float *tc_tab; // [n][2][C][2][768] hi/lo MMA operand blocks
+	const double *pi;
+	const uint32_t *weights;
+	double *root_val;    // [C][ldp] pi . x at the root
+	int32_t *root_exp;   // [C][ldp] its power-of-two exponent
+	double *site_lnl;    // [ldp]
+	double *cat_lnl;     // [C][ldp] or null
+	double *block_sums;  // [ldp / 128]
+	unsigned *ticket;    // zero between launches
+	double *lnl_out;
+	unsigned *status;    // set to 1 when a bounded tensor-core wait gave up
+	uint32_t n, ldp, C, L;
+	uint32_t ops_smem;   // stage the list in shared memory
+	uint32_t tips_smem;  // stage the tile's tip codes in shared memory
+	double log_inv_c;
+};
+// Tables of both kinds for the tensor-core path: p.ptab receives the FP32
+// tip rows, tc_tab the operand blocks.
+cudaError_t launch_ptab20tc(const PtabParams &p, float *tc_tab, cudaStream_t s);
+// Pruning (one CTA per 128-pattern tile and category) then the root's
+// category mixing and fold.
+cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s);
 // 20-state path (prune20.cuh): transition tables [n][2][C][21][20] computed
 // in FP64, then one thread per (pattern, category) column walks the list;
 // blocks of 32 patterns x C (C <= 8) categories.

@@ -118,6 +118,10 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	use_runs_ = f32_ && S_ == 4 && runs_tile_ * C_ <= 512;
 	// fused single-launch evaluation of short lists (B3G_DIRECT=0 turns
 	// it off, e.g. to time the two-kernel path)
+	// 20-state FP32 lists on the tensor cores (B3G_TC20=0: CUDA-core walk)
+	use_tc20_ = f32_ && S_ == 20;
+	if (const char *env = std::getenv("B3G_TC20"))
+		use_tc20_ = use_tc20_ && std::atoi(env) != 0;
 	use_direct_ = f32_ && S_ == 4 && C_ == 4;
 	if (const char *env = std::getenv("B3G_DIRECT"))
 		use_direct_ = use_direct_ && std::atoi(env) != 0;
@@ -160,6 +164,18 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		dev_alloc(d_block_sums_, nblocks * sizeof(double), "block sums");
 		dev_alloc(d_ticket_, sizeof(unsigned), "ticket");
 		dev_alloc(d_lnl_, sizeof(double), "lnl");
+		if (use_tc20_) {
+			dev_alloc(d_tc_tab_, (size_t)I_ * 2 * C_ * 2 * 768 * sizeof(float),
+				  "tensor-core tables");
+			dev_alloc(d_root_val_, (size_t)C_ * ldp_ * sizeof(double), "root values");
+			dev_alloc(d_root_exp_, (size_t)C_ * ldp_ * sizeof(int32_t), "root exponents");
+			dev_alloc(d_status_, sizeof(unsigned), "status");
+			check_cuda(cudaMemset(d_status_, 0, sizeof(unsigned)), "zero status");
+			check_cuda(cudaHostAlloc((void **)&h_status_, sizeof(unsigned),
+						 cudaHostAllocDefault),
+				   "pinned status");
+			*h_status_ = 0;
+		}
 		dev_alloc(d_model_, sizeof(ModelDev), "model");
 		dev_alloc(d_ptab_, (size_t)I_ * 2 * C_ * (S_ + 1) * S_ * rsz,
 			  "transition tables");
@@ -242,6 +258,17 @@ void Calculator::release()
 	cudaFree(d_weights_);
 	cudaFree(d_site_);
 	cudaFree(d_cat_);
+	cudaFree(d_tc_tab_);
+	cudaFree(d_root_val_);
+	cudaFree(d_root_exp_);
+	cudaFree(d_status_);
+	if (h_status_)
+		cudaFreeHost(h_status_);
+	d_tc_tab_ = nullptr;
+	d_root_val_ = nullptr;
+	d_root_exp_ = nullptr;
+	d_status_ = nullptr;
+	h_status_ = nullptr;
 	cudaFree(d_block_sums_);
 	cudaFree(d_ticket_);
 	cudaFree(d_lnl_);
@@ -499,6 +526,50 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 	pt.n = n;
 	pt.C = C_;
 	pt.ptab = d_ptab_;
+	if (use_tc20_) {
+		check_cuda(launch_ptab20tc(pt, d_tc_tab_, stream_), "transition kernel");
+		check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+		Tc20Params tp{};
+		tp.tips = d_tips_;
+		tp.partials = static_cast<float *>(d_partials_);
+		tp.scales = d_scales_;
+		tp.ops = reinterpret_cast<const NodeOp *>(d_stage_);
+		tp.tab = static_cast<const float *>(d_ptab_);
+		tp.tc_tab = d_tc_tab_;
+		tp.pi = reinterpret_cast<const double *>(d_stage_ + off_pi_);
+		tp.weights = d_weights_;
+		tp.root_val = d_root_val_;
+		tp.root_exp = d_root_exp_;
+		tp.site_lnl = d_site_;
+		tp.cat_lnl = want_cat ? d_cat_ : nullptr;
+		tp.block_sums = d_block_sums_;
+		tp.ticket = d_ticket_;
+		tp.lnl_out = d_lnl_;
+		tp.status = d_status_;
+		tp.n = n;
+		tp.ldp = ldp_;
+		tp.C = C_;
+		tp.L = L_;
+		// the list and the tile's tip codes in shared memory when each
+		// fits in 32 KiB (two CTAs per SM still fit)
+		tp.ops_smem = (size_t)n * sizeof(NodeOp) <= 32u * 1024u ? 1u : 0u;
+		tp.tips_smem = (size_t)L_ * 128u <= 32u * 1024u ? 1u : 0u;
+		tp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
+		check_cuda(launch_prune20tc(tp, stream_), "tensor-core pruning kernel");
+		check_cuda(cudaEventRecord(slot.k1, stream_), "event");
+		slot.pending = true;
+		++ring_next_;
+		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
+					   cudaMemcpyDeviceToHost, stream_),
+			   "read lnl");
+		check_cuda(cudaMemcpyAsync(h_status_, d_status_, sizeof(unsigned),
+					   cudaMemcpyDeviceToHost, stream_),
+			   "read status");
+		have_result_ = true;
+		stream_dirty_ = true;
+		cat_valid_ = want_cat;
+		return;
+	}
 	check_cuda(launch_ptab20(pt, f32_, stream_), "transition kernel");
 	check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
 	PruneParams pp{};
@@ -688,6 +759,9 @@ double Calculator::log_likelihood()
 	if (!have_result_)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	if (h_status_ && *h_status_)
+		throw Error(B3G_ERR_TIMEOUT,
+			    "a tensor-core wait of the 20-state kernel gave up");
 	return *h_lnl_;
 }
 

@@ -173,6 +173,12 @@ class Calculator {
 	uint32_t runs_tile_ = 64;
 	bool use_runs_ = false;
 	bool use_direct_ = false;
+	bool use_tc20_ = false;
+	float *d_tc_tab_ = nullptr;     // 20-state MMA operand blocks
+	double *d_root_val_ = nullptr;  // [C][ldp] root pi . x per category
+	int32_t *d_root_exp_ = nullptr; // [C][ldp] its exponent
+	unsigned *d_status_ = nullptr;  // bounded tensor-core waits
+	unsigned *h_status_ = nullptr;
 };
 
 } // namespace b3g

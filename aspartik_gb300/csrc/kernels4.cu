@@ -24,6 +24,7 @@
 // the other buffer, every slot stores the count of its whole subtree, so the
 // root count is always exact, also when a proposal is evaluated twice.
 #include "b3g_device.cuh"
+#include "tc_ptx.cuh"
 
 #include <math.h>
 
@@ -586,6 +587,7 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 
 // ---------------------------------------------------------------------------
 #include "prune20.cuh"
+#include "prune20tc.cuh"
 
 } // namespace
 
@@ -714,6 +716,32 @@ cudaError_t launch_prune20(const PruneParams &p, bool f32, cudaStream_t s)
 		return cudaErrorInvalidValue;
 	return f32 ? launch_prune20_t<float, true>(p, s)
 		   : launch_prune20_t<double, false>(p, s);
+}
+
+cudaError_t launch_ptab20tc(const PtabParams &p, float *tc_tab, cudaStream_t s)
+{
+	ptab20tc_kernel<<<p.n * 2u * p.C, 768, 0, s>>>(p, tc_tab);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s)
+{
+	if (p.C == 0 || p.C > 8 || p.ldp % kTcRows || p.n == 0)
+		return cudaErrorInvalidValue;
+	const bool narrow = (uint64_t)p.L * 2 * p.C * p.ldp < (1ull << 31);
+	auto kern = narrow ? prune20tc_kernel<uint32_t> : prune20tc_kernel<size_t>;
+	const int smem = (int)(kTcSmem + 1024 + (p.ops_smem ? p.n * sizeof(NodeOp) : 0) +
+			       (p.tips_smem ? p.L * kTcRows : 0));
+	cudaError_t e = cudaFuncSetAttribute(
+		kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+	if (e != cudaSuccess)
+		return e;
+	kern<<<dim3(p.ldp / kTcRows, p.C), 128, smem, s>>>(p);
+	e = cudaGetLastError();
+	if (e != cudaSuccess)
+		return e;
+	finish20_kernel<<<p.ldp / kTcRows, 128, 0, s>>>(p);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,

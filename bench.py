@@ -311,6 +311,53 @@ def batched(device: int, steps: int, warmup: int, chains: int = 32, seed: int = 
                       "persistent pruning kernel, read-back"}
 
 
+def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
+    """The 20-state workload: 128 taxa, 5,000 sites, exchangeabilities
+    r_ij ~ LogNormal(0, 1) (190 values), pi ~ Dir(1 x 20), Gamma4 alpha = 1,
+    simulated down a seeded Yule tree.  Whole-tree evaluations of both
+    forms, device time per evaluation from CUDA events; GB/s counts the
+    algorithmic bytes with S = 20, TFLOP/s the algorithmic flops
+    sum_v C P (2 S^2 per internal child + S)."""
+    from aspartik_gb300.calculator import Calculator
+
+    rng = np.random.default_rng(seed)
+    L, N, K = 128, 5000, 4
+    tree = sim.yule_tree(L, rng, root_height=1.0)
+    pi = sim.dirichlet([1.0] * 20, rng)
+    pi = np.maximum(pi, 1e-4)
+    pi /= pi.sum()
+    rates = rng.lognormal(0.0, 1.0, size=190)
+    Q = sim.reversible_q(rates, pi)
+    states = sim.simulate_alignment(tree, N, Q, pi, rng, cat_rates=sim.gamma_rates(1.0, K))
+    leaves, weights, _ = sim.deduplicate(states, dna=False)
+    P = leaves.shape[1]
+    top = schedule.Topology(tree.parents, tree.heights)
+    lists = top.full()
+    ch = top.children[np.asarray(lists[0], dtype=np.int64) - top.L]
+    n_int = int((ch >= top.L).sum())
+    flops = K * P * (n_int * 2 * 20 * 20 + len(lists[0]) * 20)
+    out = {"workload": "prot128x5000_rev20_g4", "taxa": L, "sites": N, "patterns": P,
+           "categories": K, "states": 20}
+    for precision, w in (("f32", 4), ("f64", 8)):
+        calc = Calculator.GB300(device, precision).make20(leaves, P, num_categories=K)
+        calc.set_weights(weights)
+        calc.set_reversible(rates, pi)
+        calc.set_gamma(1.0)
+        k = steps if precision == "f32" else max(3, min(steps, 20))
+        ms, _, prune_ms, _ = device_throughput(calc, lists, k, warmup, 1)
+        lnl = calc.log_likelihood()
+        calc.close()
+        b = schedule.algorithmic_bytes(top, lists[0], P, K, 20, w=w, e_b=4, w_p=w)
+        out[precision] = {"ms_per_eval": round(ms / k, 5), "kernel_ms": round(prune_ms, 5),
+                          "bytes_per_eval": b, "GB_s": round(b / (ms / k * 1e-3) / 1e9, 2),
+                          "kernel_GB_s": round(b / (prune_ms * 1e-3) / 1e9, 2),
+                          "kernel_TFLOP_s": round(flops / (prune_ms * 1e-3) / 1e12, 3),
+                          "lnl": lnl}
+    out["flops_per_eval"] = flops
+    out["lnl_rel_err_f32_vs_f64"] = abs(out["f32"]["lnl"] - out["f64"]["lnl"]) / abs(out["f64"]["lnl"])
+    return out
+
+
 def mcmc_ess(wl, steps: int, device: int) -> dict:
     """ESS per second of the cold chain on the workload: the plain FP64 form,
     the FP32 chosen form, and the chosen form with delayed-acceptance
@@ -422,6 +469,7 @@ def run_ours(args):
     c64.close()
 
     mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
+    prot = None if args.no_protein else protein20(device, min(args.steps, 100), args.warmup)
     batch = None if args.no_batch else batched(device, min(args.steps, 200), args.warmup)
 
     cpu = None
@@ -475,6 +523,7 @@ def run_ours(args):
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
         "batched": batch,
+        "protein20": prot,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
@@ -533,6 +582,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-chains leg")
+    ap.add_argument("--no-protein", action="store_true", help="skip the 20-state leg")
     ap.add_argument("--mcmc-steps", type=int, default=20000,
                     help="MCMC steps per form for the ESS/s comparison (0 = skip)")
     args = ap.parse_args()

@@ -118,3 +118,48 @@ def test_protein_workload_forms_agree():
         g.close()
     assert np.isfinite(out["f64"])
     assert out["f32"] == pytest.approx(out["f64"], rel=F32_TOL)
+
+
+def make20_cuda_cores(c, K):
+    """FP32 calculator that walks on the CUDA cores instead of the tensor
+    cores (B3G_TC20=0 at construction)."""
+    import os
+
+    old = os.environ.get("B3G_TC20")
+    os.environ["B3G_TC20"] = "0"
+    try:
+        return make20(c, "f32", K)
+    finally:
+        if old is None:
+            os.environ.pop("B3G_TC20", None)
+        else:
+            os.environ["B3G_TC20"] = old
+
+
+def test_tensor_core_path_matches_cuda_core_walk(rng):
+    """3xTF32 MMAs (FP32 accumulation) against the FP32 CUDA-core walk and
+    the FP64 form, whole tree and dirty paths."""
+    c = protein_case(40, 700, seed=47, alpha=0.8, num_categories=4, gaps=0.02)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    tc, cc, g64 = make20(c, "f32", 4), make20_cuda_cores(c, 4), make20(c, "f64", 4)
+    for g in (tc, cc, g64):
+        g.set_reversible(c.rates, c.pi)
+        g.set_gamma(0.8)
+        g.propose_lengths(*whole(tree), 1.0)
+        g.accept()
+    tree.accept()
+    for step in range(10):
+        random_move(tree, rng)
+        inc = lists_and_lengths(tree)
+        for g in (tc, cc, g64):
+            g.propose_lengths(*inc, 1.0)
+        a, b, ref = tc.log_likelihood(), cc.log_likelihood(), g64.log_likelihood()
+        assert a == pytest.approx(ref, rel=F32_TOL), step
+        assert a == pytest.approx(b, rel=F32_TOL), step
+        np.testing.assert_allclose(tc.site_log_likelihoods(), g64.site_log_likelihoods(),
+                                   rtol=2e-5)
+        tree.accept()
+        for g in (tc, cc, g64):
+            g.accept()
+    for g in (tc, cc, g64):
+        g.close()
