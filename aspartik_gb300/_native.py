@@ -133,6 +133,8 @@ SIGNATURES = {
     "b3g_calculator_propose_lengths": (
         ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
     "b3g_calculator_log_likelihood": (ct.c_int, [_vp, _f64p]),
+    "b3g_calculator_autotune": (
+        ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double, _u32p]),
     "b3g_calculator_site_log_likelihoods": (ct.c_int, [_vp, _f64p]),
     "b3g_calculator_last_timing": (ct.c_int, [_vp, _f32p, _f32p]),
     "b3g_calculator_timing_totals": (

@@ -172,6 +172,23 @@ class GpuCalculator:
             self._h, nat.as_ptr(internals, ct.c_uint32), nat.as_ptr(children, ct.c_uint32),
             n, nat.as_ptr(lengths, ct.c_double), float(clock_rate)))
 
+    def autotune(self, internals, children, lengths, clock_rate: float = 1.0) -> int:
+        """Time the list with each launch configuration of this form and keep
+        the fastest (no counterpart in the reference); returns the patterns
+        per tile (4 states), 1 / 0 for tensor / CUDA cores (20 states), 0 for
+        the FP64 form.  Trial proposals are rejected: call between steps."""
+        internals = nat.u32(internals)
+        children = nat.u32(children).reshape(-1)
+        lengths = nat.f64(lengths).reshape(-1)
+        n = internals.size
+        if children.size != 2 * n or lengths.size != 2 * n:
+            raise ValueError("children and lengths need two values per internal")
+        out = ct.c_uint32()
+        check(lib.b3g_calculator_autotune(
+            self._h, nat.as_ptr(internals, ct.c_uint32), nat.as_ptr(children, ct.c_uint32),
+            n, nat.as_ptr(lengths, ct.c_double), float(clock_rate), ct.byref(out)))
+        return int(out.value)
+
     def log_likelihood(self) -> float:
         out = ct.c_double()
         check(lib.b3g_calculator_log_likelihood(self._h, ct.byref(out)))

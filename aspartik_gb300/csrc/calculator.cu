@@ -846,6 +846,57 @@ float Calculator::span_end()
 	return ms;
 }
 
+uint32_t Calculator::autotune(const uint32_t *internals,
+			      const uint32_t *children, uint32_t n,
+			      const double *lengths, double clock_rate)
+{
+	DeviceGuard g(device_);
+	if (!f32_)
+		return 0;
+	// best of three timed evaluations after one warm-up, each rejected
+	auto trial = [&]() {
+		float best = INFINITY;
+		for (int r = 0; r < 4; ++r) {
+			propose_lengths(internals, children, n, lengths, clock_rate);
+			(void)log_likelihood();
+			float t = 0.0f, p = 0.0f;
+			last_timing(&t, &p);
+			reject();
+			if (r > 0)
+				best = std::min(best, t + p);
+		}
+		return best;
+	};
+	if (S_ == 20) {
+		if (!d_tc_tab_) // built without tensor-core buffers
+			return 0;
+		use_tc20_ = true;
+		const float tc = trial();
+		use_tc20_ = false;
+		const float cc = trial();
+		use_tc20_ = tc <= cc;
+		return use_tc20_ ? 1u : 0u;
+	}
+	// the direct launch of short lists and path-like lists do not use the
+	// tuned tile
+	if (!use_runs_ || (use_direct_ && n <= kDirectMax))
+		return runs_tile_;
+	uint32_t best_tile = runs_tile_;
+	float best_ms = INFINITY;
+	for (const uint32_t t : {32u, 64u, 128u}) {
+		if (t * C_ > 512)
+			continue;
+		runs_tile_ = t;
+		const float ms = trial();
+		if (ms < best_ms) {
+			best_ms = ms;
+			best_tile = t;
+		}
+	}
+	runs_tile_ = best_tile;
+	return best_tile;
+}
+
 void Calculator::accept()
 {
 	// Cpu4Calculator::accept (cpu4.rs:78-83): EditBuf::accept
@@ -1186,6 +1237,20 @@ B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms)
 		if (!ms)
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
 		*ms = calc_of(calc)->span_end();
+	});
+}
+
+B3G_API b3g_status b3g_calculator_autotune(b3g_calculator *calc,
+					   const uint32_t *internals,
+					   const uint32_t *children, uint32_t n,
+					   const double *lengths,
+					   double clock_rate, uint32_t *choice)
+{
+	return guarded([&] {
+		if (!choice)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*choice = calc_of(calc)->autotune(internals, children, n, lengths,
+						  clock_rate);
 	});
 }
 

@@ -69,6 +69,8 @@ class Calculator {
 	void span_begin();
 	float span_end();
 	uint64_t last_upload_bytes() const { return last_upload_bytes_; }
+	uint32_t autotune(const uint32_t *internals, const uint32_t *children,
+			  uint32_t n, const double *lengths, double clock_rate);
 
 	// Batched evaluation: validate and stage a dirty-path evaluation
 	// without launching; a Batch evaluates all staged members at once.

@@ -176,6 +176,15 @@ void Mcmc::set_parameters(double kappa, const double *rates,
 		ch.prior_cache = prior(ch);
 		ch.launched = ch.model_sent = ch.alpha_sent = false;
 	}
+	// the launch configuration for this alignment and GPU, tuned once on
+	// the whole tree (trial proposals are rejected)
+	if (cfg_.precision == B3G_PRECISION_F32 && !tuned_) {
+		for (auto &chp : chains_)
+			chp->calc->autotune(chp->internals.data(), chp->children.data(),
+					    (uint32_t)chp->internals.size(),
+					    chp->lengths.data(), 1.0);
+		tuned_ = true;
+	}
 }
 
 // Yule (priors/yule.rs:23-40), LogNormal parameter priors and symmetric

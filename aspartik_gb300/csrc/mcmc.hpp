@@ -216,6 +216,7 @@ class Mcmc {
 	std::vector<double> drift_;
 	size_t drift_pos_ = 0;
 	DaStats da_;
+	bool tuned_ = false; // the calculators' launch configuration is tuned
 };
 
 } // namespace b3g

@@ -59,6 +59,11 @@ WORKLOADS = {
                            root_height=0.5, pi_conc=10.0),
 }
 DEFAULT_WORKLOAD = "dna256x20000_gtr_g4"
+# DRAM bytes (read + write) of one whole-tree launch of prune4_runs_kernel on
+# the default workload, from an ncu capture (dram__bytes_read.sum 55.06 MB +
+# dram__bytes_write.sum 305.74 MB); children written earlier in the same pass
+# are re-read from L2, so this is about half the algorithmic bytes.
+TRAFFIC_RUNS_BYTES = 360_801_024
 
 
 def make_workload(name: str, seed: int = 4) -> dict:
@@ -207,36 +212,43 @@ def device_throughput(calc, lists, steps, warmup, world):
     return ms, tt / max(n, 1), tp / max(n, 1), n
 
 
-def cpu_oracle_eval(wl, num_threads: int, pattern_limit: int | None = None):
-    """One whole-tree evaluation on the CPU oracle (restated cpu4, one
-    calculator per category as GammaLikelihood runs them).  Returns
-    (seconds, patterns used, threads)."""
-    from oracle import oracle as O
+class CpuReference:
+    """The restated cpu4 on (a pattern sample of) the workload, built once:
+    one calculator per category as GammaLikelihood runs them
+    (likelihood/gamma.rs:97-169), the transition matrices of the whole tree,
+    `threads` host threads.  `evaluate()` times one whole-tree evaluation
+    (propose of every category, log-sum-exp mixing, weighted sum)."""
 
-    leaves = wl["leaves"]
-    weights = wl["weights"]
-    if pattern_limit is not None and pattern_limit < leaves.shape[1]:
-        leaves = np.ascontiguousarray(leaves[:, :pattern_limit])
-        weights = weights[:pattern_limit]
-    P = leaves.shape[1]
-    top = wl["top"]
-    internals, children, lengths = top.full()
-    model = O.gtr(wl["rates"], wl["pi"])
-    cats = O.gamma_categories(wl["spec"]["alpha"], wl["spec"]["categories"]) \
-        if wl["spec"]["alpha"] else np.ones(1)
-    mats = [np.stack([model.transition(d * r) for d in lengths.reshape(-1)]) for r in cats]
-    calcs = [O.Cpu4Calculator(leaves, P, 30, num_threads) for _ in cats]
-    t0 = time.perf_counter()
-    per = []
-    for calc, m in zip(calcs, mats):
-        calc.propose(internals, children, m, wl["pi"])
-        per.append(calc.likelihoods())
-    per = np.array(per)
-    mx = per.max(axis=0)
-    site = mx + np.log(np.exp(per - mx).sum(axis=0)) + np.log(1.0 / len(cats))
-    lnl = float(site @ weights.astype(np.float64))
-    dt = time.perf_counter() - t0
-    return dt, P, calcs[0].num_threads(), lnl
+    def __init__(self, wl, num_threads: int, pattern_limit: int | None = None):
+        from oracle import oracle as O
+
+        leaves, weights = wl["leaves"], wl["weights"]
+        if pattern_limit is not None and pattern_limit < leaves.shape[1]:
+            leaves = np.ascontiguousarray(leaves[:, :pattern_limit])
+            weights = weights[:pattern_limit]
+        self.P = leaves.shape[1]
+        self.weights = weights.astype(np.float64)
+        self.pi = wl["pi"]
+        self.internals, self.children, lengths = wl["top"].full()
+        model = O.gtr(wl["rates"], wl["pi"])
+        cats = O.gamma_categories(wl["spec"]["alpha"], wl["spec"]["categories"]) \
+            if wl["spec"]["alpha"] else np.ones(1)
+        self.mats = [np.stack([model.transition(d * r) for d in lengths.reshape(-1)])
+                     for r in cats]
+        self.calcs = [O.Cpu4Calculator(leaves, self.P, 30, num_threads) for _ in cats]
+        self.threads = self.calcs[0].num_threads()
+
+    def evaluate(self):
+        t0 = time.perf_counter()
+        per = []
+        for calc, m in zip(self.calcs, self.mats):
+            calc.propose(self.internals, self.children, m, self.pi)
+            per.append(calc.likelihoods())
+        per = np.array(per)
+        mx = per.max(axis=0)
+        site = mx + np.log(np.exp(per - mx).sum(axis=0)) + np.log(1.0 / len(self.calcs))
+        lnl = float(site @ self.weights)
+        return time.perf_counter() - t0, lnl
 
 
 def batched(device: int, steps: int, warmup: int, chains: int = 32, seed: int = 4) -> dict:
@@ -343,6 +355,12 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
         calc.set_weights(weights)
         calc.set_reversible(rates, pi)
         calc.set_gamma(1.0)
+        engine = None
+        if precision == "f32":
+            calc.propose_lengths(*lists, 1.0)
+            calc.log_likelihood()
+            calc.accept()
+            engine = "tensor cores" if calc.autotune(*lists, 1.0) else "CUDA cores"
         k = steps if precision == "f32" else max(3, min(steps, 20))
         ms, _, prune_ms, _ = device_throughput(calc, lists, k, warmup, 1)
         lnl = calc.log_likelihood()
@@ -353,6 +371,8 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
                           "kernel_GB_s": round(b / (prune_ms * 1e-3) / 1e9, 2),
                           "kernel_TFLOP_s": round(flops / (prune_ms * 1e-3) / 1e12, 3),
                           "lnl": lnl}
+        if engine:
+            out[precision]["engine"] = engine
     out["flops_per_eval"] = flops
     out["lnl_rel_err_f32_vs_f64"] = abs(out["f32"]["lnl"] - out["f64"]["lnl"]) / abs(out["f64"]["lnl"])
     return out
@@ -423,6 +443,12 @@ def run_ours(args):
     pk = peaks()
 
     calc = make_calc(wl, "f32", device)
+    # the library's autotuner picks the tile size of the whole-tree walk
+    # (trial evaluations are rejected; outside the timed region)
+    calc.propose_lengths(*full, 1.0)
+    calc.log_likelihood()
+    calc.accept()
+    tile = calc.autotune(*full, 1.0)
     clocks = ClockSampler(device)
     clocks.start()
     time.sleep(0.3)
@@ -475,10 +501,12 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
-        dt1, Pu, thr, cpu_lnl = cpu_oracle_eval(wl, cores)
+        ref = CpuReference(wl, cores)
+        dt1, cpu_lnl = ref.evaluate()
         reps = int(max(1, min(20, 5.0 / max(dt1, 1e-3))))
-        times = [cpu_oracle_eval(wl, cores)[0] for _ in range(reps)]
+        times = [ref.evaluate()[0] for _ in range(reps)]
         t_cpu = statistics.median(times)
+        Pu, thr = ref.P, ref.threads
         cpu = {"value": round(B32 / t_cpu / 1e9, 4), "unit": UNIT, "cores": thr,
                "kind": "port",
                "sample": f"{reps} whole-tree evaluations of the full workload ({Pu} patterns x "
@@ -504,8 +532,12 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
-                     "traffic": None, "peak_source": pk["source"],
+                     "traffic": TRAFFIC_RUNS_BYTES if args.workload == DEFAULT_WORKLOAD else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                       "one whole-tree launch of this workload",
+                     "peak_source": pk["source"],
                      "kernel": "prune4_runs_kernel (FP32, run-synchronous)",
+                     "tile_patterns": tile,
                      "kernel_ms": round(t_pr, 5), "transition_kernel_ms": round(t_tr, 5)},
         "e2e": {"value": round(e2e, 2), "unit": UNIT,
                 "h2d_bytes_per_step": h2d,
@@ -540,17 +572,19 @@ def run_reference(args):
     C = spec["categories"]
     full = top.full()
     cores = os.cpu_count() or 1
-    # bound the run: size each step's pattern sample so that warmup + steps
-    # take about a minute at most
-    dt1, _, thr, _ = cpu_oracle_eval(wl, cores)
+    # bound the run: each step's pattern sample is sized so that warmup +
+    # steps take about a minute of evaluation at most
+    dt1, _ = CpuReference(wl, cores).evaluate()
     budget = 60.0
     frac = min(1.0, budget / max(dt1 * (args.steps + args.warmup), 1e-9))
     Pu = max(128, int(P * frac)) if frac < 1.0 else P
+    ref = CpuReference(wl, cores, Pu)
+    thr = ref.threads
     for _ in range(args.warmup):
-        cpu_oracle_eval(wl, cores, Pu)
+        ref.evaluate()
     total = 0.0
     for _ in range(args.steps):
-        total += cpu_oracle_eval(wl, cores, Pu)[0]
+        total += ref.evaluate()[0]
     B = schedule.algorithmic_bytes(top, full[0], Pu, C, 4, w=4, e_b=4, w_p=4)
     value = args.steps * B / total / 1e9
     sample = (f"whole-tree evaluations over {Pu} of {P} patterns x {C} categories per step; "

@@ -197,6 +197,20 @@ B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
 B3G_API b3g_status b3g_calculator_span_begin(b3g_calculator *calc);
 B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
 
+/* Autotuner (no counterpart in the reference).  Times a representative list
+ * (normally the whole tree) with each launch configuration of this
+ * calculator's form and keeps the fastest: patterns per tile of the
+ * run-synchronous walk (32, 64 or 128; four-state FP32), or tensor cores
+ * against CUDA cores (20-state FP32).  Every trial proposal is rejected, so
+ * call it between steps; the accepted state is unchanged.  `choice`
+ * receives the tile, or 1 (tensor cores) / 0 (CUDA cores); the FP64 form
+ * has nothing to tune and returns 0. */
+B3G_API b3g_status b3g_calculator_autotune(b3g_calculator *calc,
+					   const uint32_t *internals,
+					   const uint32_t *children, uint32_t n,
+					   const double *lengths,
+					   double clock_rate, uint32_t *choice);
+
 /* ---- batched evaluation ----------------------------------------------------
  * Many calculators (chains: replicates or heated copies, each with its own
  * alignment, tree and model) evaluated by one launch.  Members stage their
