@@ -141,6 +141,15 @@ __global__ void __launch_bounds__(128) prune20tc_kernel(Tc20Params prm)
 	const uint32_t tmem = holder;
 	const uint32_t lane_base = (32u * warp) << 16;
 	constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
+	// operand descriptors of K step 0: [child][hi, lo]
+	uint64_t dA[2][2], dB[2][2];
+#pragma unroll
+	for (uint32_t j = 0; j < 2; j++)
+#pragma unroll
+		for (uint32_t h = 0; h < 2; h++) {
+			dA[j][h] = tc::smem_desc(tc::smem_u32(sA + (2 * j + h) * kTcA), 128, 768);
+			dB[j][h] = tc::smem_desc(tc::smem_u32(sB + (2 * j + h) * kTcB), 128, 768);
+		}
 
 	// Inputs of one entry, fetched into registers ahead of their use: for
 	// an internal side the child's partial row, scale and this side's
@@ -223,19 +232,17 @@ __global__ void __launch_bounds__(128) prune20tc_kernel(Tc20Params prm)
 				for (uint32_t j = 0; j < 2; j++) {
 					if (ids[j] & kTipBit)
 						continue;
-					const uint32_t a0 = tc::smem_u32(sA + (2 * j) * kTcA);
-					const uint32_t b0 = tc::smem_u32(sB + (2 * j) * kTcB);
+					// the start address sits in the low bits (>> 4):
+					// the next K step (+256 B) adds 16
 #pragma unroll
 					for (uint32_t s = 0; s < 3; s++) {
 						// x_hi P_hi, x_hi P_lo, x_lo P_hi
-#pragma unroll
-						for (uint32_t term = 0; term < 3; term++) {
-							const uint32_t a = a0 + (term == 2 ? kTcA * 4 : 0) + s * 256;
-							const uint32_t b = b0 + (term == 1 ? kTcB * 4 : 0) + s * 256;
-							tc::mma_tf32(tmem + 32 * j, tc::smem_desc(a, 128, 768),
-								     tc::smem_desc(b, 128, 768), idesc,
-								     (s | term) != 0);
-						}
+						tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
+							     dB[j][0] + 16 * s, idesc, s != 0);
+						tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
+							     dB[j][1] + 16 * s, idesc, 1);
+						tc::mma_tf32(tmem + 32 * j, dA[j][1] + 16 * s,
+							     dB[j][0] + 16 * s, idesc, 1);
 					}
 				}
 				tc::mma_commit(mb);

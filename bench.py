@@ -323,7 +323,8 @@ def batched(device: int, steps: int, warmup: int, chains: int = 32, seed: int = 
                       "persistent pruning kernel, read-back"}
 
 
-def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
+def protein20(device: int, steps: int, warmup: int, seed: int = 4, L: int = 128,
+              N: int = 5000, forms=("f32", "f64")) -> dict:
     """The 20-state workload: 128 taxa, 5,000 sites, exchangeabilities
     r_ij ~ LogNormal(0, 1) (190 values), pi ~ Dir(1 x 20), Gamma4 alpha = 1,
     simulated down a seeded Yule tree.  Whole-tree evaluations of both
@@ -333,7 +334,7 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
     from aspartik_gb300.calculator import Calculator
 
     rng = np.random.default_rng(seed)
-    L, N, K = 128, 5000, 4
+    K = 4
     tree = sim.yule_tree(L, rng, root_height=1.0)
     pi = sim.dirichlet([1.0] * 20, rng)
     pi = np.maximum(pi, 1e-4)
@@ -348,15 +349,26 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
     ch = top.children[np.asarray(lists[0], dtype=np.int64) - top.L]
     n_int = int((ch >= top.L).sum())
     flops = K * P * (n_int * 2 * 20 * 20 + len(lists[0]) * 20)
-    out = {"workload": "prot128x5000_rev20_g4", "taxa": L, "sites": N, "patterns": P,
+    out = {"workload": f"prot{L}x{N}_rev20_g4", "taxa": L, "sites": N, "patterns": P,
            "categories": K, "states": 20}
-    for precision, w in (("f32", 4), ("f64", 8)):
-        calc = Calculator.GB300(device, precision).make20(leaves, P, num_categories=K)
+    for form in forms:
+        precision = "f64" if form == "f64" else "f32"
+        w = 8 if precision == "f64" else 4
+        old_env = os.environ.get("B3G_TC20")
+        if form == "f32_cuda_cores":
+            os.environ["B3G_TC20"] = "0"
+        try:
+            calc = Calculator.GB300(device, precision).make20(leaves, P, num_categories=K)
+        finally:
+            if old_env is None:
+                os.environ.pop("B3G_TC20", None)
+            else:
+                os.environ["B3G_TC20"] = old_env
         calc.set_weights(weights)
         calc.set_reversible(rates, pi)
         calc.set_gamma(1.0)
-        engine = None
-        if precision == "f32":
+        engine = "CUDA cores" if form == "f32_cuda_cores" else None
+        if form == "f32":
             calc.propose_lengths(*lists, 1.0)
             calc.log_likelihood()
             calc.accept()
@@ -366,15 +378,20 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4) -> dict:
         lnl = calc.log_likelihood()
         calc.close()
         b = schedule.algorithmic_bytes(top, lists[0], P, K, 20, w=w, e_b=4, w_p=w)
-        out[precision] = {"ms_per_eval": round(ms / k, 5), "kernel_ms": round(prune_ms, 5),
+        out[form] = {"ms_per_eval": round(ms / k, 5), "kernel_ms": round(prune_ms, 5),
                           "bytes_per_eval": b, "GB_s": round(b / (ms / k * 1e-3) / 1e9, 2),
                           "kernel_GB_s": round(b / (prune_ms * 1e-3) / 1e9, 2),
                           "kernel_TFLOP_s": round(flops / (prune_ms * 1e-3) / 1e12, 3),
                           "lnl": lnl}
         if engine:
-            out[precision]["engine"] = engine
+            out[form]["engine"] = engine
     out["flops_per_eval"] = flops
-    out["lnl_rel_err_f32_vs_f64"] = abs(out["f32"]["lnl"] - out["f64"]["lnl"]) / abs(out["f64"]["lnl"])
+    if "f64" in out:
+        out["lnl_rel_err_f32_vs_f64"] = abs(out["f32"]["lnl"] - out["f64"]["lnl"]) / abs(
+            out["f64"]["lnl"])
+    if "f32_cuda_cores" in out:
+        out["lnl_rel_diff_tensor_vs_cuda_cores"] = abs(
+            out["f32"]["lnl"] - out["f32_cuda_cores"]["lnl"]) / abs(out["f32_cuda_cores"]["lnl"])
     return out
 
 
@@ -495,7 +512,11 @@ def run_ours(args):
     c64.close()
 
     mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
-    prot = None if args.no_protein else protein20(device, min(args.steps, 100), args.warmup)
+    prot = prot_big = None
+    if not args.no_protein:
+        prot = protein20(device, min(args.steps, 100), args.warmup)
+        prot_big = protein20(device, min(args.steps, 20), args.warmup, N=50000,
+                             forms=("f32", "f32_cuda_cores"))
     batch = None if args.no_batch else batched(device, min(args.steps, 200), args.warmup)
 
     cpu = None
@@ -556,6 +577,7 @@ def run_ours(args):
         "mcmc": mcmc,
         "batched": batch,
         "protein20": prot,
+        "protein20_large": prot_big,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
