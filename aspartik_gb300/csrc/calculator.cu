@@ -434,7 +434,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	if (slot.pending)
 		harvest(slot); // recorded kRing proposals ago: long complete
 	slot.direct = false;
-	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
+	record(slot.k0);
 
 	if (S_ == 20) {
 		launch20(n, matrices_mode, clock_rate, want_cat, slot);
@@ -453,7 +453,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pt.C = C_;
 	pt.ptab = d_ptab_;
 	check_cuda(launch_ptab4(pt, f32_, stream_), "transition kernel");
-	check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+	record(slot.kmid);
 
 	PruneParams pp{};
 	pp.tips = d_tips_;
@@ -499,9 +499,9 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	} else {
 		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
 	}
-	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
-	slot.pending = true;
-	++ring_next_;
+	record(slot.k1);
+	slot.pending = timing_;
+	ring_next_ += timing_ ? 1 : 0;
 	check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read lnl");
@@ -528,7 +528,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 	pt.ptab = d_ptab_;
 	if (use_tc20_) {
 		check_cuda(launch_ptab20tc(pt, d_tc_tab_, stream_), "transition kernel");
-		check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+		record(slot.kmid);
 		Tc20Params tp{};
 		tp.tips = d_tips_;
 		tp.partials = static_cast<float *>(d_partials_);
@@ -556,9 +556,9 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		tp.tips_smem = (size_t)L_ * 128u <= 32u * 1024u ? 1u : 0u;
 		tp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 		check_cuda(launch_prune20tc(tp, stream_), "tensor-core pruning kernel");
-		check_cuda(cudaEventRecord(slot.k1, stream_), "event");
-		slot.pending = true;
-		++ring_next_;
+		record(slot.k1);
+		slot.pending = timing_;
+		ring_next_ += timing_ ? 1 : 0;
 		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
 					   cudaMemcpyDeviceToHost, stream_),
 			   "read lnl");
@@ -571,7 +571,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		return;
 	}
 	check_cuda(launch_ptab20(pt, f32_, stream_), "transition kernel");
-	check_cuda(cudaEventRecord(slot.kmid, stream_), "event");
+	record(slot.kmid);
 	PruneParams pp{};
 	pp.tips = d_tips_;
 	pp.partials = d_partials_;
@@ -594,9 +594,9 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 	check_cuda(launch_prune20(pp, f32_, stream_), "pruning kernel");
-	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
-	slot.pending = true;
-	++ring_next_;
+	record(slot.k1);
+	slot.pending = timing_;
+	ring_next_ += timing_ ? 1 : 0;
 	check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read lnl");
@@ -638,12 +638,12 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	if (slot.pending)
 		harvest(slot);
 	slot.direct = true;
-	check_cuda(cudaEventRecord(slot.k0, stream_), "event");
+	record(slot.k0);
 	const uint32_t ctas = std::min(ldp_ / 128u, 2 * num_sms_);
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
-	check_cuda(cudaEventRecord(slot.k1, stream_), "event");
-	slot.pending = true;
-	++ring_next_;
+	record(slot.k1);
+	slot.pending = timing_;
+	ring_next_ += timing_ ? 1 : 0;
 	have_result_ = true;
 	stream_dirty_ = true;
 	cat_valid_ = false;
@@ -778,6 +778,12 @@ void Calculator::site_log_likelihoods(double *out)
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 }
 
+void Calculator::record(cudaEvent_t e)
+{
+	if (timing_)
+		check_cuda(cudaEventRecord(e, stream_), "event");
+}
+
 void Calculator::harvest(TimingSlot &s)
 {
 	check_cuda(cudaEventSynchronize(s.k1), "timing sync");
@@ -853,6 +859,13 @@ uint32_t Calculator::autotune(const uint32_t *internals,
 	DeviceGuard g(device_);
 	if (!f32_)
 		return 0;
+	const bool timing = timing_;
+	timing_ = true; // the trials read the kernel timings
+	struct Restore {
+		bool &flag;
+		bool value;
+		~Restore() { flag = value; }
+	} restore{timing_, timing};
 	// best of three timed evaluations after one warm-up, each rejected
 	auto trial = [&]() {
 		float best = INFINITY;

@@ -127,6 +127,16 @@ class Calculator {
 	double acc_transition_ms_ = 0.0, acc_prune_ms_ = 0.0;
 	uint64_t acc_count_ = 0;
 	void harvest(TimingSlot &s);
+	void record(cudaEvent_t e); // a timing event, when timing is on
+	bool timing_ = true;
+
+      public:
+	// Per-proposal device timing (events around the kernels).  On by
+	// default; a driver that never reads it turns it off to save the
+	// event calls on every launch.
+	void set_timing(bool on) { timing_ = on; }
+
+      private:
 
 	// device buffers
 	uint8_t *d_tips_ = nullptr;

@@ -111,6 +111,7 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 			throw Error(B3G_ERR_INVALID_ARGUMENT, e.what());
 		}
 		ch->calc = std::make_unique<Calculator>(cc, samples);
+		ch->calc->set_timing(false); // the driver reads no kernel timings
 		ch->calc->set_weights(weights);
 		ch->beta = 1.0 / (1.0 + cfg.heat * i);
 		ch->index = i;
