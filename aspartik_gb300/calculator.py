@@ -278,4 +278,48 @@ class Batch:
         return ms.value
 
 
-__all__ = ["Calculator", "GpuCalculator", "Batch", "B3GError"]
+class Hetero:
+    """Per-pattern class mixture over calculators (``HeteroLikelihood``,
+    likelihood/hetero.rs:97-168): class k is member k (its own model and
+    clock), pattern p counts under class c(p).  Members must be evaluated and
+    accepted before the mixture is built; per step propose the changed
+    members and/or ``set_classes``, then ``log_likelihood`` and exactly one of
+    ``accept`` / ``reject``."""
+
+    def __init__(self, members: list):
+        self.members = list(members)
+        arr = (ct.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        h = ct.c_void_p()
+        check(lib.b3g_hetero_create(arr, len(self.members), ct.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.b3g_hetero_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_classes(self, classes) -> None:
+        c = nat.u32(classes)
+        if c.size != self.members[0].num_patterns():
+            raise ValueError("one class per pattern")
+        check(lib.b3g_hetero_set_classes(self._h, nat.as_ptr(c, ct.c_uint32)))
+
+    def log_likelihood(self) -> float:
+        out = ct.c_double()
+        check(lib.b3g_hetero_log_likelihood(self._h, ct.byref(out)))
+        return out.value
+
+    def accept(self) -> None:
+        check(lib.b3g_hetero_accept(self._h))
+
+    def reject(self) -> None:
+        check(lib.b3g_hetero_reject(self._h))
+
+
+__all__ = ["Calculator", "GpuCalculator", "Batch", "Hetero", "B3GError"]

@@ -506,6 +506,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read lnl");
 	have_result_ = true;
+	outstanding_ = true;
 	stream_dirty_ = true;
 	cat_valid_ = want_cat;
 }
@@ -566,6 +567,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 					   cudaMemcpyDeviceToHost, stream_),
 			   "read status");
 		have_result_ = true;
+		outstanding_ = true;
 		stream_dirty_ = true;
 		cat_valid_ = want_cat;
 		return;
@@ -601,6 +603,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read lnl");
 	have_result_ = true;
+	outstanding_ = true;
 	stream_dirty_ = true;
 	cat_valid_ = want_cat;
 }
@@ -645,6 +648,7 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	slot.pending = timing_;
 	ring_next_ += timing_ ? 1 : 0;
 	have_result_ = true;
+	outstanding_ = true;
 	stream_dirty_ = true;
 	cat_valid_ = false;
 }
@@ -912,6 +916,7 @@ uint32_t Calculator::autotune(const uint32_t *internals,
 
 void Calculator::accept()
 {
+	outstanding_ = false;
 	// Cpu4Calculator::accept (cpu4.rs:78-83): EditBuf::accept
 	for (auto &m : selectors_)
 		m &= 1u;
@@ -919,6 +924,7 @@ void Calculator::accept()
 
 void Calculator::reject()
 {
+	outstanding_ = false;
 	// Cpu4Calculator::reject (cpu4.rs:85-89): EditBuf::reject
 	for (auto &m : selectors_)
 		m = static_cast<uint8_t>((m ^ (m >> 1)) & 1u);

@@ -77,6 +77,7 @@ class Calculator {
 	void stage_lengths(const uint32_t *internals, const uint32_t *children,
 			   uint32_t n, const double *lengths, double clock_rate);
 	friend class Batch;
+	friend class Hetero;
 
       private:
 	void validate_lists(const uint32_t *internals,
@@ -107,6 +108,7 @@ class Calculator {
 	uint32_t tip_children_ = 0;      // tip children in the staged list
 	bool model_set_ = false;
 	bool have_result_ = false;
+	bool outstanding_ = false; // evaluated since the last accept/reject
 	bool cat_valid_ = false;
 	ModelDev model_host_{};
 

@@ -1,5 +1,7 @@
 // mcmc.cpp -- native MCMC driver (see mcmc.hpp).
 #include "mcmc.hpp"
+
+#include <cstdlib>
 #include "host_math.hpp"
 
 #include <algorithm>
@@ -123,9 +125,14 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		chains_.push_back(std::move(ch));
 	}
 	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
-	// several FP32 chains share one batched launch per step; a single
-	// chain launches its own (short lists take the fused one-kernel path)
-	if (cfg.precision == B3G_PRECISION_F32 && chains_.size() > 1) {
+	// several FP32 chains can share one batched launch per step
+	// (B3G_MCMC_BATCH=1); by default every chain launches its own
+	// evaluations on its own stream (short lists take the fused
+	// one-kernel path) and the launches of a step run concurrently
+	bool use_batch = false;
+	if (const char *env = std::getenv("B3G_MCMC_BATCH"))
+		use_batch = std::atoi(env) != 0;
+	if (cfg.precision == B3G_PRECISION_F32 && chains_.size() > 1 && use_batch) {
 		std::vector<Calculator *> calcs;
 		for (auto &ch : chains_)
 			calcs.push_back(ch->calc.get());

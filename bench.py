@@ -445,6 +445,37 @@ def mcmc_ess(wl, steps: int, device: int) -> dict:
     return out
 
 
+def mc3(wl, steps: int, device: int, chains: int = 8) -> dict:
+    """Metropolis-coupled MCMC on the workload: `chains` FP32 chains at
+    beta_i = 1 / (1 + 0.1 i), swap attempts every 10 steps, the moves of
+    mcmc_ess; every step stages all chains' proposals and evaluates them with
+    one CUDA-graph replay of the batched kernels."""
+    from aspartik_gb300.ess import min_ess
+    from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
+
+    s = McmcSettings(model="gtr", precision="f32", num_categories=wl["spec"]["categories"],
+                     num_chains=chains, heat=0.1, swap_every=10, seed=4, sample_every=10,
+                     weights=dict(GTR_WEIGHTS), device=device)
+    m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
+    m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
+                     alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
+    m.run(min(200, steps))  # warm-up (operator tuning, first graph replays)
+    t0 = time.perf_counter()
+    m.run(steps)
+    dt = time.perf_counter() - t0
+    tried, accepted = m.swaps()
+    keep = (steps // 10) // 5
+    traces = {k: m.trace(k)[keep:] for k in ("lnl", "root_height", "kappa_or_rate0")}
+    e, _ = min_ess(traces, burn_in=0.0)
+    out = {"chains": chains, "steps": steps, "seconds": round(dt, 3),
+           "us_per_step": round(dt / steps * 1e6, 2),
+           "chain_steps_per_s": round(chains * steps / dt, 1),
+           "swaps_tried": tried, "swaps_accepted": accepted,
+           "cold_chain_ess_min": round(e, 2), "check_rel": m.check()}
+    m.close()
+    return out
+
+
 def run_ours(args):
     world, rank, local = dist_setup()
     device = local
@@ -512,6 +543,7 @@ def run_ours(args):
     c64.close()
 
     mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
+    mc3_out = None if args.mcmc_steps <= 0 else mc3(wl, max(1000, args.mcmc_steps // 4), device)
     prot = prot_big = None
     if not args.no_protein:
         prot = protein20(device, min(args.steps, 100), args.warmup)
@@ -575,6 +607,7 @@ def run_ours(args):
                        "mean_nodes": mean_path,
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
+        "mc3": mc3_out,
         "batched": batch,
         "protein20": prot,
         "protein20_large": prot_big,

@@ -237,6 +237,30 @@ B3G_API b3g_status b3g_batch_log_likelihoods(b3g_batch *batch, double *out);
 /* Device time of the last replay (events inside the graph), ms. */
 B3G_API b3g_status b3g_batch_last_ms(b3g_batch *batch, float *ms);
 
+/* ---- per-pattern class mixture ---------------------------------------------
+ * Replaces HeteroLikelihood (crates/b3/src/likelihood/hetero.rs:97-168): K
+ * classes, each a calculator over the same patterns with its own substitution
+ * model and clock (the caller proposes each member with its own edge lengths
+ * and model); pattern p belongs to class c(p) and the log-likelihood is
+ * sum_p w_p lnL_{c(p)}(p), weights taken from the first member.  Members
+ * must be evaluated and accepted before the mixture is built.  Per step:
+ * propose the members whose tree, model or clock changed and/or
+ * b3g_hetero_set_classes, then b3g_hetero_log_likelihood, then exactly one
+ * of b3g_hetero_accept / _reject (which accept or reject the evaluated
+ * members too).  A member not evaluated in the step contributes its accepted
+ * per-pattern values, so a step that changes only the classes prunes
+ * nothing.  At most 16 classes. */
+typedef struct b3g_hetero b3g_hetero;
+B3G_API b3g_status b3g_hetero_create(b3g_calculator *const *members,
+				     uint32_t count, b3g_hetero **out);
+B3G_API void b3g_hetero_destroy(b3g_hetero *h);
+/* classes[num_patterns], each < count. */
+B3G_API b3g_status b3g_hetero_set_classes(b3g_hetero *h,
+					  const uint32_t *classes);
+B3G_API b3g_status b3g_hetero_log_likelihood(b3g_hetero *h, double *out);
+B3G_API b3g_status b3g_hetero_accept(b3g_hetero *h);
+B3G_API b3g_status b3g_hetero_reject(b3g_hetero *h);
+
 /* ---- native MCMC driver ---------------------------------------------------
  * The caller side of the path: b3's MCMC step (crates/b3/src/mcmc.rs:
  * 314-393) in C++ -- operator proposal, prior (reject at -inf before any
