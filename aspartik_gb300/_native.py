@@ -133,6 +133,8 @@ SIGNATURES = {
     "b3g_calculator_propose_lengths": (
         ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
     "b3g_calculator_log_likelihood": (ct.c_int, [_vp, _f64p]),
+    "b3g_deduplicate": (ct.c_int, [_u8p, ct.c_uint32, ct.c_uint32, ct.c_int, ct.c_int32,
+                                   _u8p, _u32p, _u32p, _u32p, _f32p]),
     "b3g_hetero_create": (ct.c_int, [ct.POINTER(_vp), ct.c_uint32, ct.POINTER(_vp)]),
     "b3g_hetero_destroy": (None, [_vp]),
     "b3g_hetero_set_classes": (ct.c_int, [_vp, _u32p]),

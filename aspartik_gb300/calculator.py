@@ -278,6 +278,24 @@ class Batch:
         return ms.value
 
 
+def deduplicate(msa: np.ndarray, dna: bool = True, device: int = 0):
+    """Site-pattern compression on the GPU (``deduplicate``,
+    likelihood/mod.rs:74-132): returns (leaves [L][P], weights [P],
+    site_to_pattern [N], device milliseconds)."""
+    msa = np.ascontiguousarray(msa, dtype=np.uint8)
+    L, N = msa.shape
+    leaves = np.empty(L * N, dtype=np.uint8)
+    weights = np.empty(N, dtype=np.uint32)
+    s2p = np.empty(N, dtype=np.uint32)
+    P = ct.c_uint32()
+    ms = ct.c_float()
+    check(lib.b3g_deduplicate(nat.as_ptr(msa, ct.c_uint8), L, N, int(bool(dna)), int(device),
+                              nat.as_ptr(leaves, ct.c_uint8), nat.as_ptr(weights, ct.c_uint32),
+                              nat.as_ptr(s2p, ct.c_uint32), ct.byref(P), ct.byref(ms)))
+    p = P.value
+    return leaves[: L * p].reshape(L, p).copy(), weights[:p].copy(), s2p, ms.value
+
+
 class Hetero:
     """Per-pattern class mixture over calculators (``HeteroLikelihood``,
     likelihood/hetero.rs:97-168): class k is member k (its own model and
@@ -322,4 +340,4 @@ class Hetero:
         check(lib.b3g_hetero_reject(self._h))
 
 
-__all__ = ["Calculator", "GpuCalculator", "Batch", "Hetero", "B3GError"]
+__all__ = ["Calculator", "GpuCalculator", "Batch", "Hetero", "deduplicate", "B3GError"]

@@ -445,6 +445,37 @@ def mcmc_ess(wl, steps: int, device: int) -> dict:
     return out
 
 
+def dedup_leg(device: int, seed: int = 4) -> dict:
+    """Site-pattern compression of the largest batched configuration's
+    alignment size (200 taxa x 50,000 sites, simulated under GTR) on the
+    GPU; CPU baseline: the restated deduplicate (hash map, one thread)."""
+    from aspartik_gb300.calculator import deduplicate
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(seed)
+    tree = sim.yule_tree(200, rng, root_height=0.5)
+    pi = sim.dirichlet([5.0] * 4, rng)
+    Q = sim.reversible_q(rng.gamma(2.0, 1.0, 6), pi)
+    msa = sim.to_dna_codes(sim.simulate_alignment(tree, 50000, Q, pi, rng))
+    deduplicate(msa, device=device)  # warm-up
+    dev, wall = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        leaves, weights, s2p, ms = deduplicate(msa, device=device)
+        wall.append(time.perf_counter() - t0)
+        dev.append(ms)
+    t0 = time.perf_counter()
+    ol, ow, os_ = O.deduplicate(msa)
+    t_cpu = time.perf_counter() - t0
+    same = bool(np.array_equal(leaves, ol) and np.array_equal(weights, ow)
+                and np.array_equal(s2p, os_))
+    return {"taxa": 200, "sites": 50000, "patterns": int(weights.size),
+            "device_ms": round(statistics.median(dev), 4),
+            "e2e_ms": round(statistics.median(wall) * 1e3, 4),
+            "alignment_GB_s": round(msa.nbytes / (statistics.median(dev) * 1e-3) / 1e9, 2),
+            "cpu_baseline_ms": round(t_cpu * 1e3, 3), "identical_to_cpu": same}
+
+
 def mc3(wl, steps: int, device: int, chains: int = 8) -> dict:
     """Metropolis-coupled MCMC on the workload: `chains` FP32 chains at
     beta_i = 1 / (1 + 0.1 i), swap attempts every 10 steps, the moves of
@@ -544,6 +575,7 @@ def run_ours(args):
 
     mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
     mc3_out = None if args.mcmc_steps <= 0 else mc3(wl, max(1000, args.mcmc_steps // 4), device)
+    dedup = None if args.no_cpu else dedup_leg(device)
     prot = prot_big = None
     if not args.no_protein:
         prot = protein20(device, min(args.steps, 100), args.warmup)
@@ -608,6 +640,7 @@ def run_ours(args):
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
         "mc3": mc3_out,
+        "dedup": dedup,
         "batched": batch,
         "protein20": prot,
         "protein20_large": prot_big,

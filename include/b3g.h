@@ -237,6 +237,22 @@ B3G_API b3g_status b3g_batch_log_likelihoods(b3g_batch *batch, double *out);
 /* Device time of the last replay (events inside the graph), ms. */
 B3G_API b3g_status b3g_batch_last_ms(b3g_batch *batch, float *ms);
 
+/* ---- site-pattern compression on the device ---------------------------------
+ * Replaces deduplicate (crates/b3/src/likelihood/mod.rs:74-132) for large
+ * alignments: msa is [num_sequences][num_sites] (row per sequence, host
+ * memory); the unique columns in first-occurrence order go to
+ * leaves[num_sequences][*num_patterns] (capacity num_sequences * num_sites),
+ * their site counts to weights (capacity num_sites) and every site's pattern
+ * to site_to_pattern[num_sites].  dna_gaps != 0 maps code 0 (gap) to 0b1111
+ * as the reference does for DNA; 0 keeps codes (protein state indices).
+ * device_ms (may be NULL) receives the device time of the compression.
+ * Allocates and frees its own device memory (ingest time, not per step). */
+B3G_API b3g_status b3g_deduplicate(const uint8_t *msa, uint32_t num_sequences,
+				   uint32_t num_sites, int dna_gaps,
+				   int32_t device, uint8_t *leaves,
+				   uint32_t *weights, uint32_t *site_to_pattern,
+				   uint32_t *num_patterns, float *device_ms);
+
 /* ---- per-pattern class mixture ---------------------------------------------
  * Replaces HeteroLikelihood (crates/b3/src/likelihood/hetero.rs:97-168): K
  * classes, each a calculator over the same patterns with its own substitution
