@@ -79,7 +79,7 @@ class PruneBuffers(ct.Structure):
     ]
 
 
-OP_COUNT = 8
+OP_COUNT = 10
 
 
 class McmcConfig(ct.Structure):
@@ -102,6 +102,8 @@ class McmcConfig(ct.Structure):
         ("da_hidden", ct.c_uint32),
         ("da_reserved", ct.c_uint32),
         ("da_drift_limit", ct.c_double),
+        ("clock_categories", ct.c_uint32),
+        ("clock_reserved", ct.c_uint32),
     ]
 
 
@@ -133,6 +135,8 @@ SIGNATURES = {
     "b3g_calculator_propose_lengths": (
         ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
     "b3g_calculator_log_likelihood": (ct.c_int, [_vp, _f64p]),
+    "b3g_mcmc_set_clock": (ct.c_int, [_vp, ct.c_double, _u32p]),
+    "b3g_lognormal_categories": (ct.c_int, [ct.c_double, ct.c_uint32, _f64p]),
     "b3g_deduplicate": (ct.c_int, [_u8p, ct.c_uint32, ct.c_uint32, ct.c_int, ct.c_int32,
                                    _u8p, _u32p, _u32p, _u32p, _f32p]),
     "b3g_hetero_create": (ct.c_int, [ct.POINTER(_vp), ct.c_uint32, ct.POINTER(_vp)]),

@@ -11,6 +11,7 @@
 // inverts it by Newton steps on log x kept inside a shrinking bracket.
 #include "host_math.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <limits>
 
@@ -160,6 +161,49 @@ void gamma_categories(double alpha, int k, double *rates)
 		rates[i] = rates[i] / mean;
 }
 
+
+// Standard normal quantile: bisection-safeguarded Newton steps on
+// Phi(x) = erfc(-x / sqrt 2) / 2 from a logistic start, on the lower half
+// (Phi^-1(q) = -Phi^-1(1 - q) above 1/2, so the residual never cancels).
+double normal_quantile(double q)
+{
+	if (!(q > 0.0))
+		return -std::numeric_limits<double>::infinity();
+	if (!(q < 1.0))
+		return std::numeric_limits<double>::infinity();
+	if (q > 0.5)
+		return -normal_quantile(1.0 - q);
+	if (q == 0.5)
+		return 0.0;
+	const double pi = 3.14159265358979323846;
+	double lo = -40.0, hi = 0.0;
+	double x = std::max(lo, std::sqrt(pi / 8.0) * std::log(q / (1.0 - q)));
+	for (int it = 0; it < 200; ++it) {
+		const double cdf = 0.5 * std::erfc(-x / std::sqrt(2.0));
+		if (cdf < q)
+			lo = x;
+		else
+			hi = x;
+		const double pdf = std::exp(-0.5 * x * x) / std::sqrt(2.0 * pi);
+		double next = x - (cdf - q) / pdf;
+		if (!(next > lo && next < hi) || pdf == 0.0)
+			next = 0.5 * (lo + hi);
+		if (std::fabs(next - x) <= 1e-15 * std::max(1.0, std::fabs(x)))
+			return next;
+		x = next;
+	}
+	return x;
+}
+
+// Relaxed-clock rates (RelaxedClock::update_rates, crates/b3/src/clock.rs:
+// 66-84): the quantiles at (i + 1/2) / k of a LogNormal with mean one and
+// log-scale standard deviation sd (mu = -sd^2 / 2).
+void lognormal_categories(double sd, int k, double *rates)
+{
+	const double mu = -0.5 * sd * sd;
+	for (int i = 0; i < k; ++i)
+		rates[i] = std::exp(mu + sd * normal_quantile((i + 0.5) / k));
+}
 
 // Reversible Q from exchangeabilities and frequencies, normalised to mean
 // rate 1 (GTR::update_matrices, crates/b3/src/substitution.rs:502-555), and

@@ -14,6 +14,13 @@ void gamma_categories(double alpha, int k, double *rates);
 void hky_eigen(double kappa, const double *pi, double *V, double *Vinv,
 	       double *lambda, double *Q);
 
+// Standard normal quantile (host, double precision).
+double normal_quantile(double q);
+// Median rates of k equal-probability categories of a mean-one LogNormal
+// with log-scale standard deviation sd (relaxed clock,
+// crates/b3/src/clock.rs:66-84).
+void lognormal_categories(double sd, int k, double *rates);
+
 constexpr int kHostMaxStates = 20;
 // Reversible model of n <= kHostMaxStates states from upper-triangle
 // exchangeabilities and frequencies: normalised Q and its eigensystem, all

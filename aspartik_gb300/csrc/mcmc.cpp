@@ -122,6 +122,13 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		ch->birth_rate.v = 1.0;
 		ch->rates.v.assign(6, 1.0);
 		ch->freqs.v.assign(4, 0.25);
+		if (cfg.clock_categories) {
+			ch->edge_cat.resize(2 * L - 1);
+			for (uint32_t v = 0; v < 2 * L - 1; ++v)
+				ch->edge_cat[v] = v % cfg.clock_categories;
+			ch->clock_sd.v = 0.3;
+			clock_rates(*ch);
+		}
 		chains_.push_back(std::move(ch));
 	}
 	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
@@ -171,7 +178,7 @@ void Mcmc::set_parameters(double kappa, const double *rates,
 		if (cfg_.num_categories > 1)
 			ch.calc->set_gamma(alpha);
 		// DnaLikelihood::new: mark all, evaluate, accept (dna.rs:34-66)
-		ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+		lists(ch);
 		ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
 					 (uint32_t)ch.internals.size(),
 					 ch.lengths.data(), 1.0);
@@ -218,7 +225,51 @@ double Mcmc::prior(const Chain &ch) const
 	out += sym_dirichlet_lnpdf(ch.freqs.v, 1.0);
 	if (cfg_.num_categories > 1)
 		out += lognormal_lnpdf(ch.alpha.v, 0.0, 1.0);
+	if (cfg_.clock_categories) {
+		// relaxed-clock sd ~ Exponential(mean 1/3); categories uniform
+		const double sd = ch.clock_sd.v;
+		out += sd > 0.0 ? std::log(3.0) - 3.0 * sd : kNegInf;
+	}
 	return std::isnan(out) ? kNegInf : out;
+}
+
+void Mcmc::clock_rates(Chain &ch)
+{
+	ch.clock_rates.resize(cfg_.clock_categories);
+	lognormal_categories(ch.clock_sd.v, (int)cfg_.clock_categories,
+			     ch.clock_rates.data());
+}
+
+void Mcmc::lists(Chain &ch)
+{
+	ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+	if (!cfg_.clock_categories)
+		return;
+	// RelaxedClock::get_rate (clock.rs:118-122): edge id = child node
+	for (size_t k = 0; k < ch.lengths.size(); ++k)
+		ch.lengths[k] *= ch.clock_rates[ch.edge_cat[ch.children[k]]];
+}
+
+void Mcmc::set_clock(double sd, const uint32_t *categories)
+{
+	const uint32_t K = cfg_.clock_categories;
+	if (!K)
+		throw Error(B3G_ERR_STATE, "the chains use a strict clock");
+	if (!(sd > 0.0) || !std::isfinite(sd))
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "clock sd must be finite and > 0");
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		const uint32_t nodes = ch.tree->num_nodes();
+		for (uint32_t v = 0; v < nodes; ++v) {
+			const uint32_t c = categories ? categories[v] : v % K;
+			if (c >= K && v != ch.tree->root())
+				throw Error(B3G_ERR_INVALID_ARGUMENT,
+					    "clock category out of range");
+			ch.edge_cat[v] = c < K ? c : 0;
+		}
+		ch.clock_sd.v = sd;
+		clock_rates(ch);
+	}
 }
 
 namespace {
@@ -393,6 +444,35 @@ void Mcmc::propose(Chain &ch)
 		ch.local = true;
 		break;
 	}
+	case kOpRelaxedCategory: { // one edge's class (clock.rs:107-112)
+		const uint32_t K = cfg_.clock_categories;
+		if (K < 2) {
+			ch.status = 1;
+			break;
+		}
+		const uint32_t e = random_nonroot(t, ch.rng);
+		uint32_t c = ch.rng.below(K - 1);
+		if (c >= ch.edge_cat[e])
+			++c;
+		ch.cat_edge = e;
+		ch.cat_old = ch.edge_cat[e];
+		ch.edge_cat[e] = c;
+		ch.cat_changed = true;
+		t.mark_edge_updated(e);
+		break;
+	}
+	case kOpScaleClockSd: { // ScaleReal on the sd; every rate changes
+		if (!cfg_.clock_categories) {
+			ch.status = 1;
+			break;
+		}
+		const double s = scale_factor();
+		ch.clock_sd.set(ch.clock_sd.v * s);
+		ch.hastings = -std::log(s);
+		clock_rates(ch);
+		t.mark_all_edges_updated();
+		break;
+	}
 	default:
 		ch.status = 1;
 	}
@@ -418,7 +498,7 @@ void Mcmc::launch(Chain &ch)
 		ch.lnl_new = ch.lnl_cache;
 		return;
 	}
-	ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+	lists(ch);
 	if (batch_)
 		ch.calc->stage_lengths(ch.internals.data(), ch.children.data(),
 				       (uint32_t)ch.internals.size(),
@@ -585,6 +665,8 @@ void Mcmc::finish(Chain &ch)
 		ch.birth_rate.accept();
 		ch.rates.accept();
 		ch.freqs.accept();
+		ch.clock_sd.accept();
+		ch.cat_changed = false;
 		if (ch.launched)
 			ch.calc->accept();
 		ch.lnl_cache = ch.lnl_new;
@@ -602,6 +684,14 @@ void Mcmc::finish(Chain &ch)
 		ch.birth_rate.reject();
 		ch.rates.reject();
 		ch.freqs.reject();
+		if (ch.clock_sd.changed) {
+			ch.clock_sd.reject();
+			clock_rates(ch);
+		}
+		if (ch.cat_changed) {
+			ch.edge_cat[ch.cat_edge] = ch.cat_old;
+			ch.cat_changed = false;
+		}
 		if (ch.launched)
 			ch.calc->reject();
 		if (restore_model)
@@ -677,6 +767,7 @@ void Mcmc::record()
 	trace_[4].push_back(cfg_.model == 0 ? cold->kappa.v : cold->rates.v[0]);
 	trace_[5].push_back(cold->alpha.v);
 	trace_[6].push_back(length);
+	trace_[7].push_back(cfg_.clock_categories ? cold->clock_sd.v : 0.0);
 }
 
 void Mcmc::run(uint64_t steps)
@@ -724,7 +815,7 @@ double Mcmc::check_full_recompute()
 	for (auto &chp : chains_) {
 		Chain &ch = *chp;
 		ch.tree->mark_all_edges_updated();
-		ch.tree->partials_lists(ch.internals, ch.children, ch.lengths);
+		lists(ch);
 		ch.calc->propose_lengths(ch.internals.data(), ch.children.data(),
 					 (uint32_t)ch.internals.size(),
 					 ch.lengths.data(), 1.0);

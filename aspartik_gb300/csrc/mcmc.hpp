@@ -84,6 +84,8 @@ enum OpKind : uint32_t {
 	kOpScaleBirthRate,
 	kOpDeltaRates,
 	kOpDeltaFreqs,
+	kOpRelaxedCategory, // one edge's relaxed-clock category
+	kOpScaleClockSd,    // the relaxed clock's LogNormal sd
 	kOpCount
 };
 
@@ -110,6 +112,7 @@ struct McmcConfig {
 	uint32_t da_epochs;
 	uint32_t da_hidden;
 	double da_drift_limit;
+	uint32_t clock_categories; // 0: strict clock
 };
 
 // Inputs of the surrogate: 5 branch lengths around the node a tree move
@@ -130,6 +133,13 @@ struct Chain {
 	Rng rng;
 	Real kappa, alpha, birth_rate;
 	RealVec rates, freqs;
+	// relaxed clock: category of every edge (by child node), LogNormal sd
+	// and the category rates it gives
+	std::vector<uint32_t> edge_cat;
+	bool cat_changed = false;
+	uint32_t cat_edge = 0, cat_old = 0; // the proposal's change
+	Real clock_sd;
+	std::vector<double> clock_rates;
 	double beta = 1.0;
 	uint32_t index = 0;
 	double lnl_cache = 0.0, lnl_new = 0.0;
@@ -156,6 +166,7 @@ class Mcmc {
 	     const uint8_t *samples, const uint32_t *weights,
 	     const uint32_t *parents, const double *heights);
 
+	void set_clock(double sd, const uint32_t *categories);
 	void set_parameters(double kappa, const double *rates,
 			    const double *freqs, double alpha,
 			    double birth_rate);
@@ -180,6 +191,10 @@ class Mcmc {
 
       private:
 	void propose(Chain &ch);
+	// the tree's dirty lists with the per-edge lengths (relaxed clock:
+	// times the edge's category rate)
+	void lists(Chain &ch);
+	void clock_rates(Chain &ch);
 	double prior(const Chain &ch) const;
 	void sync_model(Chain &ch);
 	void launch(Chain &ch);
@@ -204,7 +219,7 @@ class Mcmc {
 	uint64_t swaps_tried_ = 0, swaps_accepted_ = 0;
 	uint32_t tune_rounds_ = 0;
 	Rng swap_rng_;
-	std::vector<double> trace_[7];
+	std::vector<double> trace_[8];
 
 	// delayed acceptance: pilot pairs, the trained surrogate, input and
 	// output normalisation, the drift window of (exact - surrogate)

@@ -1,4 +1,6 @@
 // mcmc_abi.cpp -- C ABI of the native MCMC driver (include/b3g.h).
+#include "host_math.hpp"
+#include <cmath>
 #include "mcmc.hpp"
 
 #include <algorithm>
@@ -78,6 +80,12 @@ B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
 		c.da_epochs = config->da_epochs;
 		c.da_hidden = config->da_hidden;
 		c.da_drift_limit = config->da_drift_limit;
+		if (config->clock_reserved != 0)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "clock_reserved must be 0");
+		if (config->clock_categories > 64)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "at most 64 relaxed-clock categories");
+		c.clock_categories = config->clock_categories;
 		auto *m = new b3g::Mcmc(c, num_leaves, num_patterns, samples,
 					weights, parents, heights);
 		*out = reinterpret_cast<b3g_mcmc *>(m);
@@ -100,6 +108,22 @@ B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
 	});
 }
 
+B3G_API b3g_status b3g_mcmc_set_clock(b3g_mcmc *mcmc, double sd,
+				      const uint32_t *categories)
+{
+	return guarded([&] { mcmc_of(mcmc)->set_clock(sd, categories); });
+}
+
+B3G_API b3g_status b3g_lognormal_categories(double sd, uint32_t k, double *rates)
+{
+	return guarded([&] {
+		if (!rates || k < 1 || !(sd > 0.0) || !std::isfinite(sd))
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "need sd > 0, k >= 1 and an output");
+		b3g::lognormal_categories(sd, (int)k, rates);
+	});
+}
+
 B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps)
 {
 	return guarded([&] { mcmc_of(mcmc)->run(steps); });
@@ -110,7 +134,7 @@ B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
 				  uint64_t *count)
 {
 	return guarded([&] {
-		if (field > 6 || !count)
+		if (field > 7 || !count)
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "bad trace field");
 		const auto &t = mcmc_of(mcmc)->trace(field);
 		*count = t.size();

@@ -17,9 +17,10 @@ from ._native import check, lib
 
 MODELS = {"hky": 0, "gtr": 1}
 OPERATORS = ["tree_scale", "subtree_slide", "narrow_exchange", "scale_kappa",
-             "scale_alpha", "scale_birth_rate", "delta_rates", "delta_frequencies"]
+             "scale_alpha", "scale_birth_rate", "delta_rates", "delta_frequencies",
+             "relaxed_category", "scale_clock_sd"]
 TRACE_FIELDS = ["lnl", "prior", "posterior", "root_height", "kappa_or_rate0", "alpha",
-                "tree_length"]
+                "tree_length", "clock_sd"]
 
 # the operator mix of the reference's config recipe for a Yule + GTR model
 # (python/aspartik/b3/config/__init__.py:660-730, 853-858)
@@ -47,6 +48,8 @@ class McmcSettings:
     da_epochs: int = 20
     da_hidden: int = 256
     da_drift_limit: float = 0.0
+    # relaxed clock: rate categories per edge (0: strict clock)
+    clock_categories: int = 0
 
 
 class Mcmc:
@@ -64,7 +67,7 @@ class Mcmc:
                              settings.swap_every, settings.sample_every, settings.tune_every,
                              settings.device, (ct.c_double * nat.OP_COUNT)(*w),
                              settings.da_pilot_steps, settings.da_epochs, settings.da_hidden,
-                             0, settings.da_drift_limit)
+                             0, settings.da_drift_limit, settings.clock_categories, 0)
         self._wts = nat.u32(weights)
         self._par = nat.u32(parents)
         self._hei = nat.f64(heights)
@@ -96,6 +99,14 @@ class Mcmc:
             self._h, float(kappa), None if r is None else nat.as_ptr(r, ct.c_double),
             None if f is None else nat.as_ptr(f, ct.c_double), float(alpha),
             float(birth_rate)))
+
+    def set_clock(self, sd: float, categories=None):
+        """Relaxed-clock start state (before ``set_parameters``): the LogNormal
+        sd and one category per node (its parent edge; the root's is
+        ignored), or None for node % k."""
+        c = None if categories is None else nat.u32(categories)
+        check(lib.b3g_mcmc_set_clock(self._h, float(sd),
+                                     None if c is None else nat.as_ptr(c, ct.c_uint32)))
 
     def run(self, steps: int):
         check(lib.b3g_mcmc_run(self._h, int(steps)))

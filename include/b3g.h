@@ -237,6 +237,11 @@ B3G_API b3g_status b3g_batch_log_likelihoods(b3g_batch *batch, double *out);
 /* Device time of the last replay (events inside the graph), ms. */
 B3G_API b3g_status b3g_batch_last_ms(b3g_batch *batch, float *ms);
 
+/* Rates of k relaxed-clock categories: quantiles (i + 1/2) / k of a
+ * mean-one LogNormal with log-scale sd (clock.rs:66-84). */
+B3G_API b3g_status b3g_lognormal_categories(double sd, uint32_t k,
+					    double *rates);
+
 /* ---- site-pattern compression on the device ---------------------------------
  * Replaces deduplicate (crates/b3/src/likelihood/mod.rs:74-132) for large
  * alignments: msa is [num_sequences][num_sites] (row per sequence, host
@@ -302,7 +307,9 @@ enum {
 	B3G_OP_SCALE_BIRTH_RATE = 5,
 	B3G_OP_DELTA_RATES = 6,
 	B3G_OP_DELTA_FREQUENCIES = 7,
-	B3G_OP_COUNT = 8
+	B3G_OP_RELAXED_CATEGORY = 8, /* one edge's relaxed-clock rate category */
+	B3G_OP_SCALE_CLOCK_SD = 9,   /* the relaxed clock's LogNormal sd */
+	B3G_OP_COUNT = 10
 };
 
 /* Trace fields of the cold chain, sampled every sample_every steps. */
@@ -313,7 +320,8 @@ enum {
 	B3G_TRACE_ROOT_HEIGHT = 3,
 	B3G_TRACE_KAPPA_OR_RATE0 = 4,
 	B3G_TRACE_ALPHA = 5,
-	B3G_TRACE_TREE_LENGTH = 6
+	B3G_TRACE_TREE_LENGTH = 6,
+	B3G_TRACE_CLOCK_SD = 7
 };
 
 typedef struct b3g_mcmc_config {
@@ -342,6 +350,13 @@ typedef struct b3g_mcmc_config {
 	uint32_t da_hidden;
 	uint32_t da_reserved; /* must be 0 */
 	double da_drift_limit;
+	/* Relaxed clock (RelaxedClock, crates/b3/src/clock.rs:41-134): 0 =
+	 * strict clock; k > 0 = every edge has one of k rate categories whose
+	 * rates are the median quantiles of a mean-one LogNormal with
+	 * log-scale sd (prior Exponential, mean 1/3).  A category change
+	 * marks only its edge for recomputation, an sd change every edge. */
+	uint32_t clock_categories;
+	uint32_t clock_reserved; /* must be 0 */
 } b3g_mcmc_config;
 
 /* parents[2L-1] (root: 0xFFFFFFFF) and heights[2L-1] give the start tree of
@@ -358,6 +373,11 @@ B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
 					   const double *rates,
 					   const double *frequencies,
 					   double alpha, double birth_rate);
+/* Relaxed clock start state (before b3g_mcmc_set_parameters): sd > 0 and
+ * the category of every edge, categories[2L-1] indexed by the edge's child
+ * node (the root's entry is ignored), or NULL for node % k. */
+B3G_API b3g_status b3g_mcmc_set_clock(b3g_mcmc *mcmc, double sd,
+				      const uint32_t *categories);
 B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps);
 /* Copies up to `capacity` samples of a B3G_TRACE_* field; *count = all. */
 B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
