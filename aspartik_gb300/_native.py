@@ -135,6 +135,8 @@ SIGNATURES = {
     "b3g_calculator_propose_lengths": (
         ct.c_int, [_vp, _u32p, _u32p, ct.c_uint32, _f64p, ct.c_double]),
     "b3g_calculator_log_likelihood": (ct.c_int, [_vp, _f64p]),
+    "b3g_mcmc_samples": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), _u32p, _f64p, _f64p,
+                                    ct.c_uint64, ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_set_clock": (ct.c_int, [_vp, ct.c_double, _u32p]),
     "b3g_lognormal_categories": (ct.c_int, [ct.c_double, ct.c_uint32, _f64p]),
     "b3g_deduplicate": (ct.c_int, [_u8p, ct.c_uint32, ct.c_uint32, ct.c_int, ct.c_int32,

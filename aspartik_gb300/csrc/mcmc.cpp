@@ -768,6 +768,19 @@ void Mcmc::record()
 	trace_[5].push_back(cold->alpha.v);
 	trace_[6].push_back(length);
 	trace_[7].push_back(cfg_.clock_categories ? cold->clock_sd.v : 0.0);
+	// the whole sample for trace files: tree and parameters
+	sample_steps_.push_back(step_);
+	for (uint32_t v = 0; v < t.num_nodes(); ++v) {
+		sample_parents_.push_back(t.parent_of(v));
+		sample_heights_.push_back(t.height(v));
+	}
+	const double p[kSampleParams] = {
+		cold->kappa.v, cold->alpha.v, cold->birth_rate.v,
+		cold->rates.v[0], cold->rates.v[1], cold->rates.v[2],
+		cold->rates.v[3], cold->rates.v[4], cold->rates.v[5],
+		cold->freqs.v[0], cold->freqs.v[1], cold->freqs.v[2],
+		cold->freqs.v[3], cfg_.clock_categories ? cold->clock_sd.v : 0.0};
+	sample_params_.insert(sample_params_.end(), p, p + kSampleParams);
 }
 
 void Mcmc::run(uint64_t steps)

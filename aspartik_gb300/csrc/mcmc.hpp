@@ -121,6 +121,10 @@ struct McmcConfig {
 // or log kappa, three frequencies).
 constexpr uint32_t kDaInputs = 14;
 
+// Parameters of one sample: kappa, alpha, birth rate, 6 exchangeabilities,
+// 4 frequencies, relaxed-clock sd.
+constexpr uint32_t kSampleParams = 14;
+
 struct DaStats {
 	uint64_t pilot_pairs = 0, stage1_rejects = 0, stage2_accepts = 0,
 		 stage2_rejects = 0, exact_evaluations = 0, fallback = 0;
@@ -178,6 +182,13 @@ class Mcmc {
 		return trace_[field];
 	}
 	void op_stats(uint32_t op, uint64_t out[4], double *tuning) const;
+	// samples: steps[n], parents[n][nodes], heights[n][nodes],
+	// parameters[n][kSampleParams]
+	uint64_t num_samples() const { return sample_steps_.size(); }
+	const std::vector<uint64_t> &sample_steps() const { return sample_steps_; }
+	const std::vector<uint32_t> &sample_parents() const { return sample_parents_; }
+	const std::vector<double> &sample_heights() const { return sample_heights_; }
+	const std::vector<double> &sample_params() const { return sample_params_; }
 	const DaStats &da_stats() const { return da_; }
 	uint64_t swaps_accepted() const { return swaps_accepted_; }
 	uint64_t swaps_tried() const { return swaps_tried_; }
@@ -220,6 +231,11 @@ class Mcmc {
 	uint32_t tune_rounds_ = 0;
 	Rng swap_rng_;
 	std::vector<double> trace_[8];
+	// per sample: the step, the cold chain's tree (parents and heights of
+	// every node) and its parameters (kSampleParams values)
+	std::vector<uint64_t> sample_steps_;
+	std::vector<uint32_t> sample_parents_;
+	std::vector<double> sample_heights_, sample_params_;
 
 	// delayed acceptance: pilot pairs, the trained surrogate, input and
 	// output normalisation, the drift window of (exact - surrogate)

@@ -129,6 +129,34 @@ B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps)
 	return guarded([&] { mcmc_of(mcmc)->run(steps); });
 }
 
+B3G_API b3g_status b3g_mcmc_samples(b3g_mcmc *mcmc, uint64_t *steps,
+				    uint32_t *parents, double *heights,
+				    double *parameters, uint64_t capacity,
+				    uint64_t *count)
+{
+	return guarded([&] {
+		if (!count)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null count");
+		const b3g::Mcmc &m = *mcmc_of(mcmc);
+		const uint64_t n = m.num_samples();
+		*count = n;
+		const uint64_t k = std::min(capacity, n);
+		const uint64_t nodes = n ? m.sample_parents().size() / n : 0;
+		if (steps)
+			std::copy(m.sample_steps().begin(), m.sample_steps().begin() + k, steps);
+		if (parents)
+			std::copy(m.sample_parents().begin(),
+				  m.sample_parents().begin() + k * nodes, parents);
+		if (heights)
+			std::copy(m.sample_heights().begin(),
+				  m.sample_heights().begin() + k * nodes, heights);
+		if (parameters)
+			std::copy(m.sample_params().begin(),
+				  m.sample_params().begin() + k * b3g::kSampleParams,
+				  parameters);
+	});
+}
+
 B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
 				  double *out, uint64_t capacity,
 				  uint64_t *count)

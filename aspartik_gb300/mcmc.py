@@ -120,6 +120,25 @@ class Mcmc:
                                  ct.byref(n)))
         return out
 
+    def samples(self) -> dict:
+        """Every sample of the cold chain: steps, tree (parents and heights of
+        every node) and parameters."""
+        n = ct.c_uint64()
+        check(lib.b3g_mcmc_samples(self._h, None, None, None, None, 0, ct.byref(n)))
+        k = n.value
+        steps = np.zeros(k, dtype=np.uint64)
+        parents = np.zeros((k, self.num_nodes), dtype=np.uint32)
+        heights = np.zeros((k, self.num_nodes))
+        params = np.zeros((k, 14))
+        check(lib.b3g_mcmc_samples(
+            self._h, steps.ctypes.data_as(ct.POINTER(ct.c_uint64)),
+            nat.as_ptr(parents, ct.c_uint32), nat.as_ptr(heights, ct.c_double),
+            nat.as_ptr(params, ct.c_double), k, ct.byref(n)))
+        return {"step": steps, "parents": parents, "heights": heights,
+                "kappa": params[:, 0], "alpha": params[:, 1], "birth_rate": params[:, 2],
+                "rates": params[:, 3:9], "frequencies": params[:, 9:13],
+                "clock_sd": params[:, 13]}
+
     def operator_stats(self) -> dict:
         out = {}
         for k, name in enumerate(OPERATORS):

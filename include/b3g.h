@@ -379,6 +379,15 @@ B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
 B3G_API b3g_status b3g_mcmc_set_clock(b3g_mcmc *mcmc, double sd,
 				      const uint32_t *categories);
 B3G_API b3g_status b3g_mcmc_run(b3g_mcmc *mcmc, uint64_t steps);
+/* Whole samples of the cold chain (for trace files), up to `capacity`;
+ * *count = all.  steps[n]; parents[n][2L-1] (root: 0xFFFFFFFF) and
+ * heights[n][2L-1]; parameters[n][14] = kappa, alpha, birth rate, 6
+ * exchangeabilities, 4 frequencies, relaxed-clock sd (0 if strict).  Any
+ * output may be NULL. */
+B3G_API b3g_status b3g_mcmc_samples(b3g_mcmc *mcmc, uint64_t *steps,
+				    uint32_t *parents, double *heights,
+				    double *parameters, uint64_t capacity,
+				    uint64_t *count);
 /* Copies up to `capacity` samples of a B3G_TRACE_* field; *count = all. */
 B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
 				  double *out, uint64_t capacity,
