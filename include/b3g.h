@@ -341,7 +341,7 @@ typedef struct b3g_mcmc_config {
 	 * around the moved node and 9 model parameters; da_hidden units per
 	 * hidden layer) is trained for da_epochs on the pilot's tree-move pairs
 	 * and screens later subtree-slide and narrow-exchange proposals; the
-	 * exact likelihood stays the second-stage judge, so the target
+	 * exact likelihood stays the second-stage test, so the target
 	 * distribution is unchanged.  Screening stops for good when the RMS of
 	 * (exact - surrogate) over the last 200 screened proposals exceeds
 	 * da_drift_limit (0: never).  da_pilot_steps = 0 turns it off. */
