@@ -22,6 +22,9 @@ constexpr int kMaxStates = 20;
 constexpr int kMaxCategories = 16;
 constexpr uint32_t kPatternAlign = 128;
 
+// Shared-memory slot code meaning "global memory only" (run walk).
+constexpr uint32_t kNoSlot = 0xFFu;
+
 // One entry of the children-first schedule: output slot and the two
 // children, each either a partial slot or (kTipBit | leaf id).
 struct NodeOp {
@@ -80,6 +83,22 @@ struct PruneParams {
 	uint32_t n_runs;
 	uint32_t tile; // patterns per tile
 	uint32_t ptab_smem; // stage the transition tables in shared memory
+	// per entry: shared-memory slot of the output (bits 0-7) and of the
+	// left (8-15) and right (16-23) child, kNoSlot where the value lives
+	// in global memory only; null or n_slots 0: no slots
+	const uint32_t *slots;
+	uint32_t n_slots;
+	// run walk that builds its own transition tables (tables_inline):
+	// run r + 1's tables are built while run r is walked, into a double
+	// buffer of max_run entries in shared memory, with ptab4_kernel's
+	// arithmetic, from the edge lengths (or the given matrices)
+	const ModelDev *model;
+	const double *lengths;  // [n][2], or null
+	const double *matrices; // [n][2][C][4][4], or null
+	double clock_rate;
+	uint32_t tables_inline;
+	uint32_t max_run;
+	uint32_t lengths_smem; // stage the lengths in shared memory
 	double scale_threshold;
 	double scale_mult;
 	double log_inv_c;
@@ -125,6 +144,10 @@ struct BatchParams {
 	uint32_t smem_ptab_bytes; // shared memory reserved for staged tables
 };
 
+// A run of the schedule holds at most kRunCap / C entries (at least 8):
+// the run walk builds one run's transition tables in shared memory.
+constexpr uint32_t kRunCap = 128;
+
 // Transition tables of one list fit shared memory at most this large.
 constexpr uint32_t kPtabSmemBytes = 32u * 1024u;
 
@@ -158,8 +181,11 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 			  cudaStream_t s);
 // Run-synchronous FP32 walk: `ctas` persistent blocks over ldp / p.tile
 // pattern tiles.  Needs p.runs; block sums sized for `ctas`.
+// dynamic shared memory of prune4_runs_kernel for these parameters
+size_t prune4_runs_smem(const PruneParams &p);
+// block: 512 (two blocks per SM) or 1024 threads (one per SM)
 cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
-			       cudaStream_t s);
+			       uint32_t block, cudaStream_t s);
 // 20-state tensor-core path (prune20tc.cuh), FP32 chosen form.
 struct Tc20Params {
 	const uint8_t *tips;

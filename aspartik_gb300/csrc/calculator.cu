@@ -115,6 +115,11 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		if (t == 32 || t == 64 || t == 128)
 			runs_tile_ = t;
 	}
+	if (const char *env = std::getenv("B3G_RUNS_BLOCK")) {
+		const uint32_t b = static_cast<uint32_t>(std::atoi(env));
+		if (b == 512 || b == 1024)
+			runs_block_ = b;
+	}
 	use_runs_ = f32_ && S_ == 4 && runs_tile_ * C_ <= 512;
 	// fused single-launch evaluation of short lists (B3G_DIRECT=0 turns
 	// it off, e.g. to time the two-kernel path)
@@ -130,6 +135,28 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	stamp_.assign(2 * L_ - 1, 0);
 	pos_.assign(2 * L_ - 1, 0);
 	run_of_.assign(I_, 0);
+	smem_of_.assign(2ull * I_, static_cast<uint8_t>(kNoSlot));
+	// shared-memory slots of the run walk (B3G_RUNS_SLOTS=0: children of
+	// listed entries read back from global memory, to time the difference)
+	if (const char *env = std::getenv("B3G_RUNS_SLOTS"))
+		use_slots_ = std::atoi(env) != 0;
+	// per-run tables built by the run walk itself (B3G_RUNS_INLINE=0: a
+	// separate transition kernel writes every table to global memory)
+	if (const char *env = std::getenv("B3G_RUNS_INLINE"))
+		use_inline_ = std::atoi(env) != 0;
+	{
+		int per_sm = 0, reserved = 0;
+		check_cuda(cudaDeviceGetAttribute(
+				   &per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+				   device_),
+			   "shared memory per SM");
+		check_cuda(cudaDeviceGetAttribute(
+				   &reserved, cudaDevAttrReservedSharedMemoryPerBlock,
+				   device_),
+			   "reserved shared memory");
+		smem_per_sm_ = static_cast<uint32_t>(per_sm);
+		smem_reserved_ = static_cast<uint32_t>(reserved);
+	}
 
 	const size_t slots = 2ull * I_;
 	const size_t rsz = f32_ ? sizeof(float) : sizeof(double);
@@ -182,7 +209,8 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 
 		off_pi_ = align_up((size_t)I_ * sizeof(NodeOp), 256);
 		off_runs_ = align_up(off_pi_ + S_ * sizeof(double), 256);
-		off_in_ = align_up(off_runs_ + (size_t)(I_ + 1) * sizeof(uint32_t), 256);
+		off_slots_ = align_up(off_runs_ + (size_t)(I_ + 1) * sizeof(uint32_t), 256);
+		off_in_ = align_up(off_slots_ + (size_t)I_ * sizeof(uint32_t), 256);
 		stage_bytes_ = off_in_ + (size_t)I_ * 2 * C_ * S_ * S_ * sizeof(double);
 		dev_alloc(d_stage_, stage_bytes_, "stage");
 		check_cuda(cudaHostAlloc((void **)&h_stage_, stage_bytes_,
@@ -383,9 +411,14 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 	// Runs of mutually independent entries: entry i opens a new run when
 	// one of its children is listed inside the current run.  validate_lists
 	// left stamp_[v] == stamp_epoch_ on every listed internal.
+	// A run holds at most kRunCap / C entries, so that the run walk's
+	// per-run transition tables fit shared memory.
 	uint32_t run_start = 0;
+	const uint32_t cap = std::max(8u, kRunCap / C_);
 	tip_children_ = 0;
 	for (uint32_t i = 0; i < n; ++i) {
+		if (i - run_start >= cap)
+			run_start = i;
 		NodeOp op;
 		op.out = slot_of(internals[i]);
 		const uint32_t l = children[2 * i], r = children[2 * i + 1];
@@ -408,10 +441,68 @@ void Calculator::stage_ops(const uint32_t *internals, const uint32_t *children,
 	// run starts, then n
 	uint32_t *runs = reinterpret_cast<uint32_t *>(h_stage_ + off_runs_);
 	n_runs_ = 0;
+	max_run_ = 0;
 	for (uint32_t i = 0; i < n; ++i)
-		if (run_of_[i] == i)
+		if (run_of_[i] == i) {
+			if (n_runs_)
+				max_run_ = std::max(max_run_, i - runs[n_runs_ - 1]);
 			runs[n_runs_++] = i;
+		}
 	runs[n_runs_] = n;
+	if (n_runs_)
+		max_run_ = std::max(max_run_, n - runs[n_runs_ - 1]);
+}
+
+// Shared-memory slots for the run walk's outputs (at most `capacity`),
+// written as per-entry codes beside the schedule.  A listed child is read
+// by exactly one entry, its parent, so an entry may write its output into
+// its left (else right) child's slot; an entry without a slotted child
+// takes a slot released in an earlier run; the slot of a second slotted
+// child is released at the end of the run.  Outputs left without a slot,
+// and the last entry's, are read from global memory (or, for the last,
+// from registers).  Returns the number of slots used.
+uint32_t Calculator::assign_slots(uint32_t n, uint32_t capacity)
+{
+	if (capacity == 0)
+		return 0;
+	const NodeOp *ops = reinterpret_cast<const NodeOp *>(h_stage_);
+	uint32_t *codes = reinterpret_cast<uint32_t *>(h_stage_ + off_slots_);
+	free_slots_.clear();
+	pending_slots_.clear();
+	for (uint32_t k = capacity; k-- > 0;)
+		free_slots_.push_back(static_cast<uint8_t>(k));
+	auto src = [&](uint32_t id) -> uint32_t {
+		return (id & kTipBit) ? kNoSlot : smem_of_[id];
+	};
+	uint32_t used = 0;
+	for (uint32_t i = 0; i < n; ++i) {
+		if (run_of_[i] == i) {
+			free_slots_.insert(free_slots_.end(), pending_slots_.begin(),
+					   pending_slots_.end());
+			pending_slots_.clear();
+		}
+		const uint32_t ls = src(ops[i].left), rs = src(ops[i].right);
+		uint32_t os = kNoSlot;
+		if (i + 1 < n) {
+			if (ls != kNoSlot) {
+				os = ls;
+				if (rs != kNoSlot)
+					pending_slots_.push_back(static_cast<uint8_t>(rs));
+			} else if (rs != kNoSlot) {
+				os = rs;
+			} else if (!free_slots_.empty()) {
+				os = free_slots_.back();
+				free_slots_.pop_back();
+			}
+		}
+		smem_of_[ops[i].out] = static_cast<uint8_t>(os);
+		if (os != kNoSlot)
+			used = std::max(used, os + 1);
+		codes[i] = os | (ls << 8) | (rs << 16);
+	}
+	for (uint32_t i = 0; i < n; ++i)
+		smem_of_[ops[i].out] = static_cast<uint8_t>(kNoSlot);
+	return used;
 }
 
 void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
@@ -421,6 +512,52 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	    n <= kDirectMax) {
 		launch_direct(n, clock_rate);
 		return;
+	}
+	// run walk configuration, decided before the upload because the slot
+	// codes travel with the schedule
+	const bool runs = S_ == 4 && use_runs_ && n <= 4096;
+	PruneParams pp{};
+	uint32_t block = 512;
+	if (runs) {
+		pp.n = n;
+		pp.C = C_;
+		pp.num_leaves = L_;
+		pp.n_runs = n_runs_;
+		pp.tile = pick_tile(n);
+		pp.tips_smem = (4ull * tip_children_ >= L_ &&
+				(size_t)L_ * pp.tile <= 32u * 1024u)
+				       ? 1u
+				       : 0u;
+		pp.ptab_smem = (size_t)n * 2 * C_ * 5 * 16 <= kPtabSmemBytes ? 1u : 0u;
+		const uint32_t cols = pp.tile * C_;
+		// 1024-thread blocks only for the run walk proper (a 512-column
+		// tile is the serial walk of a 512-thread block)
+		block = (runs_block_ == 1024 && cols < 512) ? 1024u : 512u;
+		const uint32_t budget = smem_budget(block);
+		if (use_inline_ && block / cols >= 2 && max_run_ > 0) {
+			// the walk builds each run's tables itself, one run ahead
+			pp.tables_inline = 1;
+			pp.ptab_smem = 0;
+			pp.max_run = max_run_;
+			pp.lengths_smem = (!matrices_mode && n <= 1024) ? 1u : 0u;
+			if (prune4_runs_smem(pp) > budget) {
+				pp.tables_inline = 0;
+				pp.max_run = 0;
+				pp.lengths_smem = 0;
+				pp.ptab_smem = (size_t)n * 2 * C_ * 5 * 16 <= kPtabSmemBytes
+						       ? 1u
+						       : 0u;
+			}
+		}
+		if (use_slots_ && block / cols >= 2) {
+			// as many slots as fit beside the rest
+			pp.n_slots = 1;
+			const size_t one = prune4_runs_smem(pp);
+			const size_t per = (size_t)cols * (sizeof(float4) + sizeof(int32_t));
+			const size_t cap = one <= budget ? 1 + (budget - one) / per : 0;
+			pp.n_slots = assign_slots(
+				n, static_cast<uint32_t>(std::min<size_t>(cap, kNoSlot - 1)));
+		}
 	}
 	const size_t in_bytes =
 		matrices_mode ? (size_t)n * 2 * C_ * S_ * S_ * sizeof(double)
@@ -452,10 +589,16 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pt.n = n;
 	pt.C = C_;
 	pt.ptab = d_ptab_;
-	check_cuda(launch_ptab4(pt, f32_, stream_), "transition kernel");
+	if (pp.tables_inline) {
+		pp.model = d_model_;
+		pp.lengths = pt.lengths;
+		pp.matrices = pt.matrices;
+		pp.clock_rate = clock_rate;
+	} else {
+		check_cuda(launch_ptab4(pt, f32_, stream_), "transition kernel");
+	}
 	record(slot.kmid);
 
-	PruneParams pp{};
 	pp.tips = d_tips_;
 	pp.partials = d_partials_;
 	pp.scales = d_scales_;
@@ -474,28 +617,24 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	pp.scale_ln = scale_ln_;
 	pp.num_leaves = L_;
 	// stage the tip tile when the list reads at least a quarter of the
-	// leaves and the tile fits in 64 KiB of shared memory
-	pp.tips_smem = (4ull * tip_children_ >= L_ &&
-			(size_t)L_ * tile_ <= 64u * 1024u)
-			       ? 1u
-			       : 0u;
+	// leaves and the tile fits in 64 KiB of shared memory (the run walk
+	// decided its own above)
+	if (!runs)
+		pp.tips_smem = (4ull * tip_children_ >= L_ &&
+				(size_t)L_ * tile_ <= 64u * 1024u)
+				       ? 1u
+				       : 0u;
 	pp.scale_threshold = std::exp(-static_cast<double>(scale_ln_));
 	pp.scale_mult = std::exp(static_cast<double>(scale_ln_));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 	// the run-synchronous walk stages the schedule in shared memory: keep
 	// it for lists up to 4,096 entries
-	if (use_runs_ && n <= 4096) {
+	if (runs) {
 		pp.runs = reinterpret_cast<const uint32_t *>(d_stage_ + off_runs_);
-		pp.n_runs = n_runs_;
-		pp.tile = pick_tile(n);
-		pp.tips_smem = (4ull * tip_children_ >= L_ &&
-				(size_t)L_ * pp.tile <= 32u * 1024u)
-				       ? 1u
-				       : 0u;
-		pp.ptab_smem = (size_t)n * 2 * C_ * 5 * 16 <= kPtabSmemBytes ? 1u : 0u;
+		pp.slots = reinterpret_cast<const uint32_t *>(d_stage_ + off_slots_);
 		const uint32_t tiles = ldp_ / pp.tile;
-		const uint32_t ctas = std::min(tiles, 2 * num_sms_);
-		check_cuda(launch_prune4_runs(pp, ctas, stream_), "pruning kernel");
+		const uint32_t ctas = std::min(tiles, num_sms_ * (1024 / block));
+		check_cuda(launch_prune4_runs(pp, ctas, block, stream_), "pruning kernel");
 	} else {
 		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
 	}
@@ -898,19 +1037,25 @@ uint32_t Calculator::autotune(const uint32_t *internals,
 	// tuned tile
 	if (!use_runs_ || (use_direct_ && n <= kDirectMax))
 		return runs_tile_;
-	uint32_t best_tile = runs_tile_;
+	// (patterns per tile, threads per block)
+	uint32_t best_tile = runs_tile_, best_block = runs_block_;
 	float best_ms = INFINITY;
-	for (const uint32_t t : {32u, 64u, 128u}) {
-		if (t * C_ > 512)
+	const uint32_t cand[][2] = {{32, 512}, {64, 512}, {128, 512}, {32, 1024}, {64, 1024}};
+	for (const auto &tb : cand) {
+		const uint32_t t = tb[0], b = tb[1];
+		if (t * C_ > 512 || (b == 1024 && t * C_ >= 512))
 			continue;
 		runs_tile_ = t;
+		runs_block_ = b;
 		const float ms = trial();
 		if (ms < best_ms) {
 			best_ms = ms;
 			best_tile = t;
+			best_block = b;
 		}
 	}
 	runs_tile_ = best_tile;
+	runs_block_ = best_block;
 	return best_tile;
 }
 

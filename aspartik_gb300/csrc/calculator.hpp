@@ -104,6 +104,25 @@ class Calculator {
 	std::vector<uint32_t> stamp_;    // per-node epoch stamps
 	std::vector<uint32_t> pos_;      // list position of each listed node
 	std::vector<uint32_t> run_of_;   // start of the run of each entry
+	// run walk: shared-memory slot of each listed output, indexed by the
+	// output's partial slot (kNoSlot outside assign_slots), and the pools
+	std::vector<uint8_t> smem_of_;
+	std::vector<uint8_t> free_slots_, pending_slots_;
+	// dynamic shared memory a run-walk block may take: the SM's, halved
+	// for 512-thread blocks (two per SM), less the reserved share
+	uint32_t smem_per_sm_ = 0, smem_reserved_ = 0;
+	uint32_t smem_budget(uint32_t block) const
+	{
+		const int64_t b = (int64_t)smem_per_sm_ / (1024 / block) -
+				  (int64_t)smem_reserved_ - 256;
+		return b > 0 ? (uint32_t)b : 0u;
+	}
+	// threads per block of the run walk (512 or 1024, autotuned)
+	uint32_t runs_block_ = 512;
+	bool use_slots_ = true;
+	bool use_inline_ = true;
+	size_t off_slots_ = 0;
+	uint32_t assign_slots(uint32_t n, uint32_t capacity);
 	uint32_t stamp_epoch_ = 0;
 	uint32_t tip_children_ = 0;      // tip children in the staged list
 	bool model_set_ = false;
@@ -162,6 +181,7 @@ class Calculator {
 	size_t stage_bytes_ = 0;
 	size_t off_pi_ = 0, off_runs_ = 0, off_in_ = 0;
 	uint32_t n_runs_ = 0;
+	uint32_t max_run_ = 0; // entries of the widest run
 	uint64_t last_upload_bytes_ = 0;
 	// batch membership: staged proposal and the event after which the
 	// batch no longer reads this calculator's staging buffer

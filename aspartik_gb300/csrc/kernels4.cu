@@ -729,21 +729,48 @@ cudaError_t launch_prune4(const PruneParams &p, bool f32, uint32_t tile,
 	return cudaGetLastError();
 }
 
-cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
-			       cudaStream_t s)
+size_t prune4_runs_smem(const PruneParams &p)
 {
 	const uint32_t cols = p.tile * p.C;
-	if (cols > 512)
-		return cudaErrorInvalidValue;
-	const uint32_t threads = cols * (512 / cols);
-	size_t smem = sizeof(double) * (cols + (cols + 1) / 2 + 2 * (size_t)threads) +
-		      sizeof(NodeOp) * p.n + sizeof(uint32_t) * ((p.n_runs + 4) & ~3u);
+	size_t off = sizeof(double) * (cols + (cols + 1) / 2 + 32) +
+		     sizeof(NodeOp) * p.n + sizeof(uint32_t) * ((p.n_runs + 4) & ~3u);
 	if (p.tips_smem)
-		smem += (size_t)p.num_leaves * p.tile;
+		off += (size_t)p.num_leaves * p.tile;
+	off = (off + 15) & ~(size_t)15;
 	if (p.ptab_smem)
-		smem += 16 + (size_t)p.n * 2 * p.C * 5 * sizeof(float4);
+		off += (size_t)p.n * 2 * p.C * 5 * sizeof(float4);
+	if (p.tables_inline) {
+		off += 2 * (size_t)p.max_run * 2 * p.C * 5 * sizeof(float4);
+		off += sizeof(double) * ((p.C + 1) & ~1u) + 40 * sizeof(float);
+		if (p.lengths_smem)
+			off += 2 * sizeof(double) * p.n;
+	}
+	if (p.n_slots) {
+		off = (off + 15) & ~(size_t)15;
+		off += (size_t)p.n_slots * cols * (sizeof(float4) + sizeof(int32_t));
+	}
+	return off;
+}
+
+cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
+			       uint32_t block, cudaStream_t s)
+{
+	const uint32_t cols = p.tile * p.C;
+	if ((block != 512 && block != 1024) || cols > 512 || p.n_slots >= kNoSlot ||
+	    (block == 1024 && cols * 2 > block) ||
+	    (p.n_slots && (block / cols < 2 || !p.slots)) ||
+	    (p.tables_inline &&
+	     (block / cols < 2 || !p.model || p.C > 16 || p.max_run == 0 ||
+	      (!p.lengths && !p.matrices) || (p.lengths_smem && !p.lengths))))
+		return cudaErrorInvalidValue;
+	const uint32_t threads = cols * (block / cols);
+	const size_t smem = prune4_runs_smem(p);
 	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
-	auto kern = narrow ? prune4_runs_kernel<uint32_t> : prune4_runs_kernel<size_t>;
+	auto kern = block == 1024
+			    ? (narrow ? prune4_runs_kernel<uint32_t, 1024>
+				      : prune4_runs_kernel<size_t, 1024>)
+			    : (narrow ? prune4_runs_kernel<uint32_t, 512>
+				      : prune4_runs_kernel<size_t, 512>);
 	if (smem > 48 * 1024) {
 		const cudaError_t e = cudaFuncSetAttribute(
 			kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -27,47 +27,58 @@ struct TileArgs {
 	double *cat_lnl;
 	uint32_t ldp, C, L, tile, n, n_runs, tips_smem;
 	double log_inv_c;
+	// inline tables (RunSmem::tabs set): their sources
+	const ModelDev *model;
+	const double *lengths;
+	const double *matrices;
 };
 
-// Tip codes come from the block's shared-memory tile (tip_row = tile) or
-// from global memory (tips_p = tips + p, tip_row = ldp); the schedule from
-// shared memory.
-template <typename Idx>
-__device__ __forceinline__ void run_item(const NodeOp *__restrict__ ops,
-					 const uint8_t *__restrict__ tips_p,
-					 uint32_t tip_row,
-					 const float4 *__restrict__ ptab,
-					 float4 *__restrict__ part,
-					 int32_t *__restrict__ scales, uint32_t C,
-					 Idx stride, Idx col_off, uint32_t c,
-					 uint32_t i, float4 &y, int32_t &cnt)
+// Shared-memory extras of the run walk (all null: none).  sp/ss: slot
+// partials and counts (the entries' slot codes travel in NodeOp::pad of the
+// schedule's shared-memory copy); tabs: two buffers of
+// tab_stride float4 for the per-run tables; eig (V, V^-1, lambda in FP32),
+// rate (clock rate x category rate) and len (edge lengths, or null: read
+// from global memory) feed the table builder.
+struct RunSmem {
+	float4 *sp;
+	int32_t *ss;
+	float4 *tabs;
+	uint32_t tab_stride;
+	const float *eig;
+	const double *rate;
+	const double *len;
+};
+
+// Transition tables of entries [lo, hi) into buf, entry lo first, in
+// ptab4_kernel's layout and with its arithmetic (the same FP32 eigensystem,
+// the same product of the length and the rates in FP64), one matrix per
+// thread.
+__device__ __forceinline__ void build_run_tables(const TileArgs &a,
+						 const RunSmem &rs,
+						 uint32_t lo, uint32_t hi,
+						 float4 *buf)
 {
-	const NodeOp op = ops[i];
-	const float4 *tl = ptab + ((size_t)(2 * i) * C + c) * 5;
-	const float4 *tr = tl + 5 * C;
-	float4 a, b;
-	int32_t sa = 0, sb = 0;
-	if (op.left & kTipBit) {
-		a = tl[tips_p[(Idx)(op.left & ~kTipBit) * tip_row]];
-	} else {
-		const Idx ix = (Idx)op.left * stride + col_off;
-		const float4 x = part[ix];
-		sa = scales[ix];
-		a = v4_apply(tl, x);
+	const uint32_t C = a.C;
+	const uint32_t count = (hi - lo) * 2 * C;
+	// highest threads first: the last group walks the fewest entries
+	for (uint32_t k = blockDim.x - 1u - threadIdx.x; k < count; k += blockDim.x) {
+		const uint32_t id = lo * 2 * C + k;
+		const uint32_t c = id % C, es = id / C;
+		float P[16];
+		if (a.matrices) {
+			const double *src = a.matrices + (size_t)id * 16;
+			for (int q = 0; q < 16; q++)
+				P[q] = (float)src[q];
+		} else {
+			const double len = rs.len ? rs.len[es] : a.lengths[es];
+			transition4f_eig(a.model, rs.eig, len * rs.rate[c], P);
+		}
+		float4 *out = buf + k * 5;
+#pragma unroll
+		for (int q = 0; q < 4; q++)
+			out[q] = make_float4(P[q], P[4 + q], P[8 + q], P[12 + q]);
+		out[4] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
 	}
-	if (op.right & kTipBit) {
-		b = tr[tips_p[(Idx)(op.right & ~kTipBit) * tip_row]];
-	} else {
-		const Idx ix = (Idx)op.right * stride + col_off;
-		const float4 x = part[ix];
-		sb = scales[ix];
-		b = v4_apply(tr, x);
-	}
-	y = v4_mul(a, b);
-	cnt = sa + sb + rescale_pow2(y);
-	const Idx ox = (Idx)op.out * stride + col_off;
-	part[ox] = y;
-	scales[ox] = cnt;
 }
 
 // Root: frequency-weighted sum of the partial vector, in FP32 (the FP64
@@ -78,14 +89,96 @@ __device__ __forceinline__ float root_dot4(const float *pi, const float4 &y)
 	return fmaf(pi[3], y.w, fmaf(pi[2], y.z, fmaf(pi[1], y.y, pi[0] * y.x)));
 }
 
+// Per-thread constants of a tile walk.  Tip codes come from the block's
+// shared-memory tile (tip_row = tile) or from global memory (tips_p = tips
+// + p, tip_row = ldp); the schedule and the slot codes from shared memory.
+// A listed child whose output sits in a shared-memory slot (sp/ss: slot k
+// of column col at k * cols + col) is read from there: the children of a
+// whole-tree list are then never read back from L2 or DRAM.
+template <typename Idx>
+struct WalkCtx {
+	const NodeOp *ops; // pad: the entry's slot codes
+	float4 *sp;
+	int32_t *ss;
+	const uint8_t *tips_p;
+	const float *pi;
+	const float4 *tab; // tables of entry tab_i0 first
+	uint32_t tab_i0;
+	uint32_t tip_row, c, col, cols;
+	Idx stride, col_off;
+};
+
+// One child of entry i: a tip gives its table row (the product itself), a
+// partial its vector and cumulative count (transformed by the caller).
+template <typename Idx>
+__device__ __forceinline__ void load_child(const TileArgs &a,
+					   const WalkCtx<Idx> &w, uint32_t id,
+					   uint32_t slot, const float4 *tb,
+					   float4 &x, int32_t &s)
+{
+	if (id & kTipBit) {
+		x = tb[w.tips_p[(Idx)(id & ~kTipBit) * w.tip_row]];
+		s = 0;
+	} else if (slot != kNoSlot) {
+		x = w.sp[slot * w.cols + w.col];
+		s = w.ss[slot * w.cols + w.col];
+	} else {
+		const Idx ix = (Idx)id * w.stride + w.col_off;
+		x = a.part[ix];
+		s = a.scales[ix];
+	}
+}
+
+// Entry i of the current run: both children (a tip's table row, a slot,
+// or global memory), the product, the rescaling, the store to global
+// memory (read by later evaluations) and, when the entry has one, to its
+// slot; the list's last entry (the root) leaves its frequency-weighted sum
+// and count in s_dot / s_cnt.  The host gives an entry one of its own
+// children's slots or a slot released in an earlier run, so no other
+// entry of the run reads the slot it writes.
+template <typename Idx>
+__device__ __forceinline__ void run_item(const TileArgs &a,
+					 const WalkCtx<Idx> &w, uint32_t i,
+					 float *s_dot, int32_t *s_cnt)
+{
+	const NodeOp op = w.ops[i];
+	const uint32_t sw = op.pad;
+	const float4 *tl = w.tab + ((2 * (i - w.tab_i0)) * a.C + w.c) * 5;
+	const float4 *tr = tl + 5 * a.C;
+	float4 xa, xb;
+	int32_t sa, sb;
+	load_child<Idx>(a, w, op.left, (sw >> 8) & 0xFFu, tl, xa, sa);
+	load_child<Idx>(a, w, op.right, (sw >> 16) & 0xFFu, tr, xb, sb);
+	if (!(op.left & kTipBit))
+		xa = v4_apply(tl, xa);
+	if (!(op.right & kTipBit))
+		xb = v4_apply(tr, xb);
+	float4 y = v4_mul(xa, xb);
+	const int32_t cnt = sa + sb + rescale_pow2(y);
+	const Idx ox = (Idx)op.out * w.stride + w.col_off;
+	a.part[ox] = y;
+	a.scales[ox] = cnt;
+	const uint32_t os = sw & 0xFFu;
+	if (os != kNoSlot) {
+		w.sp[os * w.cols + w.col] = y;
+		w.ss[os * w.cols + w.col] = cnt;
+	}
+	if (i == a.n - 1) {
+		s_dot[w.col] = root_dot4(w.pi, y);
+		s_cnt[w.col] = cnt;
+	}
+}
+
 // One pattern tile t: every run of the schedule, then the category mixing
 // of the root.  Returns the tile's weighted site sum in thread 0.  Ends with
-// the block synchronised.  s_dot/s_cnt hold tile * C entries, s_red 32.
+// the block synchronised.  s_dot/s_cnt hold tile * C entries, s_red 32;
+// rs the run walk's shared-memory extras.  The run walk reads each entry's
+// slot codes from NodeOp::pad of s_ops (0xFFFFFF: no slots).
 template <typename Idx>
 __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			    int32_t *s_cnt, double *s_red,
 			    const NodeOp *s_ops, const uint32_t *s_runs,
-			    uint8_t *s_tips)
+			    uint8_t *s_tips, const RunSmem &rs = RunSmem{})
 {
 	const uint32_t tile = a.tile, C = a.C;
 	const uint32_t cols = tile * C;
@@ -120,6 +213,9 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 		tips_p = a.tips + p;
 		tip_row = a.ldp;
 	}
+	const bool inl = !serial && rs.tabs != nullptr && a.n_runs != 0;
+	if (inl)
+		build_run_tables(a, rs, s_runs[0], s_runs[1], rs.tabs);
 	__syncthreads();
 	if (serial) {
 		// One thread per column (tile * C == blockDim.x) walks the whole
@@ -173,37 +269,44 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 		s_cnt[col] = c0;
 		__syncthreads();
 	}
-	for (uint32_t r = 0; r < a.n_runs && !serial; ++r) {
-		const uint32_t start = s_runs[r], end = s_runs[r + 1];
-		if (worker) {
-			uint32_t i = start + g;
-			// two independent entries per iteration: all their loads
-			// are issued before either product
-			for (; i + groups < end; i += 2 * groups) {
-				float4 y0, y1;
-				int32_t c0, c1;
-				run_item<Idx>(s_ops, tips_p, tip_row, a.ptab, a.part,
-					      a.scales, C, stride, col_off, c, i, y0, c0);
-				run_item<Idx>(s_ops, tips_p, tip_row, a.ptab, a.part,
-					      a.scales, C, stride, col_off, c,
-					      i + groups, y1, c1);
-				if (i + groups == a.n - 1) {
-					s_dot[col] = root_dot4(s_pi, y1);
-					s_cnt[col] = c1;
-				}
+	if (!serial) {
+		WalkCtx<Idx> w;
+		w.ops = s_ops;
+		w.sp = rs.sp;
+		w.ss = rs.ss;
+		w.tab = a.ptab;
+		w.tab_i0 = 0;
+		w.tips_p = tips_p;
+		w.pi = s_pi;
+		w.tip_row = tip_row;
+		w.c = c;
+		w.col = col;
+		w.cols = cols;
+		w.stride = stride;
+		w.col_off = col_off;
+		for (uint32_t r = 0; r < a.n_runs; ++r) {
+			const uint32_t start = s_runs[r], end = s_runs[r + 1];
+			if (inl) {
+				// the next run's tables into the other buffer (last
+				// read before the previous barrier)
+				if (r + 1 < a.n_runs)
+					build_run_tables(a, rs, end, s_runs[r + 2],
+							 rs.tabs + ((r + 1) & 1u) * rs.tab_stride);
+				w.tab = rs.tabs + (r & 1u) * rs.tab_stride;
+				w.tab_i0 = start;
 			}
-			if (i < end) {
-				float4 y0;
-				int32_t c0;
-				run_item<Idx>(s_ops, tips_p, tip_row, a.ptab, a.part,
-					      a.scales, C, stride, col_off, c, i, y0, c0);
-				if (i == a.n - 1) {
-					s_dot[col] = root_dot4(s_pi, y0);
-					s_cnt[col] = c0;
+			if (worker) {
+				// two independent entries per iteration
+				uint32_t i = start + g;
+				for (; i + groups < end; i += 2 * groups) {
+					run_item<Idx>(a, w, i, s_dot, s_cnt);
+					run_item<Idx>(a, w, i + groups, s_dot, s_cnt);
 				}
+				if (i < end)
+					run_item<Idx>(a, w, i, s_dot, s_cnt);
 			}
+			__syncthreads();
 		}
-		__syncthreads();
 	}
 	// root: category mixing per pattern (threads 0 .. tile-1)
 	double contrib = 0.0;
@@ -278,26 +381,60 @@ __device__ double block_fold(const double *sums, uint32_t count, double *s_red)
 	return total;
 }
 
-// shared memory: [dot: cols][cnt: cols/2][red: 2 * blockDim][ops][runs][tips]
-template <typename Idx>
-__global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
+// shared memory (byte offsets as prune4_runs_smem computes them):
+// [dot: cols][cnt: cols/2][red: 32][ops][runs][tips], 16-byte aligned
+// [list tables], [run table buffers: 2 * max_run * 2C * 5 float4][rates: C
+// doubles, rounded up to even][eigensystem: 40 floats][lengths: 2n
+// doubles], 16-byte aligned [slot partials: n_slots * cols][slot counts:
+// n_slots * cols]
+template <typename Idx, int kThreads>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads)
+	prune4_runs_kernel(PruneParams prm)
 {
 	const uint32_t cols = prm.tile * prm.C;
 	const uint32_t tid = threadIdx.x;
-	extern __shared__ double smem[];
+	extern __shared__ __align__(16) double smem[];
 	double *s_dot = smem;
 	int32_t *s_cnt = (int32_t *)(smem + cols);
-	double *s_red = smem + cols + (cols + 1) / 2;
-	NodeOp *s_ops = (NodeOp *)(s_red + 2 * blockDim.x);
+	double *s_red = smem + cols + (cols + 1) / 2; // one per warp
+	NodeOp *s_ops = (NodeOp *)(s_red + 32);
 	uint32_t *s_runs = (uint32_t *)(s_ops + prm.n);
 	uint8_t *s_tips = (uint8_t *)(s_runs + ((prm.n_runs + 4) & ~3u));
 	float4 *s_ptab = (float4 *)(((uintptr_t)s_tips +
 				     (prm.tips_smem ? prm.num_leaves * prm.tile : 0u) + 15) &
 				    ~(uintptr_t)15);
+	float4 *s_tabs = s_ptab + (prm.ptab_smem ? prm.n * 2 * prm.C * 5 : 0u);
+	const uint32_t tab_stride = prm.max_run * 2 * prm.C * 5;
+	double *s_rate = (double *)(s_tabs + (prm.tables_inline ? 2 * tab_stride : 0u));
+	float *s_eig = (float *)(s_rate + (prm.tables_inline ? (prm.C + 1) & ~1u : 0u));
+	double *s_len = (double *)(s_eig + (prm.tables_inline ? 40 : 0));
+	float4 *s_sp = (float4 *)(((uintptr_t)(s_len + (prm.lengths_smem ? 2 * prm.n : 0u)) +
+				   15) &
+				  ~(uintptr_t)15);
+	int32_t *s_ss = (int32_t *)(s_sp + (size_t)prm.n_slots * cols);
 	__shared__ unsigned s_last;
 
-	for (uint32_t k = tid; k < prm.n; k += blockDim.x)
-		s_ops[k] = prm.ops[k];
+	if (prm.tables_inline) {
+		const ModelDev *m = prm.model;
+		if (tid < 16)
+			s_eig[tid] = (float)m->V[tid];
+		else if (tid < 32)
+			s_eig[tid] = (float)m->Vinv[tid - 16];
+		else if (tid < 36)
+			s_eig[tid] = (float)m->lambda[tid - 32];
+		else if (tid < 36 + prm.C)
+			s_rate[tid - 36] = prm.clock_rate * m->cat_rates[tid - 36];
+		if (prm.lengths_smem)
+			for (uint32_t k = tid; k < 2 * prm.n; k += blockDim.x)
+				s_len[k] = prm.lengths[k];
+	}
+
+	const bool slots = prm.n_slots != 0;
+	for (uint32_t k = tid; k < prm.n; k += blockDim.x) {
+		NodeOp op = prm.ops[k];
+		op.pad = slots ? prm.slots[k] : 0xFFFFFFu;
+		s_ops[k] = op;
+	}
 	for (uint32_t k = tid; k <= prm.n_runs; k += blockDim.x)
 		s_runs[k] = prm.runs[k];
 
@@ -318,6 +455,21 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 	a.n_runs = prm.n_runs;
 	a.tips_smem = prm.tips_smem;
 	a.log_inv_c = prm.log_inv_c;
+	a.model = prm.model;
+	a.lengths = prm.lengths;
+	a.matrices = prm.matrices;
+	RunSmem rs{};
+	if (slots) {
+		rs.sp = s_sp;
+		rs.ss = s_ss;
+	}
+	if (prm.tables_inline) {
+		rs.tabs = s_tabs;
+		rs.tab_stride = tab_stride;
+		rs.eig = s_eig;
+		rs.rate = s_rate;
+		rs.len = prm.lengths_smem ? s_len : nullptr;
+	}
 	if (prm.ptab_smem) {
 		// every table row of the list, once per block (one load latency)
 		const uint32_t rows = prm.n * 2 * prm.C * 5;
@@ -326,12 +478,12 @@ __global__ void __launch_bounds__(512, 2) prune4_runs_kernel(PruneParams prm)
 		a.ptab = s_ptab;
 	}
 
+	__syncthreads(); // the schedule and the table sources are staged
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
 	const uint32_t ntiles = prm.ldp / prm.tile;
 	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const double tsum =
-			tile_walk<Idx>(a, t, (float *)s_dot, s_cnt, s_red, s_ops,
-				       s_runs, s_tips);
+		const double tsum = tile_walk<Idx>(a, t, (float *)s_dot, s_cnt,
+						   s_red, s_ops, s_runs, s_tips, rs);
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
 	}
@@ -549,8 +701,11 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 			const NodeOp *g_ops = (const NodeOp *)md.stage;
 			const uint32_t *g_runs = (const uint32_t *)(md.stage + md.off_runs);
 			s_runs = (uint32_t *)(s_ops + st.n);
-			for (uint32_t k = tid; k < st.n; k += blockDim.x)
-				s_ops[k] = g_ops[k];
+			for (uint32_t k = tid; k < st.n; k += blockDim.x) {
+				NodeOp op = g_ops[k];
+				op.pad = 0xFFFFFFu; // no slots
+				s_ops[k] = op;
+			}
 			for (uint32_t k = tid; k <= st.n_runs; k += blockDim.x)
 				s_runs[k] = g_runs[k];
 			// a small list's tables in shared memory (see the single-
