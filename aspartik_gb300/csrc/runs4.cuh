@@ -105,67 +105,99 @@ struct WalkCtx {
 	const float4 *tab; // tables of entry tab_i0 first
 	uint32_t tab_i0;
 	uint32_t tip_row, c, col, cols;
+	uint32_t half; // the thread's second column: col + half (pattern + half)
 	Idx stride, col_off;
 };
 
-// One child of entry i: a tip gives its table row (the product itself), a
-// partial its vector and cumulative count (transformed by the caller).
+// sum_k x_k * row_k for two vectors with the same four table rows (loaded
+// once), in v4_apply's order.
+__device__ __forceinline__ void v4_apply_pair(const float4 *pt, float4 &x0,
+					      float4 &x1)
+{
+	const float4 r[4] = {pt[0], pt[1], pt[2], pt[3]};
+	x0 = v4_apply(r, x0);
+	x1 = v4_apply(r, x1);
+}
+
+// One child of entry i for the thread's two columns: a tip gives its
+// table rows (the products themselves), a partial its vectors and
+// cumulative counts (transformed by the caller).
 template <typename Idx>
-__device__ __forceinline__ void load_child(const TileArgs &a,
-					   const WalkCtx<Idx> &w, uint32_t id,
-					   uint32_t slot, const float4 *tb,
-					   float4 &x, int32_t &s)
+__device__ __forceinline__ void load_child2(const TileArgs &a,
+					    const WalkCtx<Idx> &w, uint32_t id,
+					    uint32_t slot, const float4 *tb,
+					    float4 &x0, float4 &x1, int32_t &s0,
+					    int32_t &s1)
 {
 	if (id & kTipBit) {
-		x = tb[w.tips_p[(Idx)(id & ~kTipBit) * w.tip_row]];
-		s = 0;
+		const uint8_t *tp = w.tips_p + (Idx)(id & ~kTipBit) * w.tip_row;
+		x0 = tb[tp[0]];
+		x1 = tb[tp[w.half]];
+		s0 = 0;
+		s1 = 0;
 	} else if (slot != kNoSlot) {
-		x = w.sp[slot * w.cols + w.col];
-		s = w.ss[slot * w.cols + w.col];
+		const uint32_t k = slot * w.cols + w.col;
+		x0 = w.sp[k];
+		x1 = w.sp[k + w.half];
+		s0 = w.ss[k];
+		s1 = w.ss[k + w.half];
 	} else {
 		const Idx ix = (Idx)id * w.stride + w.col_off;
-		x = a.part[ix];
-		s = a.scales[ix];
+		x0 = a.part[ix];
+		x1 = a.part[ix + w.half];
+		s0 = a.scales[ix];
+		s1 = a.scales[ix + w.half];
 	}
 }
 
-// Entry i of the current run: both children (a tip's table row, a slot,
-// or global memory), the product, the rescaling, the store to global
-// memory (read by later evaluations) and, when the entry has one, to its
-// slot; the list's last entry (the root) leaves its frequency-weighted sum
-// and count in s_dot / s_cnt.  The host gives an entry one of its own
-// children's slots or a slot released in an earlier run, so no other
-// entry of the run reads the slot it writes.
+// Entry i of the current run for the thread's two columns: both children
+// (a tip's table row, a slot, or global memory), the products, the
+// rescalings, the stores to global memory (read by later evaluations) and,
+// when the entry has one, to its slot; the list's last entry (the root)
+// leaves its frequency-weighted sums and counts in s_dot / s_cnt.  The
+// entry's schedule word, slot codes and table rows are read once for both
+// columns.  The host gives an entry one of its own children's slots or a
+// slot released in an earlier run, so no other entry of the run reads the
+// slot it writes.
 template <typename Idx>
-__device__ __forceinline__ void run_item(const TileArgs &a,
-					 const WalkCtx<Idx> &w, uint32_t i,
-					 float *s_dot, int32_t *s_cnt)
+__device__ __forceinline__ void run_item2(const TileArgs &a,
+					  const WalkCtx<Idx> &w, uint32_t i,
+					  float *s_dot, int32_t *s_cnt)
 {
 	const NodeOp op = w.ops[i];
 	const uint32_t sw = op.pad;
 	const float4 *tl = w.tab + ((2 * (i - w.tab_i0)) * a.C + w.c) * 5;
 	const float4 *tr = tl + 5 * a.C;
-	float4 xa, xb;
-	int32_t sa, sb;
-	load_child<Idx>(a, w, op.left, (sw >> 8) & 0xFFu, tl, xa, sa);
-	load_child<Idx>(a, w, op.right, (sw >> 16) & 0xFFu, tr, xb, sb);
+	float4 a0, a1, b0, b1;
+	int32_t sa0, sa1, sb0, sb1;
+	load_child2<Idx>(a, w, op.left, (sw >> 8) & 0xFFu, tl, a0, a1, sa0, sa1);
+	load_child2<Idx>(a, w, op.right, (sw >> 16) & 0xFFu, tr, b0, b1, sb0,
+			 sb1);
 	if (!(op.left & kTipBit))
-		xa = v4_apply(tl, xa);
+		v4_apply_pair(tl, a0, a1);
 	if (!(op.right & kTipBit))
-		xb = v4_apply(tr, xb);
-	float4 y = v4_mul(xa, xb);
-	const int32_t cnt = sa + sb + rescale_pow2(y);
+		v4_apply_pair(tr, b0, b1);
+	float4 y0 = v4_mul(a0, b0), y1 = v4_mul(a1, b1);
+	const int32_t n0 = sa0 + sb0 + rescale_pow2(y0);
+	const int32_t n1 = sa1 + sb1 + rescale_pow2(y1);
 	const Idx ox = (Idx)op.out * w.stride + w.col_off;
-	a.part[ox] = y;
-	a.scales[ox] = cnt;
+	a.part[ox] = y0;
+	a.part[ox + w.half] = y1;
+	a.scales[ox] = n0;
+	a.scales[ox + w.half] = n1;
 	const uint32_t os = sw & 0xFFu;
 	if (os != kNoSlot) {
-		w.sp[os * w.cols + w.col] = y;
-		w.ss[os * w.cols + w.col] = cnt;
+		const uint32_t k = os * w.cols + w.col;
+		w.sp[k] = y0;
+		w.sp[k + w.half] = y1;
+		w.ss[k] = n0;
+		w.ss[k + w.half] = n1;
 	}
 	if (i == a.n - 1) {
-		s_dot[w.col] = root_dot4(w.pi, y);
-		s_cnt[w.col] = cnt;
+		s_dot[w.col] = root_dot4(w.pi, y0);
+		s_dot[w.col + w.half] = root_dot4(w.pi, y1);
+		s_cnt[w.col] = n0;
+		s_cnt[w.col + w.half] = n1;
 	}
 }
 
@@ -184,9 +216,8 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 	const uint32_t cols = tile * C;
 	const uint32_t groups = blockDim.x / cols;
 	const uint32_t tid = threadIdx.x;
-	const uint32_t col = tid % cols, g = tid / cols;
+	const uint32_t col = tid % cols;
 	const uint32_t c = col / tile, pl = col - c * tile;
-	const bool worker = g < groups;
 	const Idx stride = (Idx)C * a.ldp;
 	const uint32_t p = t * tile + pl;
 	const Idx col_off = (Idx)c * a.ldp + p;
@@ -195,7 +226,7 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 	if (tid < 4)
 		s_pi[tid] = (float)a.pi[tid];
 	const bool serial = groups == 1;
-	const uint8_t *tips_p;
+	const uint8_t *tips_p, *tips_base;
 	uint32_t tip_row;
 	if (a.tips_smem) {
 		// 4-byte loads: rows start at multiples of 32 patterns
@@ -207,12 +238,13 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			s_t32[k] = *(const uint32_t *)(a.tips + (size_t)leaf * a.ldp +
 						       t * tile + w4 * 4);
 		}
-		tips_p = s_tips + pl;
+		tips_base = s_tips;
 		tip_row = tile;
 	} else {
-		tips_p = a.tips + p;
+		tips_base = a.tips + t * tile;
 		tip_row = a.ldp;
 	}
+	tips_p = tips_base + pl;
 	const bool inl = !serial && rs.tabs != nullptr && a.n_runs != 0;
 	if (inl)
 		build_run_tables(a, rs, s_runs[0], s_runs[1], rs.tabs);
@@ -270,20 +302,27 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 		__syncthreads();
 	}
 	if (!serial) {
+		// two columns per thread: patterns ph and ph + tile / 2 of one
+		// category, so a warp still reads 32 consecutive patterns
+		const uint32_t half = tile >> 1, tcols = cols >> 1;
+		const uint32_t rgroups = blockDim.x / tcols;
+		const uint32_t ct = tid % tcols, rg = tid / tcols;
+		const uint32_t rc = ct / half, ph = ct - rc * half;
 		WalkCtx<Idx> w;
 		w.ops = s_ops;
 		w.sp = rs.sp;
 		w.ss = rs.ss;
 		w.tab = a.ptab;
 		w.tab_i0 = 0;
-		w.tips_p = tips_p;
+		w.tips_p = tips_base + ph;
 		w.pi = s_pi;
 		w.tip_row = tip_row;
-		w.c = c;
-		w.col = col;
+		w.c = rc;
+		w.col = rc * tile + ph;
 		w.cols = cols;
+		w.half = half;
 		w.stride = stride;
-		w.col_off = col_off;
+		w.col_off = (Idx)rc * a.ldp + t * tile + ph;
 		for (uint32_t r = 0; r < a.n_runs; ++r) {
 			const uint32_t start = s_runs[r], end = s_runs[r + 1];
 			if (inl) {
@@ -295,16 +334,8 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 				w.tab = rs.tabs + (r & 1u) * rs.tab_stride;
 				w.tab_i0 = start;
 			}
-			if (worker) {
-				// two independent entries per iteration
-				uint32_t i = start + g;
-				for (; i + groups < end; i += 2 * groups) {
-					run_item<Idx>(a, w, i, s_dot, s_cnt);
-					run_item<Idx>(a, w, i + groups, s_dot, s_cnt);
-				}
-				if (i < end)
-					run_item<Idx>(a, w, i, s_dot, s_cnt);
-			}
+			for (uint32_t i = start + rg; i < end; i += rgroups)
+				run_item2<Idx>(a, w, i, s_dot, s_cnt);
 			__syncthreads();
 		}
 	}
