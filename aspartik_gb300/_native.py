@@ -154,6 +154,7 @@ SIGNATURES = {
     "b3g_calculator_timing_totals": (
         ct.c_int, [_vp, ct.c_int, _f64p, _f64p, ct.POINTER(ct.c_uint64)]),
     "b3g_calculator_last_upload_bytes": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64)]),
+    "b3g_calculator_last_launches": (ct.c_int, [_vp, _u32p]),
     "b3g_calculator_span_begin": (ct.c_int, [_vp]),
     "b3g_calculator_span_end": (ct.c_int, [_vp, _f32p]),
     "b3g_prune_noalloc": (ct.c_int, [ct.POINTER(PruneBuffers), _vp]),

@@ -218,6 +218,12 @@ class GpuCalculator:
         check(lib.b3g_calculator_last_upload_bytes(self._h, ct.byref(n)))
         return int(n.value)
 
+    def last_launches(self) -> int:
+        """Kernels the last evaluation launched."""
+        n = ct.c_uint32()
+        check(lib.b3g_calculator_last_launches(self._h, ct.byref(n)))
+        return int(n.value)
+
     def span_begin(self) -> None:
         check(lib.b3g_calculator_span_begin(self._h))
 

@@ -71,6 +71,7 @@ struct PruneParams {
 	double *block_sums; // [gridDim.x]
 	unsigned *ticket;   // zero between launches
 	double *lnl_out;    // [1]
+	double *lnl_host;   // host-mapped word that also receives it, or null
 	uint32_t n;
 	uint32_t ldp;
 	uint32_t C;

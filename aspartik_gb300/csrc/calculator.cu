@@ -594,8 +594,10 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 		pp.lengths = pt.lengths;
 		pp.matrices = pt.matrices;
 		pp.clock_rate = clock_rate;
+		last_launches_ = 1;
 	} else {
 		check_cuda(launch_ptab4(pt, f32_, stream_), "transition kernel");
+		last_launches_ = 2;
 	}
 	record(slot.kmid);
 
@@ -634,6 +636,8 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 		pp.slots = reinterpret_cast<const uint32_t *>(d_stage_ + off_slots_);
 		const uint32_t tiles = ldp_ / pp.tile;
 		const uint32_t ctas = std::min(tiles, num_sms_ * (1024 / block));
+		// the result also goes straight to the mapped host word
+		pp.lnl_host = d_lnl_host_;
 		check_cuda(launch_prune4_runs(pp, ctas, block, stream_), "pruning kernel");
 	} else {
 		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
@@ -641,9 +645,10 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 	record(slot.k1);
 	slot.pending = timing_;
 	ring_next_ += timing_ ? 1 : 0;
-	check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
-				   cudaMemcpyDeviceToHost, stream_),
-		   "read lnl");
+	if (!runs)
+		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double),
+					   cudaMemcpyDeviceToHost, stream_),
+			   "read lnl");
 	have_result_ = true;
 	outstanding_ = true;
 	stream_dirty_ = true;
@@ -668,6 +673,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 	pt.ptab = d_ptab_;
 	if (use_tc20_) {
 		check_cuda(launch_ptab20tc(pt, d_tc_tab_, stream_), "transition kernel");
+		last_launches_ = 3; // tables, pruning, root and sum
 		record(slot.kmid);
 		Tc20Params tp{};
 		tp.tips = d_tips_;
@@ -712,6 +718,7 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		return;
 	}
 	check_cuda(launch_ptab20(pt, f32_, stream_), "transition kernel");
+	last_launches_ = 2;
 	record(slot.kmid);
 	PruneParams pp{};
 	pp.tips = d_tips_;
@@ -783,6 +790,7 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	record(slot.k0);
 	const uint32_t ctas = std::min(ldp_ / 128u, 2 * num_sms_);
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
+	last_launches_ = 1;
 	record(slot.k1);
 	slot.pending = timing_;
 	ring_next_ += timing_ ? 1 : 0;
@@ -1387,6 +1395,16 @@ B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
 		if (!bytes)
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
 		*bytes = calc_of(calc)->last_upload_bytes();
+	});
+}
+
+B3G_API b3g_status b3g_calculator_last_launches(b3g_calculator *calc,
+						uint32_t *kernels)
+{
+	return guarded([&] {
+		if (!kernels)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		*kernels = calc_of(calc)->last_launches();
 	});
 }
 

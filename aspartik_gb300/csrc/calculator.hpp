@@ -69,6 +69,7 @@ class Calculator {
 	void span_begin();
 	float span_end();
 	uint64_t last_upload_bytes() const { return last_upload_bytes_; }
+	uint32_t last_launches() const { return last_launches_; }
 	uint32_t autotune(const uint32_t *internals, const uint32_t *children,
 			  uint32_t n, const double *lengths, double clock_rate);
 
@@ -183,6 +184,7 @@ class Calculator {
 	uint32_t n_runs_ = 0;
 	uint32_t max_run_ = 0; // entries of the widest run
 	uint64_t last_upload_bytes_ = 0;
+	uint32_t last_launches_ = 0; // kernels the last evaluation launched
 	// batch membership: staged proposal and the event after which the
 	// batch no longer reads this calculator's staging buffer
 	bool in_batch_ = false;

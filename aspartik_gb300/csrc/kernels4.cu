@@ -175,18 +175,21 @@ __device__ void transition4(const ModelDev *__restrict__ m, double d,
 // FP32 chosen form: P(t) in single precision from the FP64 eigensystem
 // (the decomposition of Q is the only FP64 work of this step; on GB300 FP64
 // issues at 1/64 of the FP32 rate).  The shortcut tests stay in FP64.
-// eig: V (16), Vinv (16) and lambda (4) of a four-state model, in FP32.
+// eig: V (16), Vinv (16) and lambda (4) of a four-state model, in FP32,
+// then the model's shortcuts flag (nonzero: on) at eig[36], so that the
+// common path reads nothing from the model in global memory.
 __device__ void transition4f_eig(const ModelDev *__restrict__ m,
 				 const float *__restrict__ eig, double d,
 				 float P[16])
 {
-	if (m->shortcuts && d > 20.0) {
+	const bool shortcuts = eig[36] != 0.0f;
+	if (shortcuts && d > 20.0) {
 		for (int i = 0; i < 4; i++)
 			for (int j = 0; j < 4; j++)
 				P[i * 4 + j] = (float)m->pi[j];
 		return;
 	}
-	if (m->shortcuts && d < 1e-10) {
+	if (shortcuts && d < 1e-10) {
 		for (int i = 0; i < 4; i++)
 			for (int j = 0; j < 4; j++)
 				P[i * 4 + j] = i == j ? 1.0f : (float)(m->Q[i * 4 + j] * d);
@@ -214,13 +217,14 @@ __device__ void transition4f_eig(const ModelDev *__restrict__ m,
 __device__ void transition4f(const ModelDev *__restrict__ m, double d,
 			     float P[16])
 {
-	float eig[36];
+	float eig[37];
 	for (int k = 0; k < 16; k++) {
 		eig[k] = (float)m->V[k];
 		eig[16 + k] = (float)m->Vinv[k];
 	}
 	for (int k = 0; k < 4; k++)
 		eig[32 + k] = (float)m->lambda[k];
+	eig[36] = m->shortcuts ? 1.0f : 0.0f;
 	transition4f_eig(m, eig, d, P);
 }
 

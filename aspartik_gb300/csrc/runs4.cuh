@@ -453,8 +453,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 			s_eig[tid] = (float)m->Vinv[tid - 16];
 		else if (tid < 36)
 			s_eig[tid] = (float)m->lambda[tid - 32];
-		else if (tid < 36 + prm.C)
-			s_rate[tid - 36] = prm.clock_rate * m->cat_rates[tid - 36];
+		else if (tid == 36)
+			s_eig[36] = m->shortcuts ? 1.0f : 0.0f;
+		else if (tid < 40 + prm.C && tid >= 40)
+			s_rate[tid - 40] = prm.clock_rate * m->cat_rates[tid - 40];
 		if (prm.lengths_smem)
 			for (uint32_t k = tid; k < 2 * prm.n; k += blockDim.x)
 				s_len[k] = prm.lengths[k];
@@ -533,6 +535,8 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 	const double total = block_fold(prm.block_sums, gridDim.x, s_red);
 	if (tid == 0) {
 		*prm.lnl_out = total;
+		if (prm.lnl_host)
+			*prm.lnl_host = total;
 		*prm.ticket = 0u;
 	}
 }
@@ -551,7 +555,7 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 {
 	constexpr uint32_t kC = 4, kTile = 128, kCols = kTile * kC;
 	__shared__ float4 s_tab[kDirectMax * 2 * kC * 5];
-	__shared__ float s_eig[36];
+	__shared__ float s_eig[37];
 	__shared__ double s_rate[kC];
 	__shared__ float s_dot[kCols];
 	__shared__ int32_t s_cnt[kCols];
@@ -567,6 +571,8 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 		s_eig[tid] = (float)m->lambda[tid - 32];
 	else if (tid < 40)
 		s_rate[tid - 36] = prm.clock_rate * m->cat_rates[tid - 36];
+	else if (tid == 40)
+		s_eig[36] = m->shortcuts ? 1.0f : 0.0f;
 	__syncthreads();
 	if (tid < prm.n * 2 * kC) {
 		// table (entry, side, category), laid out as ptab4_kernel's

@@ -191,6 +191,12 @@ B3G_API b3g_status b3g_calculator_timing_totals(b3g_calculator *calc,
  * schedule runs, frequencies and lengths or matrices). */
 B3G_API b3g_status b3g_calculator_last_upload_bytes(b3g_calculator *calc,
 						    uint64_t *bytes);
+/* Kernels the last evaluation launched on the calculator's stream (one
+ * fused launch for a short FP32 list or a run walk that builds its own
+ * tables; tables + pruning otherwise; three for 20 states on the tensor
+ * cores). */
+B3G_API b3g_status b3g_calculator_last_launches(b3g_calculator *calc,
+						uint32_t *kernels);
 /* Device time between two markers on the calculator's stream: span_begin
  * records the first, span_end records the second, waits and returns the
  * elapsed milliseconds. */

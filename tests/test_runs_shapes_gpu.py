@@ -94,3 +94,27 @@ def test_every_shape_gives_the_same_values(K, alpha, taxa, sites, monkeypatch):
         twin = (SHAPES[0][0], SHAPES[0][1], 0, 0)
         if shape[:2] == twin[:2]:
             assert [x[0] for x in seq] == [x[0] for x in base], shape
+
+
+@pytest.mark.parametrize("precision,inline,want", [("f32", 1, 1), ("f32", 0, 2), ("f64", 1, 2)])
+def test_kernels_per_evaluation(precision, inline, want, monkeypatch):
+    """One launch for a run walk that builds its own tables, tables +
+    pruning otherwise, one fused launch for a short FP32 list."""
+    monkeypatch.setenv("B3G_RUNS_INLINE", str(inline))
+    c = dna_case(64, 2000, seed=91, model="gtr", alpha=0.5, num_categories=4)
+    g = make_gpu(c.leaves, c.weights, 4, precision)
+    g.set_reversible(c.rates, c.pi)
+    g.set_gamma(0.5)
+    tree = full(c.tree.parents, c.tree.heights)
+    g.propose_lengths(*lists_and_lengths(tree), 1.0)
+    g.log_likelihood()
+    assert g.last_launches() == want
+    g.accept()
+    tree.accept()
+    random_move(tree, np.random.default_rng(3))
+    internals, children, lengths = lists_and_lengths(tree)
+    g.propose_lengths(internals, children, lengths, 1.0)
+    g.log_likelihood()
+    if precision == "f32" and len(internals) <= 48:
+        assert g.last_launches() == 1
+    g.close()
