@@ -190,6 +190,19 @@ SIGNATURES = {
     "b3g_mcmc_check": (ct.c_int, [_vp, _f64p]),
     "b3g_mcmc_da_stats": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), _f64p]),
     "b3g_mcmc_chain_state": (ct.c_int, [_vp, ct.c_uint32, _u32p, _f64p, _f64p, _f64p]),
+    "b3g_create": (ct.c_int, [ct.POINTER(Config), _u8p, _u32p, ct.c_uint32, ct.POINTER(_vp)]),
+    "b3g_destroy": (None, [_vp]),
+    "b3g_set_model": (ct.c_int, [_vp, ct.c_uint32, ct.c_uint32, _f64p, _f64p, _f64p, _f64p,
+                                 _f64p, ct.c_uint32]),
+    "b3g_set_tree": (ct.c_int, [_vp, ct.c_uint32, _u32p, _f64p, ct.c_double]),
+    "b3g_mark_edges": (ct.c_int, [_vp, ct.c_uint32, _u32p, ct.c_uint32]),
+    "b3g_mark_all": (ct.c_int, [_vp, ct.c_uint32]),
+    "b3g_propose": (ct.c_int, [_vp, ct.c_uint64]),
+    "b3g_wait": (ct.c_int, [_vp]),
+    "b3g_lnl": (ct.c_int, [_vp, ct.c_uint32, _f64p]),
+    "b3g_site_lnl": (ct.c_int, [_vp, ct.c_uint32, _f64p]),
+    "b3g_accept": (ct.c_int, [_vp, ct.c_uint32]),
+    "b3g_reject": (ct.c_int, [_vp, ct.c_uint32]),
 }
 
 

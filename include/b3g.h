@@ -79,6 +79,7 @@ typedef struct b3g_config {
 
 typedef struct b3g_calculator b3g_calculator;
 typedef struct b3g_batch b3g_batch;
+typedef struct b3g_handle b3g_handle;
 
 /* Message of the calling thread's last failed call ("" if none). */
 B3G_API const char *b3g_last_error(void);
@@ -524,6 +525,44 @@ typedef struct b3g_prune_buffers {
 
 B3G_API b3g_status b3g_prune_noalloc(const b3g_prune_buffers *buffers,
 				     void *stream);
+
+/* ---- tree-level handle -------------------------------------------------
+ * The call sequence b3's MCMC makes around its likelihood
+ * (likelihood/dna.rs:68-124, likelihood/gamma.rs:97-169) with the tree
+ * mirrored inside the library, for 1..64 chains over one alignment: load the
+ * tree (parents[2L-1], root 0xFFFFFFFF, and heights[2L-1], as
+ * tree.rs:906-930), mark the edges a move changed (edge id = child node
+ * id, tree.rs:357-386), propose a set of chains (asynchronous; each chain
+ * has its own calculator and stream, so the chains run concurrently), read
+ * the log-likelihoods, then accept or reject each proposed chain.  The dirty
+ * list is built from the mirrored tree as partials_lists builds it
+ * (tree.rs:398-461).  A reject returns the chain's tree to its last
+ * accepted state (the first tree loaded counts as accepted).  One host
+ * thread per handle. */
+B3G_API b3g_status b3g_create(const b3g_config *config, const uint8_t *tips,
+			      const uint32_t *weights, uint32_t num_chains,
+			      b3g_handle **out);
+B3G_API void b3g_destroy(b3g_handle *h);
+/* V, Vinv row-major S x S, lambda[S], pi[S], cat_rates[C] (mean one);
+ * S and C must match the handle's configuration. */
+B3G_API b3g_status b3g_set_model(b3g_handle *h, uint32_t chain, uint32_t S,
+				 const double *V, const double *Vinv,
+				 const double *lambda, const double *pi,
+				 const double *cat_rates, uint32_t C);
+B3G_API b3g_status b3g_set_tree(b3g_handle *h, uint32_t chain,
+				const uint32_t *parents, const double *heights,
+				double clock_rate);
+B3G_API b3g_status b3g_mark_edges(b3g_handle *h, uint32_t chain,
+				  const uint32_t *edges, uint32_t n);
+B3G_API b3g_status b3g_mark_all(b3g_handle *h, uint32_t chain);
+/* bit c of chains_mask: evaluate chain c */
+B3G_API b3g_status b3g_propose(b3g_handle *h, uint64_t chains_mask);
+B3G_API b3g_status b3g_wait(b3g_handle *h);
+B3G_API b3g_status b3g_lnl(b3g_handle *h, uint32_t chain, double *out);
+/* per-pattern lnL (categories mixed, scaling removed), [num_patterns] */
+B3G_API b3g_status b3g_site_lnl(b3g_handle *h, uint32_t chain, double *out);
+B3G_API b3g_status b3g_accept(b3g_handle *h, uint32_t chain);
+B3G_API b3g_status b3g_reject(b3g_handle *h, uint32_t chain);
 
 #ifdef __cplusplus
 }
