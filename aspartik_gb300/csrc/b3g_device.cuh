@@ -172,6 +172,12 @@ struct DirectParams {
 	double clock_rate;
 	double log_inv_c;
 	double pi[4];
+	// the model as the table builder reads it, converted on the host with
+	// the same rounding: V, V^-1, lambda in FP32, the shortcuts flag at
+	// [36]; and clock rate x category rate in FP64 (the model in global
+	// memory is read only on the shortcut paths)
+	float eig[40];
+	double rate[4];
 	NodeOp ops[kDirectMax];
 	double lengths[2 * kDirectMax]; // [n][2] time lengths
 };

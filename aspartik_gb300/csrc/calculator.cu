@@ -778,6 +778,16 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	dp.clock_rate = clock_rate;
 	dp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 	std::memcpy(dp.pi, h_stage_ + off_pi_, 4 * sizeof(double));
+	for (int k = 0; k < 16; ++k) {
+		dp.eig[k] = static_cast<float>(model_host_.V[k]);
+		dp.eig[16 + k] = static_cast<float>(model_host_.Vinv[k]);
+	}
+	for (int k = 0; k < 4; ++k) {
+		dp.eig[32 + k] = static_cast<float>(model_host_.lambda[k]);
+		dp.rate[k] = clock_rate * model_host_.cat_rates[k];
+	}
+	dp.eig[36] = model_host_.shortcuts ? 1.0f : 0.0f;
+	dp.eig[37] = dp.eig[38] = dp.eig[39] = 0.0f;
 	std::memcpy(dp.ops, h_stage_, (size_t)n * sizeof(NodeOp));
 	std::memcpy(dp.lengths, h_stage_ + off_in_, (size_t)n * 2 * sizeof(double));
 	// bytes that reach the device with the launch

@@ -563,16 +563,11 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	__shared__ unsigned s_last;
 	const uint32_t tid = threadIdx.x;
 	const ModelDev *m = prm.model;
-	if (tid < 16)
-		s_eig[tid] = (float)m->V[tid];
-	else if (tid < 32)
-		s_eig[tid] = (float)m->Vinv[tid - 16];
-	else if (tid < 36)
-		s_eig[tid] = (float)m->lambda[tid - 32];
-	else if (tid < 40)
-		s_rate[tid - 36] = prm.clock_rate * m->cat_rates[tid - 36];
-	else if (tid == 40)
-		s_eig[36] = m->shortcuts ? 1.0f : 0.0f;
+	// from the parameters: no global-memory round trip before the tables
+	if (tid < 37)
+		s_eig[tid] = prm.eig[tid];
+	else if (tid < 41)
+		s_rate[tid - 37] = prm.rate[tid - 37];
 	__syncthreads();
 	if (tid < prm.n * 2 * kC) {
 		// table (entry, side, category), laid out as ptab4_kernel's
