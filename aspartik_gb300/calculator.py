@@ -169,8 +169,8 @@ class GpuCalculator:
         if children.size != 2 * n or lengths.size != 2 * n:
             raise ValueError("children and lengths need two values per internal")
         check(lib.b3g_calculator_propose_lengths(
-            self._h, nat.as_ptr(internals, ct.c_uint32), nat.as_ptr(children, ct.c_uint32),
-            n, nat.as_ptr(lengths, ct.c_double), float(clock_rate)))
+            self._h, nat.addr(internals), nat.addr(children), n, nat.addr(lengths),
+            float(clock_rate)))
 
     def autotune(self, internals, children, lengths, clock_rate: float = 1.0) -> int:
         """Time the list with each launch configuration of this form and keep
@@ -198,6 +198,11 @@ class GpuCalculator:
         out = np.empty(self._P, dtype=np.float64)
         check(lib.b3g_calculator_site_log_likelihoods(self._h, nat.as_ptr(out, ct.c_double)))
         return out
+
+    def set_timing(self, on: bool = True) -> None:
+        """CUDA events around every evaluation (for last_timing /
+        timing_totals); off by default."""
+        check(lib.b3g_calculator_set_timing(self._h, 1 if on else 0))
 
     def last_timing(self) -> tuple[float, float]:
         """(transition-kernel ms, pruning-kernel ms) of the last proposal."""
@@ -242,8 +247,8 @@ def _stage_lengths(self, internals, children, lengths, clock_rate: float = 1.0) 
     if children.size != 2 * n or lengths.size != 2 * n:
         raise ValueError("children and lengths need two values per internal")
     check(lib.b3g_calculator_stage_lengths(
-        self._h, nat.as_ptr(internals, ct.c_uint32), nat.as_ptr(children, ct.c_uint32), n,
-        nat.as_ptr(lengths, ct.c_double), float(clock_rate)))
+        self._h, nat.addr(internals), nat.addr(children), n, nat.addr(lengths),
+        float(clock_rate)))
 
 
 GpuCalculator.stage_lengths = _stage_lengths

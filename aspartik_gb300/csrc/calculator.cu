@@ -964,6 +964,9 @@ void Calculator::harvest(TimingSlot &s)
 void Calculator::last_timing(float *transition_ms, float *prune_ms)
 {
 	DeviceGuard g(device_);
+	if (!timing_)
+		throw Error(B3G_ERR_STATE,
+			    "timing is off (b3g_calculator_set_timing)");
 	if (!have_result_ || ring_next_ == 0)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
 	TimingSlot &s = ring_[(ring_next_ - 1) % kRing];
@@ -1371,6 +1374,11 @@ B3G_API b3g_status b3g_calculator_site_log_likelihoods(b3g_calculator *calc,
 						       double *out)
 {
 	return guarded([&] { calc_of(calc)->site_log_likelihoods(out); });
+}
+
+B3G_API b3g_status b3g_calculator_set_timing(b3g_calculator *calc, int on)
+{
+	return guarded([&] { calc_of(calc)->set_timing(on != 0); });
 }
 
 B3G_API b3g_status b3g_calculator_last_timing(b3g_calculator *calc,

@@ -150,7 +150,7 @@ class Calculator {
 	uint64_t acc_count_ = 0;
 	void harvest(TimingSlot &s);
 	void record(cudaEvent_t e); // a timing event, when timing is on
-	bool timing_ = true;
+	bool timing_ = false; // CUDA events around every evaluation (off: none)
 
       public:
 	// Per-proposal device timing (events around the kernels).  On by

@@ -28,6 +28,8 @@
 
 #include <math.h>
 
+#include <atomic>
+
 namespace b3g {
 namespace {
 
@@ -776,10 +778,35 @@ cudaError_t launch_prune4_runs(const PruneParams &p, uint32_t ctas,
 			    : (narrow ? prune4_runs_kernel<uint32_t, 512>
 				      : prune4_runs_kernel<size_t, 512>);
 	if (smem > 48 * 1024) {
-		const cudaError_t e = cudaFuncSetAttribute(
-			kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		// once per (kernel variant, device): allow the device's whole
+		// opt-in shared memory (a permission, not a reservation), so no
+		// call lowers another's limit and later launches pay nothing
+		static std::atomic<bool> opted[4][64];
+		int dev = 0;
+		cudaError_t e = cudaGetDevice(&dev);
 		if (e != cudaSuccess)
 			return e;
+		const int v = (block == 1024 ? 2 : 0) + (narrow ? 0 : 1);
+		if (dev < 0 || dev >= 64 || !opted[v][dev].load(std::memory_order_acquire)) {
+			int most = 0;
+			e = cudaDeviceGetAttribute(
+				&most, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+			if (e != cudaSuccess)
+				return e;
+			cudaFuncAttributes fa{};
+			e = cudaFuncGetAttributes(&fa, kern);
+			if (e != cudaSuccess)
+				return e;
+			most -= (int)fa.sharedSizeBytes; // static + dynamic <= opt-in
+			if ((int)smem > most)
+				return cudaErrorInvalidValue;
+			e = cudaFuncSetAttribute(
+				kern, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+			if (e != cudaSuccess)
+				return e;
+			if (dev >= 0 && dev < 64)
+				opted[v][dev].store(true, std::memory_order_release);
+		}
 	}
 	kern<<<ctas, threads, smem, s>>>(p);
 	return cudaGetLastError();

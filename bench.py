@@ -198,18 +198,27 @@ def make_calc(wl, precision: str, device: int):
 
 
 def device_throughput(calc, lists, steps, warmup, world):
+    """Device time of `steps` back-to-back evaluations (no per-launch
+    events, as a caller runs them), then the same evaluations again with
+    CUDA events around each kernel for the per-kernel times."""
     internals, children, lengths = lists
+    calc.set_timing(False)
     for _ in range(warmup):
         calc.propose_lengths(internals, children, lengths, 1.0)
     calc.log_likelihood()
-    calc.timing_totals(reset=True)
     barrier(world)
     calc.span_begin()
     for _ in range(steps):
         calc.propose_lengths(internals, children, lengths, 1.0)
     ms = calc.span_end()
     barrier(world)
+    calc.set_timing(True)
+    calc.timing_totals(reset=True)
+    for _ in range(steps):
+        calc.propose_lengths(internals, children, lengths, 1.0)
+    calc.log_likelihood()
     tt, tp, n = calc.timing_totals(reset=True)
+    calc.set_timing(False)
     return ms, tt / max(n, 1), tp / max(n, 1), n
 
 
@@ -558,12 +567,17 @@ def run_ours(args):
     for p in paths[:args.warmup]:
         calc.propose_lengths(*p, 1.0)
     calc.log_likelihood()
-    calc.timing_totals(reset=True)
     calc.span_begin()
     for p in paths:
         calc.propose_lengths(*p, 1.0)
     dms = calc.span_end()
+    calc.set_timing(True)
+    calc.timing_totals(reset=True)
+    for p in paths:
+        calc.propose_lengths(*p, 1.0)
+    calc.log_likelihood()
     _, dprune, dn = calc.timing_totals(reset=True)
+    calc.set_timing(False)
     dbytes = sum(schedule.algorithmic_bytes(top, p[0], P, C, 4, w=4, e_b=4, w_p=4) for p in paths)
     mean_path = float(np.mean([len(p[0]) for p in paths]))
     calc.close()

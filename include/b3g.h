@@ -174,9 +174,12 @@ B3G_API b3g_status b3g_calculator_log_likelihood(b3g_calculator *calc,
 /* Per-pattern mixed log-likelihoods of the last proposal, [P].  Blocks. */
 B3G_API b3g_status b3g_calculator_site_log_likelihoods(b3g_calculator *calc,
 						       double *out);
+/* CUDA events around every evaluation, for the timing calls below (off by
+ * default: each costs a few microseconds of host time per evaluation). */
+B3G_API b3g_status b3g_calculator_set_timing(b3g_calculator *calc, int on);
 /* Device time of the last proposal in milliseconds, from CUDA events on the
  * calculator's stream: the transition-matrix kernel and the pruning kernel
- * (which includes the root reduction).  Blocks. */
+ * (which includes the root reduction).  Needs timing on.  Blocks. */
 B3G_API b3g_status b3g_calculator_last_timing(b3g_calculator *calc,
 					      float *transition_ms,
 					      float *prune_ms);

@@ -43,6 +43,7 @@ def make_pair(c, K, alpha):
 def test_short_lists_match_two_kernel_path_and_oracle(rng):
     c = dna_case(64, 3000, seed=91, model="gtr", alpha=0.5, num_categories=4, gaps=0.02)
     fused, two = make_pair(c, 4, 0.5)
+    fused.set_timing(True)
     tree = O.DatedTree(c.tree.parents, c.tree.heights)
     ref = O.GammaLikelihood(c.leaves, c.weights, tree, O.gtr(c.rates, c.pi), 4, 0.5)
     tree.mark_all_edges_updated()
