@@ -567,6 +567,7 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 				   cudaMemcpyHostToDevice, stream_),
 		   "upload step");
 	check_cuda(cudaEventRecord(ev_stage_free_, stream_), "event");
+	upload_pending_ = true;
 	TimingSlot &slot = ring_[ring_next_ % kRing];
 	if (slot.pending)
 		harvest(slot); // recorded kRing proposals ago: long complete
@@ -825,7 +826,7 @@ void Calculator::propose_matrices(const uint32_t *internals,
 	for (uint32_t s = 0; s < S_; ++s)
 		if (!std::isfinite(freqs[s]))
 			throw Error(B3G_ERR_NUMERIC, "non-finite frequency");
-	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	wait_stage();
 	stage_ops(internals, children, n);
 	std::memcpy(h_stage_ + off_pi_, freqs, S_ * sizeof(double));
 	std::memcpy(h_stage_ + off_in_, matrices, count * sizeof(double));
@@ -848,7 +849,7 @@ void Calculator::propose_lengths(const uint32_t *internals,
 			throw Error(B3G_ERR_NUMERIC, "non-finite edge length");
 	if (!std::isfinite(clock_rate))
 		throw Error(B3G_ERR_NUMERIC, "non-finite clock rate");
-	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	wait_stage();
 	if (batch_done_)
 		check_cuda(cudaEventSynchronize(batch_done_), "batch stage reuse");
 	stage_ops(internals, children, n);
@@ -882,7 +883,7 @@ void Calculator::stage_lengths(const uint32_t *internals,
 		throw Error(B3G_ERR_NUMERIC, "non-finite clock rate");
 	// the batch's previous copy of this staging buffer must be done, and
 	// so must this calculator's own last launch
-	check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+	wait_stage();
 	if (batch_done_)
 		check_cuda(cudaEventSynchronize(batch_done_), "batch stage reuse");
 	stage_ops(internals, children, n);
@@ -912,6 +913,7 @@ void Calculator::likelihoods(double *out)
 				     C_, cudaMemcpyDeviceToHost, stream_),
 		   "read likelihoods");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	upload_pending_ = false;
 }
 
 double Calculator::log_likelihood()
@@ -920,6 +922,7 @@ double Calculator::log_likelihood()
 	if (!have_result_)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	upload_pending_ = false;
 	if (h_status_ && *h_status_)
 		throw Error(B3G_ERR_TIMEOUT,
 			    "a tensor-core wait of the 20-state kernel gave up");
@@ -937,6 +940,19 @@ void Calculator::site_log_likelihoods(double *out)
 				   cudaMemcpyDeviceToHost, stream_),
 		   "read site lnl");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	upload_pending_ = false;
+}
+
+// The staging buffer may be rewritten once the last upload from it has
+// run: wait for that upload, unless the stream was synchronised since it
+// was queued (the common case: the result was read before the next
+// proposal).
+void Calculator::wait_stage()
+{
+	if (upload_pending_) {
+		check_cuda(cudaEventSynchronize(ev_stage_free_), "stage reuse");
+		upload_pending_ = false;
+	}
 }
 
 void Calculator::record(cudaEvent_t e)
@@ -1104,6 +1120,7 @@ void Calculator::set_weights(const uint32_t *w)
 	std::vector<uint32_t> padded(ldp_, 0);
 	std::memcpy(padded.data(), w, P_ * sizeof(uint32_t));
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
+	upload_pending_ = false;
 	check_cuda(cudaMemcpy(d_weights_, padded.data(), ldp_ * sizeof(uint32_t),
 			      cudaMemcpyHostToDevice),
 		   "upload weights");

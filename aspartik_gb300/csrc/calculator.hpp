@@ -88,6 +88,8 @@ class Calculator {
 	void launch(uint32_t n, bool matrices_mode, double clock_rate,
 		    bool want_cat);
 	void launch_direct(uint32_t n, double clock_rate);
+	void wait_stage();
+	bool upload_pending_ = false; // an upload from h_stage_ may be in flight
 	struct TimingSlot;
 	void launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		      bool want_cat, TimingSlot &slot);
