@@ -206,7 +206,7 @@ __device__ __forceinline__ void run_item2(const TileArgs &a,
 // the block synchronised.  s_dot/s_cnt hold tile * C entries, s_red 32;
 // rs the run walk's shared-memory extras.  The run walk reads each entry's
 // slot codes from NodeOp::pad of s_ops (0xFFFFFF: no slots).
-template <typename Idx>
+template <typename Idx, bool kPrefetch = false>
 __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			    int32_t *s_cnt, double *s_red,
 			    const NodeOp *s_ops, const uint32_t *s_runs,
@@ -260,7 +260,26 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 		float4 y0 = make_float4(0.f, 0.f, 0.f, 0.f), y1 = y0;
 		int32_t c0 = 0, c1 = 0;
 		uint32_t o0 = 0xFFFFFFFFu, o1 = 0xFFFFFFFFu;
-		auto input = [&](uint32_t id, const float4 *tb, float4 &v,
+		// A child that is neither a tip nor one of the two previous
+		// outputs is read from global memory (a clean subtree, usually
+		// not in L2).  With kPrefetch (the fused short-list kernel, whose
+		// registers allow it) its load for entry i + 1 is issued before
+		// entry i's product, so the latency overlaps the arithmetic: it is
+		// never entry i's or i-1's output, and any earlier output it may
+		// be was stored by this thread before the load.
+		float4 pf[2];
+		int32_t pfs[2];
+		auto fetch = [&](const NodeOp &op, uint32_t f0, uint32_t f1) {
+			const uint32_t ids[2] = {op.left, op.right};
+#pragma unroll
+			for (int j = 0; j < 2; ++j)
+				if (!(ids[j] & kTipBit) && ids[j] != f0 && ids[j] != f1) {
+					const Idx ix = (Idx)ids[j] * stride + col_off;
+					pf[j] = a.part[ix];
+					pfs[j] = a.scales[ix];
+				}
+		};
+		auto input = [&](uint32_t id, const float4 *tb, int j, float4 &v,
 				 int32_t &sc) {
 			if (id & kTipBit) {
 				v = tb[tips_p[(Idx)(id & ~kTipBit) * tip_row]];
@@ -271,20 +290,27 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			} else if (id == o1) {
 				v = v4_apply(tb, y1);
 				sc = c1;
+			} else if (kPrefetch) {
+				v = v4_apply(tb, pf[j]);
+				sc = pfs[j];
 			} else {
 				const Idx ix = (Idx)id * stride + col_off;
 				sc = a.scales[ix];
 				v = v4_apply(tb, a.part[ix]);
 			}
 		};
+		if (kPrefetch && a.n)
+			fetch(s_ops[0], o0, o1);
 		for (uint32_t i = 0; i < a.n; ++i) {
 			const NodeOp op = s_ops[i];
 			const float4 *tl = a.ptab + ((size_t)(2 * i) * C + c) * 5;
 			const float4 *tr = tl + 5 * C;
 			float4 ca, cb;
 			int32_t sa, sb;
-			input(op.left, tl, ca, sa);
-			input(op.right, tr, cb, sb);
+			input(op.left, tl, 0, ca, sa);
+			input(op.right, tr, 1, cb, sb);
+			if (kPrefetch && i + 1 < a.n) // forwards after this entry: op.out, o0
+				fetch(s_ops[i + 1], op.out, o0);
 			float4 y = v4_mul(ca, cb);
 			const int32_t cnt = sa + sb + rescale_pow2(y);
 			const Idx ox = (Idx)op.out * stride + col_off;
@@ -603,8 +629,8 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
 	const uint32_t ntiles = prm.ldp / kTile;
 	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const double tsum = tile_walk<Idx>(a, t, s_dot, s_cnt, s_red,
-						   prm.ops, nullptr, nullptr);
+		const double tsum = tile_walk<Idx, true>(a, t, s_dot, s_cnt, s_red,
+							 prm.ops, nullptr, nullptr);
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
 	}
