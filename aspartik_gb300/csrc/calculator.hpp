@@ -70,6 +70,20 @@ class Calculator {
 	float span_end();
 	uint64_t last_upload_bytes() const { return last_upload_bytes_; }
 	uint32_t last_launches() const { return last_launches_; }
+	// launch shape of the run walk (patterns per tile, threads per block),
+	// as the autotuner leaves it; a checkpoint restores it so that whole-
+	// tree sums keep their order
+	uint32_t runs_tile() const { return runs_tile_; }
+	uint32_t runs_block() const { return runs_block_; }
+	void set_runs_shape(uint32_t tile, uint32_t block)
+	{
+		if ((tile != 32 && tile != 64 && tile != 128) ||
+		    (block != 512 && block != 1024) || tile * C_ > 512 ||
+		    (block == 1024 && tile * C_ >= 512))
+			throw Error(B3G_ERR_INVALID_ARGUMENT, "no such run-walk shape");
+		runs_tile_ = tile;
+		runs_block_ = block;
+	}
 	uint32_t autotune(const uint32_t *internals, const uint32_t *children,
 			  uint32_t n, const double *lengths, double clock_rate);
 

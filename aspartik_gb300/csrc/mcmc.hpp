@@ -30,6 +30,16 @@ class Rng {
 	uint64_t next();
 	double uniform();            // [0, 1)
 	uint32_t below(uint32_t n);  // [0, n)
+	void get_state(uint64_t out[4]) const
+	{
+		for (int k = 0; k < 4; ++k)
+			out[k] = s_[k];
+	}
+	void set_state(const uint64_t in[4])
+	{
+		for (int k = 0; k < 4; ++k)
+			s_[k] = in[k];
+	}
 
       private:
 	uint64_t s_[4];
@@ -199,6 +209,11 @@ class Mcmc {
 	void chain_state(uint32_t chain, uint32_t *parents, double *heights,
 			 double *lnl, double *beta) const;
 	uint32_t num_chains() const { return (uint32_t)chains_.size(); }
+	// Checkpoint (mcmc_state.cpp): everything later steps depend on, between
+	// steps; load needs a driver built with the same configuration and
+	// data and continues bit for bit as the dumped run would have.
+	std::vector<uint8_t> dump() const;
+	void load(const uint8_t *state, size_t size);
 
       private:
 	void propose(Chain &ch);

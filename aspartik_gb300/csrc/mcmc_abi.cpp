@@ -212,6 +212,29 @@ B3G_API b3g_status b3g_mcmc_da_stats(b3g_mcmc *mcmc, uint64_t *counts,
 	});
 }
 
+B3G_API b3g_status b3g_mcmc_dump(b3g_mcmc *mcmc, uint8_t *out,
+				 uint64_t capacity, uint64_t *size)
+{
+	return guarded([&] {
+		if (!size)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null size");
+		const std::vector<uint8_t> state = mcmc_of(mcmc)->dump();
+		*size = state.size();
+		if (!out)
+			return;
+		if (capacity < state.size())
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "buffer smaller than the checkpoint");
+		std::memcpy(out, state.data(), state.size());
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_load(b3g_mcmc *mcmc, const uint8_t *state,
+				 uint64_t size)
+{
+	return guarded([&] { mcmc_of(mcmc)->load(state, (size_t)size); });
+}
+
 B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff)
 {
 	return guarded([&] {

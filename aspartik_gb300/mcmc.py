@@ -164,6 +164,22 @@ class Mcmc:
         out["train_loss"], out["drift_rms"] = values[0], values[1]
         return out
 
+    def dump(self) -> bytes:
+        """Checkpoint of the driver between runs (b3g_mcmc_dump)."""
+        size = ct.c_uint64()
+        check(lib.b3g_mcmc_dump(self._h, None, 0, ct.byref(size)))
+        buf = np.empty(size.value, dtype=np.uint8)
+        check(lib.b3g_mcmc_dump(self._h, nat.as_ptr(buf, ct.c_uint8), size.value,
+                                ct.byref(size)))
+        return buf.tobytes()
+
+    def load(self, state: bytes) -> None:
+        """Continue from a checkpoint of a driver with the same
+        configuration and data (b3g_mcmc_load); traces start empty."""
+        buf = np.frombuffer(state, dtype=np.uint8)
+        check(lib.b3g_mcmc_load(self._h, nat.as_ptr(np.ascontiguousarray(buf), ct.c_uint8),
+                                buf.size))
+
     def check(self) -> float:
         out = ct.c_double()
         check(lib.b3g_mcmc_check(self._h, ct.byref(out)))

@@ -412,6 +412,21 @@ B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
  * values = {final training loss, last drift RMS}. */
 B3G_API b3g_status b3g_mcmc_da_stats(b3g_mcmc *mcmc, uint64_t *counts,
 				     double *values);
+/* Checkpoint between runs (Mcmc::dump, mcmc.rs:251-268, in this driver's
+ * own layout): the chains' trees, parameters, relaxed-clock categories,
+ * cached likelihoods and priors, temperatures, RNG states and run-walk
+ * launch shapes, the step counter, swap counters and RNG, the operators'
+ * statistics and tuning.  b3g_mcmc_dump sets *size to the checkpoint's
+ * bytes and writes it to out when out is not null (capacity >= *size).
+ * b3g_mcmc_load takes a checkpoint into a driver created with the same
+ * configuration and data (and its parameters set): every chain is evaluated
+ * from scratch and checked against the saved likelihood, traces and samples
+ * start empty, and later runs continue exactly as the dumped driver's
+ * would.  Not for delayed-acceptance runs (B3G_ERR_STATE). */
+B3G_API b3g_status b3g_mcmc_dump(b3g_mcmc *mcmc, uint8_t *out,
+				 uint64_t capacity, uint64_t *size);
+B3G_API b3g_status b3g_mcmc_load(b3g_mcmc *mcmc, const uint8_t *state,
+				 uint64_t size);
 /* Re-evaluates every chain from scratch and returns the largest relative
  * difference to its incrementally maintained log-likelihood. */
 B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff);
