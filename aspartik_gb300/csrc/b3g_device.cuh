@@ -153,7 +153,7 @@ constexpr uint32_t kRunCap = 128;
 constexpr uint32_t kPtabSmemBytes = 32u * 1024u;
 
 // Fused single-launch evaluation of a short list (FP32 chosen form, four
-// states, four categories): the schedule, the edge lengths and the root
+// states, one, two or four categories): the schedule, the edge lengths and the root
 // frequencies travel in the kernel parameters, so the launch needs no
 // upload, no transition kernel and no read-back copy.
 constexpr uint32_t kDirectMax = 48; // entries
@@ -168,7 +168,7 @@ struct DirectParams {
 	unsigned *ticket;   // zero between launches
 	double *lnl_out;    // device copy of the result
 	double *lnl_host;   // host-mapped pinned word, written by the last block
-	uint32_t n, ldp, L, pad0;
+	uint32_t n, ldp, L, C; // C: 1, 2 or 4 categories
 	double clock_rate;
 	double log_inv_c;
 	double pi[4];

@@ -127,7 +127,7 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	use_tc20_ = f32_ && S_ == 20;
 	if (const char *env = std::getenv("B3G_TC20"))
 		use_tc20_ = use_tc20_ && std::atoi(env) != 0;
-	use_direct_ = f32_ && S_ == 4 && C_ == 4;
+	use_direct_ = f32_ && S_ == 4 && (C_ == 1 || C_ == 2 || C_ == 4);
 	if (const char *env = std::getenv("B3G_DIRECT"))
 		use_direct_ = use_direct_ && std::atoi(env) != 0;
 
@@ -775,7 +775,7 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	dp.n = n;
 	dp.ldp = ldp_;
 	dp.L = L_;
-	dp.pad0 = 0;
+	dp.C = C_;
 	dp.clock_rate = clock_rate;
 	dp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 	std::memcpy(dp.pi, h_stage_ + off_pi_, 4 * sizeof(double));
@@ -799,7 +799,8 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 		harvest(slot);
 	slot.direct = true;
 	record(slot.k0);
-	const uint32_t ctas = std::min(ldp_ / 128u, 2 * num_sms_);
+	// 128-pattern tiles, 128 * C threads per block, 1024 threads per SM
+	const uint32_t ctas = std::min(ldp_ / 128u, (8u / C_) * num_sms_);
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
 	last_launches_ = 1;
 	record(slot.k1);

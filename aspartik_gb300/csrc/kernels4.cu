@@ -898,13 +898,27 @@ cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s)
 cudaError_t launch_prune4_direct(const DirectParams &p, uint32_t ctas,
 				 cudaStream_t s)
 {
-	if (p.n == 0 || p.n > kDirectMax || p.ldp % 128u)
+	if (p.n == 0 || p.n > kDirectMax || p.ldp % 128u ||
+	    (p.C != 1 && p.C != 2 && p.C != 4))
 		return cudaErrorInvalidValue;
-	const bool narrow = (uint64_t)p.L * 2 * 4 * p.ldp < (1ull << 31);
-	if (narrow)
-		prune4_direct_kernel<uint32_t><<<ctas, 512, 0, s>>>(p);
-	else
-		prune4_direct_kernel<size_t><<<ctas, 512, 0, s>>>(p);
+	const bool narrow = (uint64_t)p.L * 2 * p.C * p.ldp < (1ull << 31);
+	const uint32_t threads = 128 * p.C;
+	if (p.C == 4) {
+		if (narrow)
+			prune4_direct_kernel<uint32_t, 4><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_kernel<size_t, 4><<<ctas, threads, 0, s>>>(p);
+	} else if (p.C == 2) {
+		if (narrow)
+			prune4_direct_kernel<uint32_t, 2><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_kernel<size_t, 2><<<ctas, threads, 0, s>>>(p);
+	} else {
+		if (narrow)
+			prune4_direct_kernel<uint32_t, 1><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_kernel<size_t, 1><<<ctas, threads, 0, s>>>(p);
+	}
 	return cudaGetLastError();
 }
 

@@ -568,18 +568,19 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 }
 
 // ---------------------------------------------------------------------------
-// Fused evaluation of a short list in one launch (FP32, four states, four
-// categories, 128-pattern tiles: one thread per column, serial walk).  Every
+// Fused evaluation of a short list in one launch (FP32, four states, kC =
+// 1, 2 or 4 categories, 128-pattern tiles: one thread per column, serial
+// walk).  Every
 // block converts the device eigensystem to FP32, builds the list's
 // transition tables in shared memory with the same arithmetic as the
 // transition kernels (so results match a two-kernel evaluation bit for
 // bit), walks its tiles, and the last block writes the root lnL to the
 // device and to the host-mapped word.
-template <typename Idx>
-__global__ void __launch_bounds__(512, 2)
+template <typename Idx, uint32_t kC>
+__global__ void __launch_bounds__(128 * kC, 8 / kC)
 prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 {
-	constexpr uint32_t kC = 4, kTile = 128, kCols = kTile * kC;
+	constexpr uint32_t kTile = 128, kCols = kTile * kC;
 	__shared__ float4 s_tab[kDirectMax * 2 * kC * 5];
 	__shared__ float s_eig[37];
 	__shared__ double s_rate[kC];
@@ -592,7 +593,7 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	// from the parameters: no global-memory round trip before the tables
 	if (tid < 37)
 		s_eig[tid] = prm.eig[tid];
-	else if (tid < 41)
+	else if (tid < 37 + kC)
 		s_rate[tid - 37] = prm.rate[tid - 37];
 	__syncthreads();
 	if (tid < prm.n * 2 * kC) {

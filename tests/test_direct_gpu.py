@@ -40,12 +40,13 @@ def make_pair(c, K, alpha):
     return fused, two
 
 
-def test_short_lists_match_two_kernel_path_and_oracle(rng):
-    c = dna_case(64, 3000, seed=91, model="gtr", alpha=0.5, num_categories=4, gaps=0.02)
-    fused, two = make_pair(c, 4, 0.5)
+@pytest.mark.parametrize("K", [4, 2, 1])
+def test_short_lists_match_two_kernel_path_and_oracle(rng, K):
+    c = dna_case(64, 3000, seed=91, model="gtr", alpha=0.5, num_categories=K, gaps=0.02)
+    fused, two = make_pair(c, K, 0.5)
     fused.set_timing(True)
     tree = O.DatedTree(c.tree.parents, c.tree.heights)
-    ref = O.GammaLikelihood(c.leaves, c.weights, tree, O.gtr(c.rates, c.pi), 4, 0.5)
+    ref = O.GammaLikelihood(c.leaves, c.weights, tree, O.gtr(c.rates, c.pi), K, 0.5)
     tree.mark_all_edges_updated()
     for g in (fused, two):  # 63 entries: both take the two-kernel path
         g.propose_lengths(*lists_and_lengths(tree), 1.0)
