@@ -15,10 +15,12 @@ numpy FP64:
   - Gamma categories mix by log-sum-exp plus ln(1/K) and the patterns are
     weighted (gamma.rs:97-169, likelihood/mod.rs:134-151).
 
-Parity status: parity unpinned against outputs of the reference itself (the
-reference has no 20-state calculator; its GenericSubstitution is not used
-by one).  Pinned here against the 4-state restatement (the S = 4 case must
-agree with cpu4), the JC-20 closed form and brute-force enumeration.
+Parity status: for S = 20 unpinned against outputs of the reference itself
+(the reference has no 20-state calculator; its GenericSubstitution is not
+used by one).  Pinned here against the 4-state restatement (the S = 4 case
+must agree with cpu4, which in turn reproduces the reference's own FP64 CUDA
+kernel, tests/test_ref_golden.py), the JC-20 closed form and brute-force
+enumeration.
 """
 
 from __future__ import annotations

@@ -14,10 +14,18 @@ in Python the host-side orchestration around it:
 * ``GammaLikelihood`` likelihood/gamma.rs:20-225
 * substitution models JC, K80, HKY, GTR (substitution.rs:102-604)
 
-Parity status: parity unpinned against values produced by the reference
-itself (its Rust workspace cannot be built here and its trace data is
-absent); pinned against closed forms, scipy's expm, scipy's gammaincinv and
-brute-force enumeration (oracle/brute.py).
+Parity status: pinned against values produced by the reference itself.
+The reference's Rust CPU pruner cannot be built here (no Rust toolchain,
+an un-vendored git dependency), but its FP64 CUDA pruning kernel
+(crates/b3/src/calculator/cuda_partials/kernels.cu) is compiled from the
+reference tree into oracle/_ref (oracle/build.py::build_ref) and run on a
+GB300 (oracle/ref_cuda.py): its per-pattern log-likelihoods, stored with
+their inputs in tests/golden/ref_cuda_partials.npz, are reproduced by this
+restatement to 1e-12 relative (tests/test_ref_golden.py; the live kernel
+in tests/test_reference_cuda_gpu.py).  Also pinned against closed forms,
+scipy's expm, scipy's gammaincinv and brute-force enumeration
+(oracle/brute.py); the Gamma quantile of the reference's un-vendored
+computare-distributions stays unpinned (scipy stands in for it).
 """
 
 from __future__ import annotations

@@ -1,9 +1,8 @@
 """Generates tests/golden/small_trees.npz.
 
-No reference-produced likelihood exists for this path (the reference's trace
-tests read a data submodule that is absent and its Rust workspace cannot be
-built), so the golden vectors are ground truth computed independently of any
-pruning code: brute-force enumeration of internal states with P(t) from
+These golden vectors are ground truth computed independently of any pruning
+code (values produced by the reference itself, by its FP64 CUDA kernel, are
+in ref_cuda_partials.npz, made by make_ref_cuda_golden.py): brute-force enumeration of internal states with P(t) from
 scipy's matrix exponential, summed in longdouble (oracle/brute.py).  Inputs
 are seeded and small enough to regenerate in seconds.
 
