@@ -53,6 +53,11 @@ def _lib():
             "cuMemcpyDtoH_v2": [vp, u64, sz],
             "cuLaunchKernel": [vp, u, u, u, u, u, u, u, vp, ct.POINTER(vp), ct.POINTER(vp)],
             "cuGetErrorString": [i, ct.POINTER(ct.c_char_p)],
+            "cuEventCreate": [ct.POINTER(vp), u],
+            "cuEventRecord": [vp, vp],
+            "cuEventSynchronize": [vp],
+            "cuEventElapsedTime": [ct.POINTER(ct.c_float), vp, vp],
+            "cuEventDestroy_v2": [vp],
         }
         for name, args in sig.items():
             f = getattr(cu, name)
@@ -106,6 +111,7 @@ class RefCudaPartials:
 
     def close(self) -> None:
         cu = _lib()
+        self.free()
         if getattr(self, "mod", None):
             cu.cuModuleUnload(self.mod)
             self.mod = None
@@ -123,16 +129,50 @@ class RefCudaPartials:
         _check(cu.cuMemcpyHtoD_v2(ptr, buf.ctypes.data_as(ct.c_void_p), size.value),
                f"set {name}")
 
-    def likelihoods(self, ref_leaves: np.ndarray, internals, children, matrices,
-                    frequencies, scale_ln: int = 30) -> np.ndarray:
-        """Per-pattern lnL of one full evaluation.  ref_leaves [L][P] codes
-        0..4; internals [n]; children [n][2]; matrices [n][2][4][4] (P row
-        i, column j = Prob(i -> j)); frequencies [4]."""
+    def setup(self, ref_leaves: np.ndarray, scale_ln: int = 30) -> None:
+        """Device buffers of one calculator (as CudaPartialsCalculator::new,
+        cuda_partials/mod.rs:171-270) for tip codes ref_leaves [L][P]."""
         cu = _lib()
         _check(cu.cuCtxSetCurrent(self.ctx), "cuCtxSetCurrent")
+        self.free()
         leaves = np.ascontiguousarray(ref_leaves, dtype=np.uint8)
         L, P = leaves.shape
         I = L - 1
+        self.L, self.P, self.scale_ln = L, P, int(scale_ln)
+        self.bufs = {}
+
+        def alloc(name, nbytes, host=None):
+            ptr = ct.c_uint64()
+            _check(cu.cuMemAlloc_v2(ct.byref(ptr), max(int(nbytes), 1)), f"alloc {name}")
+            self.bufs[name] = ptr
+            if host is None:
+                _check(cu.cuMemsetD8_v2(ptr, 0, max(int(nbytes), 1)), f"zero {name}")
+            else:
+                _check(cu.cuMemcpyHtoD_v2(ptr, host.ctypes.data_as(ct.c_void_p), host.nbytes),
+                       f"upload {name}")
+
+        alloc("leaves", leaves.nbytes, leaves)
+        alloc("partials", I * 2 * P * 32)
+        alloc("scales", I * 2 * P)
+        alloc("scale_sums", P * 4)
+        alloc("selectors", I)
+        alloc("internals", I * 4)
+        alloc("children", I * 8)
+        alloc("transitions", I * 2 * 16 * 8)
+        alloc("likelihoods", P * 8)
+
+    def free(self) -> None:
+        cu = _lib()
+        for ptr in getattr(self, "bufs", {}).values():
+            cu.cuMemFree_v2(ptr)
+        self.bufs = {}
+
+    def propose(self, internals, children, matrices, frequencies) -> None:
+        """One launch over the list (asynchronous), from zeroed scale state:
+        internals [n], children [n][2], matrices [n][2][4][4], frequencies [4]."""
+        cu = _lib()
+        _check(cu.cuCtxSetCurrent(self.ctx), "cuCtxSetCurrent")
+        L, P, I = self.L, self.P, self.L - 1
         internals = np.ascontiguousarray(internals, dtype=np.uint32)
         children = np.ascontiguousarray(children, dtype=np.uint32).reshape(-1)
         n = internals.size
@@ -143,48 +183,67 @@ class RefCudaPartials:
             raise ValueError("node ids out of range")
         self._set_const("ref_num_patterns", int(P))
         self._set_const("ref_num_leaves", int(L))
-        self._set_const("ref_scale_ln", int(scale_ln))
-        self._set_const("ref_scale_threshold", float(np.exp(-float(scale_ln))))
-        self._set_const("ref_scale_mult", float(np.exp(float(scale_ln))))
+        self._set_const("ref_scale_ln", self.scale_ln)
+        self._set_const("ref_scale_threshold", float(np.exp(-float(self.scale_ln))))
+        self._set_const("ref_scale_mult", float(np.exp(float(self.scale_ln))))
+        b = self.bufs
+        _check(cu.cuMemsetD8_v2(b["scales"], 0, I * 2 * P), "zero scales")
+        _check(cu.cuMemsetD8_v2(b["scale_sums"], 0, P * 4), "zero scale sums")
+        for name, arr in (("internals", internals), ("children", children),
+                          ("transitions", mats)):
+            _check(cu.cuMemcpyHtoD_v2(b[name], arr.ctypes.data_as(ct.c_void_p), arr.nbytes),
+                   f"upload {name}")
+        self._freqs = np.ascontiguousarray(frequencies, dtype=np.float64)
+        self._n = ct.c_uint32(n)
+        args = [b["leaves"], b["partials"], b["scales"], b["scale_sums"], b["selectors"],
+                self._n, b["internals"], b["children"], b["transitions"], b["likelihoods"]]
+        ptrs = [ct.c_void_p(ct.addressof(a)) for a in args]
+        ptrs.append(ct.c_void_p(self._freqs.ctypes.data))
+        self._params = (ct.c_void_p * len(ptrs))(*ptrs)
+        grid = (P + BLOCK - 1) // BLOCK
+        _check(cu.cuLaunchKernel(self.fn, grid, 1, 1, BLOCK, 1, 1, 0, None, self._params, None),
+               "launch")
 
-        bufs = {}
-
-        def alloc(name, nbytes, host=None):
-            p = ct.c_uint64()
-            _check(cu.cuMemAlloc_v2(ct.byref(p), max(int(nbytes), 1)), f"alloc {name}")
-            bufs[name] = p
-            if host is None:
-                _check(cu.cuMemsetD8_v2(p, 0, max(int(nbytes), 1)), f"zero {name}")
-            else:
-                _check(cu.cuMemcpyHtoD_v2(p, host.ctypes.data_as(ct.c_void_p), host.nbytes),
-                       f"upload {name}")
-            return p
-
+    def time_launch(self, reps: int) -> float:
+        """Device milliseconds per launch of the last proposal's kernel,
+        relaunched `reps` times with the same arguments between two events
+        (every launch does the same work)."""
+        cu = _lib()
+        e0, e1 = ct.c_void_p(), ct.c_void_p()
+        _check(cu.cuEventCreate(ct.byref(e0), 0), "event")
+        _check(cu.cuEventCreate(ct.byref(e1), 0), "event")
         try:
-            d_leaves = alloc("leaves", leaves.nbytes, leaves)
-            d_partials = alloc("partials", I * 2 * P * 32)
-            d_scales = alloc("scales", I * 2 * P)
-            d_sums = alloc("scale_sums", P * 4)
-            d_sel = alloc("selectors", I)
-            d_int = alloc("internals", internals.nbytes, internals)
-            d_ch = alloc("children", children.nbytes, children)
-            d_tr = alloc("transitions", mats.nbytes, mats)
-            d_out = alloc("likelihoods", P * 8)
-            freqs = np.ascontiguousarray(frequencies, dtype=np.float64)
-            n_arg = ct.c_uint32(n)
-            args = [d_leaves, d_partials, d_scales, d_sums, d_sel, n_arg, d_int, d_ch, d_tr,
-                    d_out]
-            ptrs = [ct.c_void_p(ct.addressof(a)) for a in args]
-            ptrs.append(ct.c_void_p(freqs.ctypes.data))
-            params = (ct.c_void_p * len(ptrs))(*ptrs)
-            grid = (P + BLOCK - 1) // BLOCK
-            _check(cu.cuLaunchKernel(self.fn, grid, 1, 1, BLOCK, 1, 1, 0, None, params, None),
-                   "launch")
-            _check(cu.cuCtxSynchronize(), "synchronize")
-            out = np.empty(P, dtype=np.float64)
-            _check(cu.cuMemcpyDtoH_v2(out.ctypes.data_as(ct.c_void_p), d_out, out.nbytes),
-                   "download")
-            return out
+            grid = (self.P + BLOCK - 1) // BLOCK
+            _check(cu.cuEventRecord(e0, None), "record")
+            for _ in range(reps):
+                _check(cu.cuLaunchKernel(self.fn, grid, 1, 1, BLOCK, 1, 1, 0, None,
+                                         self._params, None), "launch")
+            _check(cu.cuEventRecord(e1, None), "record")
+            _check(cu.cuEventSynchronize(e1), "event sync")
+            ms = ct.c_float()
+            _check(cu.cuEventElapsedTime(ct.byref(ms), e0, e1), "elapsed")
+            return ms.value / reps
         finally:
-            for p in bufs.values():
-                cu.cuMemFree_v2(p)
+            cu.cuEventDestroy_v2(e0)
+            cu.cuEventDestroy_v2(e1)
+
+    def synchronize(self) -> None:
+        _check(_lib().cuCtxSynchronize(), "synchronize")
+
+    def result(self) -> np.ndarray:
+        """Per-pattern lnL of the last proposal (waits for it)."""
+        self.synchronize()
+        out = np.empty(self.P, dtype=np.float64)
+        _check(_lib().cuMemcpyDtoH_v2(out.ctypes.data_as(ct.c_void_p), self.bufs["likelihoods"],
+                                      out.nbytes), "download")
+        return out
+
+    def likelihoods(self, ref_leaves: np.ndarray, internals, children, matrices,
+                    frequencies, scale_ln: int = 30) -> np.ndarray:
+        """Per-pattern lnL of one full evaluation on fresh buffers."""
+        self.setup(ref_leaves, scale_ln)
+        try:
+            self.propose(internals, children, matrices, frequencies)
+            return self.result()
+        finally:
+            self.free()
