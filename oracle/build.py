@@ -6,9 +6,11 @@ timed CPU baseline; nothing in the product links or loads it.
 The reference's Rust workspace cannot be compiled here (no Rust toolchain,
 and its git dependency ``computare`` is not vendored), so the restatement
 stands in for its CPU pruner.  Its FP64 CUDA pruning kernel, however, is a
-self-contained CUDA source: ``build_ref()`` compiles it (through the wrapper
-``ref_cuda_partials.cu``) into ``oracle/_ref/ref_partials.cubin`` when the
-reference tree is present, and the tests run it beside the oracle.
+self-contained CUDA source, and so are the kernels of its default GPU
+calculator (cuda_propagations): ``build_ref()`` compiles both (through the
+wrappers ``ref_cuda_partials.cu`` and ``ref_cuda_propagations.cu``) into
+``oracle/_ref/`` when the reference tree is present, and the tests run them
+beside the oracle.
 """
 
 from __future__ import annotations
@@ -41,31 +43,43 @@ def build(verbose: bool = False) -> Path:
 
 # the reference tree, read only at build time in the development container;
 # the GPU machine receives the built cubin
-REF_PARTIALS = Path("/root/reference/crates/b3/src/calculator/cuda_partials")
-REF_WRAPPER = HERE / "ref_cuda_partials.cu"
-REF_CUBIN = HERE / "_ref" / "ref_partials.cubin"
+REF_CALC = Path("/root/reference/crates/b3/src/calculator")
+# (reference source directory, wrapper, output): the two CUDA calculators
+REF_BUILDS = [
+    (REF_CALC / "cuda_partials", HERE / "ref_cuda_partials.cu",
+     HERE / "_ref" / "ref_partials.cubin"),
+    (REF_CALC / "cuda_propagations", HERE / "ref_cuda_propagations.cu",
+     HERE / "_ref" / "ref_propagations.cubin"),
+]
+REF_CUBIN = REF_BUILDS[0][2]
 
 
-def build_ref(verbose: bool = False) -> Path | None:
-    """Compile the reference's cuda_partials kernel for sm_103a into
-    ``oracle/_ref/`` (None when the reference sources are absent: the
-    prebuilt cubin, if any, is used as it is)."""
-    srcs = [REF_PARTIALS / "kernels.cu", REF_PARTIALS / "typedefs.h"]
-    if not all(p.exists() for p in srcs):
-        return REF_CUBIN if REF_CUBIN.exists() else None
-    deps = srcs + [REF_WRAPPER]
-    if REF_CUBIN.exists() and REF_CUBIN.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
-        return REF_CUBIN
+def build_ref(verbose: bool = False) -> list[Path]:
+    """Compile the reference's CUDA calculator kernels for sm_103a into
+    ``oracle/_ref/``; where the reference sources are absent the prebuilt
+    cubins, if any, are used as they are.  Returns the cubins present."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    REF_CUBIN.parent.mkdir(exist_ok=True)
-    cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-           f"-I{REF_PARTIALS}", str(REF_WRAPPER), "-o", str(REF_CUBIN)]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"reference kernel build failed:\n{res.stdout}\n{res.stderr}")
-    if verbose:
-        print(f"built {REF_CUBIN}")
-    return REF_CUBIN
+    out = []
+    for src_dir, wrapper, cubin in REF_BUILDS:
+        srcs = [src_dir / "kernels.cu", src_dir / "typedefs.h"]
+        if not all(p.exists() for p in srcs):
+            if cubin.exists():
+                out.append(cubin)
+            continue
+        deps = srcs + [wrapper]
+        if not (cubin.exists() and
+                cubin.stat().st_mtime >= max(p.stat().st_mtime for p in deps)):
+            cubin.parent.mkdir(exist_ok=True)
+            cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                   f"-I{src_dir}", str(wrapper), "-o", str(cubin)]
+            res = subprocess.run(cmd, capture_output=True, text=True)
+            if res.returncode != 0:
+                raise RuntimeError(f"reference kernel build failed:\n{res.stdout}\n"
+                                   f"{res.stderr}")
+            if verbose:
+                print(f"built {cubin}")
+        out.append(cubin)
+    return out
 
 
 if __name__ == "__main__":

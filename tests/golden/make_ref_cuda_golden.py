@@ -1,6 +1,6 @@
 """Generates tests/golden/ref_cuda_partials.npz: outputs of the reference's
-own FP64 CUDA pruning kernel (crates/b3/src/calculator/cuda_partials/
-kernels.cu, built into oracle/_ref/ref_partials.cubin by
+own FP64 CUDA calculators (crates/b3/src/calculator/cuda_partials/
+kernels.cu and cuda_propagations/kernels.cu, built into oracle/_ref/ by
 oracle/build.py::build_ref) on seeded inputs, stored with those inputs so
 that the CPU tests can pin the oracle to them without a GPU.
 
@@ -34,6 +34,19 @@ CASES = [
 ]
 
 
+def propagation_inputs(tree, model, rate, L):
+    """The lists of the reference's propagations calculator for a full
+    evaluation (tree.rs:436-454): every leaf, then the internals
+    children-first with the root last; the children of those internals; P
+    of the edge above every node but the root."""
+    t = O.DatedTree(tree.parents, tree.heights)
+    t.mark_all_edges_updated()
+    internals, children = t.partials_lists()
+    nodes = np.concatenate([np.arange(L, dtype=np.uint32), np.asarray(internals, np.uint32)])
+    mats = np.array([model.transition(t.edge_length(int(v)) * rate) for v in nodes[:-1]])
+    return nodes, L, np.asarray(children, np.uint32), mats
+
+
 def inputs(case):
     _, L, N, model_name, seed, rh, gaps, amb, rate, scale_ln = case
     c = dna_case(L, N, seed=seed, model=model_name, root_height=rh, gaps=gaps, ambiguous=amb)
@@ -43,24 +56,32 @@ def inputs(case):
     internals, children = t.partials_lists()
     lengths = np.array([[t.edge_length(int(a)), t.edge_length(int(b))] for a, b in children])
     mats = np.array([[model.transition(d * rate) for d in pair] for pair in lengths])
-    return c.leaves, np.asarray(internals), np.asarray(children), mats, model.pi, scale_ln
+    prop = propagation_inputs(c.tree, model, rate, L)
+    return c.leaves, np.asarray(internals), np.asarray(children), mats, model.pi, scale_ln, prop
 
 
 def main(out: str = OUT) -> None:
     ref = ref_cuda.RefCudaPartials(0)
+    prop = ref_cuda.RefCudaPropagations(0)
     arrays = {}
     try:
         for case in CASES:
             name = case[0]
-            leaves, internals, children, mats, pi, scale_ln = inputs(case)
+            leaves, internals, children, mats, pi, scale_ln, pin = inputs(case)
             lnl = ref.likelihoods(ref_cuda.dna_codes_to_ref(leaves), internals, children, mats,
                                   pi, scale_ln)
+            nodes, k, pch, pmats = pin
+            prop.setup(leaves, scale_ln)
+            prop.propose(nodes, k, pch, pmats, pi)
+            lnl_prop = prop.result()
+            prop.free()
             arrays.update({f"{name}/leaves": leaves, f"{name}/internals": internals,
                            f"{name}/children": children, f"{name}/matrices": mats,
                            f"{name}/frequencies": pi, f"{name}/scale_ln": np.int64(scale_ln),
-                           f"{name}/site_lnl": lnl})
+                           f"{name}/site_lnl": lnl, f"{name}/site_lnl_propagations": lnl_prop})
     finally:
         ref.close()
+        prop.close()
     np.savez_compressed(out, **arrays)
     print(f"wrote {out}")
 

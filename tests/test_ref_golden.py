@@ -1,7 +1,7 @@
 """The CPU oracle pinned to the reference itself: per-pattern log-likelihoods
-that the reference's own FP64 CUDA pruning kernel (crates/b3/src/
-calculator/cuda_partials/kernels.cu, compiled from the reference tree) wrote
-on a GB300, stored with their inputs in tests/golden/ref_cuda_partials.npz
+that the reference's own FP64 CUDA calculators (crates/b3/src/calculator/
+cuda_partials/kernels.cu and cuda_propagations/kernels.cu, compiled from
+the reference tree) wrote on a GB300, stored with their inputs in tests/golden/ref_cuda_partials.npz
 by tests/golden/make_ref_cuda_golden.py.  The oracle's restatement of
 cpu4.rs must give the same values from the same inputs (FP64, 1e-12
 relative: the two differ only in the compiler's contraction of the dot
@@ -34,6 +34,10 @@ def test_oracle_reproduces_reference_kernel(name):
     want = g[f"{name}/site_lnl"]
     assert np.isfinite(want).all()
     np.testing.assert_allclose(got, want, rtol=1e-12, atol=0.0)
+    # the reference's default GPU calculator (propagations), same inputs
+    if f"{name}/site_lnl_propagations" in g.files:
+        np.testing.assert_allclose(got, g[f"{name}/site_lnl_propagations"], rtol=1e-12,
+                                   atol=0.0)
 
 
 def test_fixture_inputs_regenerate_here():
@@ -47,7 +51,7 @@ def test_fixture_inputs_regenerate_here():
 
     g = np.load(GOLDEN)
     for case in CASES:
-        leaves, internals, children, mats, pi, _ = inputs(case)
+        leaves, internals, children, mats, pi, _, _ = inputs(case)
         name = case[0]
         assert np.array_equal(leaves, g[f"{name}/leaves"]), name
         assert np.array_equal(internals, g[f"{name}/internals"]), name

@@ -1,6 +1,6 @@
-"""The reference's own FP64 CUDA pruning kernel (crates/b3/src/calculator/
-cuda_partials/kernels.cu, compiled from the reference tree into
-oracle/_ref/ref_partials.cubin) run beside the CPU oracle and this
+"""The reference's own FP64 CUDA calculators (crates/b3/src/calculator/
+cuda_partials/kernels.cu and cuda_propagations/kernels.cu, compiled from the
+reference tree into oracle/_ref/) run beside the CPU oracle and this
 library's FP64 calculator on the same inputs: per-pattern log-likelihoods
 of full evaluations with the calculator-level interface (given transition
 matrices, cpu4.rs:39-76 / cuda_partials/mod.rs:63-100), over tip codes with
@@ -61,6 +61,23 @@ def test_reference_kernel_matches_oracle_and_library(ref, case):
 
     assert np.isfinite(want_ref).all()
     np.testing.assert_allclose(oracle, want_ref, rtol=1e-12, atol=0.0)
+    # the reference's default GPU calculator (propagations) on the same inputs
+    import sys
+
+    sys.path.insert(0, "tests/golden")
+    from make_ref_cuda_golden import propagation_inputs
+    from oracle import ref_cuda
+
+    if ref_cuda.propagations_available():
+        prop = ref_cuda.RefCudaPropagations(0)
+        try:
+            prop.setup(c.leaves, scale_ln)
+            nodes, k, pch, pmats = propagation_inputs(c.tree, model, rate, L)
+            prop.propose(nodes, k, pch, pmats, model.pi)
+            got_prop = prop.result()
+        finally:
+            prop.close()
+        np.testing.assert_allclose(oracle, got_prop, rtol=1e-12, atol=0.0)
     np.testing.assert_allclose(mine, want_ref, rtol=1e-12, atol=0.0)
     # and the weighted sums
     w = c.weights.astype(np.float64)
