@@ -16,12 +16,13 @@ in Python the host-side orchestration around it:
 
 Parity status: pinned against values produced by the reference itself.
 The reference's Rust CPU pruner cannot be built here (no Rust toolchain,
-an un-vendored git dependency), but its FP64 CUDA pruning kernel
-(crates/b3/src/calculator/cuda_partials/kernels.cu) is compiled from the
-reference tree into oracle/_ref (oracle/build.py::build_ref) and run on a
-GB300 (oracle/ref_cuda.py): its per-pattern log-likelihoods, stored with
-their inputs in tests/golden/ref_cuda_partials.npz, are reproduced by this
-restatement to 1e-12 relative (tests/test_ref_golden.py; the live kernel
+an un-vendored git dependency), but the kernels of its two FP64 CUDA
+calculators (crates/b3/src/calculator/cuda_partials/kernels.cu and
+cuda_propagations/kernels.cu) are compiled from the reference tree into
+oracle/_ref (oracle/build.py::build_ref) and run on a GB300
+(oracle/ref_cuda.py): their per-pattern log-likelihoods, stored with their
+inputs in tests/golden/ref_cuda_partials.npz, are reproduced by this
+restatement to 1e-12 relative (tests/test_ref_golden.py; the live kernels
 in tests/test_reference_cuda_gpu.py).  Also pinned against closed forms,
 scipy's expm, scipy's gammaincinv and brute-force enumeration
 (oracle/brute.py); the Gamma quantile of the reference's un-vendored
