@@ -639,10 +639,13 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 		const uint32_t ctas = std::min(tiles, num_sms_ * (1024 / block));
 		// the result also goes straight to the mapped host word
 		pp.lnl_host = d_lnl_host_;
+		arm_poll();
 		check_cuda(launch_prune4_runs(pp, ctas, block, stream_), "pruning kernel");
 	} else {
+		poll_result_ = false;
 		check_cuda(launch_prune4(pp, f32_, tile_, stream_), "pruning kernel");
 	}
+	++in_flight_;
 	record(slot.k1);
 	slot.pending = timing_;
 	ring_next_ += timing_ ? 1 : 0;
@@ -660,6 +663,8 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 			  bool want_cat, TimingSlot &slot)
 {
+	poll_result_ = false; // result read back by a copy after the kernels
+	++in_flight_;
 	PtabParams pt{};
 	pt.lengths = matrices_mode
 			     ? nullptr
@@ -801,7 +806,9 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	record(slot.k0);
 	// 128-pattern tiles, 128 * C threads per block, 1024 threads per SM
 	const uint32_t ctas = std::min(ldp_ / 128u, (8u / C_) * num_sms_);
+	arm_poll();
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
+	++in_flight_;
 	last_launches_ = 1;
 	record(slot.k1);
 	slot.pending = timing_;
@@ -915,6 +922,46 @@ void Calculator::likelihoods(double *out)
 		   "read likelihoods");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 	upload_pending_ = false;
+	in_flight_ = 0;
+}
+
+namespace {
+// a NaN payload the kernels never write
+constexpr uint64_t kLnlSentinel = 0x7ff4b3a9c0de5e11ull;
+} // namespace
+
+void Calculator::arm_poll()
+{
+	poll_result_ = in_flight_ == 0;
+	if (poll_result_)
+		std::memcpy(h_lnl_, &kLnlSentinel, sizeof(double));
+}
+
+// Waits for the mapped result word to leave the sentinel; every 64 polls
+// the stream is queried, so a launch error surfaces and a stream that
+// finished without writing the word ends the wait (false: synchronise).
+bool Calculator::wait_mapped(double &value)
+{
+	const volatile uint64_t *w = reinterpret_cast<const volatile uint64_t *>(h_lnl_);
+	for (uint32_t k = 1;; ++k) {
+		uint64_t bits = *w;
+		if (bits != kLnlSentinel) {
+			std::memcpy(&value, &bits, sizeof(double));
+			return true;
+		}
+		if ((k & 63u) == 0) {
+			const cudaError_t e = cudaStreamQuery(stream_);
+			if (e == cudaSuccess) {
+				bits = *w;
+				if (bits == kLnlSentinel)
+					return false;
+				std::memcpy(&value, &bits, sizeof(double));
+				return true;
+			}
+			if (e != cudaErrorNotReady)
+				check_cuda(e, "evaluation");
+		}
+	}
 }
 
 double Calculator::log_likelihood()
@@ -922,8 +969,16 @@ double Calculator::log_likelihood()
 	DeviceGuard g(device_);
 	if (!have_result_)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
+	double value;
+	if (poll_result_ && wait_mapped(value)) {
+		// the kernel ran, so the upload before it did too
+		upload_pending_ = false;
+		in_flight_ = 0;
+		return value;
+	}
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 	upload_pending_ = false;
+	in_flight_ = 0;
 	if (h_status_ && *h_status_)
 		throw Error(B3G_ERR_TIMEOUT,
 			    "a tensor-core wait of the 20-state kernel gave up");
@@ -942,6 +997,7 @@ void Calculator::site_log_likelihoods(double *out)
 		   "read site lnl");
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 	upload_pending_ = false;
+	in_flight_ = 0;
 }
 
 // The staging buffer may be rewritten once the last upload from it has
@@ -1122,6 +1178,7 @@ void Calculator::set_weights(const uint32_t *w)
 	std::memcpy(padded.data(), w, P_ * sizeof(uint32_t));
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 	upload_pending_ = false;
+	in_flight_ = 0;
 	check_cuda(cudaMemcpy(d_weights_, padded.data(), ldp_ * sizeof(uint32_t),
 			      cudaMemcpyHostToDevice),
 		   "upload weights");

@@ -104,6 +104,15 @@ class Calculator {
 	void launch_direct(uint32_t n, double clock_rate);
 	void wait_stage();
 	bool upload_pending_ = false; // an upload from h_stage_ may be in flight
+	// The fused short-list kernel and the run walk write the result into
+	// the mapped host word h_lnl_.  Before such a launch with no earlier
+	// evaluation in flight, the host stores a sentinel there and
+	// log_likelihood polls for the result instead of synchronising the
+	// stream; otherwise (or on any other path) it synchronises.
+	uint32_t in_flight_ = 0; // evaluations launched since the last wait
+	bool poll_result_ = false;
+	void arm_poll();
+	bool wait_mapped(double &value);
 	struct TimingSlot;
 	void launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		      bool want_cat, TimingSlot &slot);
