@@ -979,6 +979,13 @@ double Calculator::log_likelihood()
 	check_cuda(cudaStreamSynchronize(stream_), "sync");
 	upload_pending_ = false;
 	in_flight_ = 0;
+	if (poll_result_) {
+		uint64_t bits;
+		std::memcpy(&bits, h_lnl_, sizeof(bits));
+		if (bits == kLnlSentinel)
+			throw Error(B3G_ERR_CUDA,
+				    "the evaluation finished without writing its result");
+	}
 	if (h_status_ && *h_status_)
 		throw Error(B3G_ERR_TIMEOUT,
 			    "a tensor-core wait of the 20-state kernel gave up");
