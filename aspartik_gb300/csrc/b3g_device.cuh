@@ -214,13 +214,18 @@ struct Tc20Params {
 	uint32_t n, ldp, C, L;
 	uint32_t ops_smem;   // stage the list in shared memory
 	uint32_t tips_smem;  // stage the tile's tip codes in shared memory
+	uint32_t groups;     // 128-thread groups per CTA (1 or 2)
 	double log_inv_c;
 };
+// Dynamic shared memory of one tensor-core pruning CTA.
+size_t prune20tc_smem(uint32_t groups, bool ops_smem, uint32_t n, bool tips_smem,
+		      uint32_t L);
 // Tables of both kinds for the tensor-core path: p.ptab receives the FP32
 // tip rows, tc_tab the operand blocks.
 cudaError_t launch_ptab20tc(const PtabParams &p, float *tc_tab, cudaStream_t s);
-// Pruning (one CTA per 128-pattern tile and category) then the root's
-// category mixing and fold.
+// Pruning (one CTA of p.groups x 128 threads per 128-pattern tile and
+// category, 4 / p.groups CTAs per SM) then the root's category mixing and
+// fold.
 cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s);
 // 20-state path (prune20.cuh): transition tables [n][2][C][21][20] computed
 // in FP64, then one thread per (pattern, category) column walks the list;

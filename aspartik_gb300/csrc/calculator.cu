@@ -127,6 +127,12 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	use_tc20_ = f32_ && S_ == 20;
 	if (const char *env = std::getenv("B3G_TC20"))
 		use_tc20_ = use_tc20_ && std::atoi(env) != 0;
+	// groups of 128 threads per tensor-core CTA (B3G_TC20_GROUPS = 1 or 2)
+	if (const char *env = std::getenv("B3G_TC20_GROUPS")) {
+		const int gr = std::atoi(env);
+		if (gr == 1 || gr == 2)
+			tc20_groups_ = static_cast<uint32_t>(gr);
+	}
 	use_direct_ = f32_ && S_ == 4 && (C_ == 1 || C_ == 2 || C_ == 4);
 	if (const char *env = std::getenv("B3G_DIRECT"))
 		use_direct_ = use_direct_ && std::atoi(env) != 0;
@@ -702,10 +708,15 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		tp.ldp = ldp_;
 		tp.C = C_;
 		tp.L = L_;
-		// the list and the tile's tip codes in shared memory when each
-		// fits in 32 KiB (two CTAs per SM still fit)
-		tp.ops_smem = (size_t)n * sizeof(NodeOp) <= 32u * 1024u ? 1u : 0u;
-		tp.tips_smem = (size_t)L_ * 128u <= 32u * 1024u ? 1u : 0u;
+		// the list, then the tile's tip codes, in shared memory when they
+		// fit beside the operand areas at 4 / groups CTAs per SM
+		tp.groups = tc20_groups_;
+		const size_t budget = smem_budget(256u * tc20_groups_);
+		const size_t ops_bytes = (size_t)n * sizeof(NodeOp);
+		size_t used = prune20tc_smem(tc20_groups_, false, n, false, L_);
+		tp.ops_smem = used + ops_bytes <= budget ? 1u : 0u;
+		used += tp.ops_smem ? ops_bytes : 0;
+		tp.tips_smem = used + (size_t)L_ * 128u <= budget ? 1u : 0u;
 		tp.log_inv_c = std::log(1.0 / static_cast<double>(C_));
 		check_cuda(launch_prune20tc(tp, stream_), "tensor-core pruning kernel");
 		record(slot.k1);

@@ -235,6 +235,7 @@ class Calculator {
 	bool use_runs_ = false;
 	bool use_direct_ = false;
 	bool use_tc20_ = false;
+	uint32_t tc20_groups_ = 2;
 	float *d_tc_tab_ = nullptr;     // 20-state MMA operand blocks
 	double *d_root_val_ = nullptr;  // [C][ldp] root pi . x per category
 	int32_t *d_root_exp_ = nullptr; // [C][ldp] its exponent

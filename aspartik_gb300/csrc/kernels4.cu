@@ -875,20 +875,37 @@ cudaError_t launch_ptab20tc(const PtabParams &p, float *tc_tab, cudaStream_t s)
 	return cudaGetLastError();
 }
 
-cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s)
+size_t prune20tc_smem(uint32_t groups, bool ops_smem, uint32_t n, bool tips_smem,
+		      uint32_t L)
 {
-	if (p.C == 0 || p.C > 8 || p.ldp % kTcRows || p.n == 0)
-		return cudaErrorInvalidValue;
-	const bool narrow = (uint64_t)p.L * 2 * p.C * p.ldp < (1ull << 31);
-	auto kern = narrow ? prune20tc_kernel<uint32_t> : prune20tc_kernel<size_t>;
-	const int smem = (int)(kTcSmem + 1024 + (p.ops_smem ? p.n * sizeof(NodeOp) : 0) +
-			       (p.tips_smem ? p.L * kTcRows : 0));
+	return 1024 + (size_t)groups * kTcGroup * sizeof(float) +
+	       (ops_smem ? (size_t)n * sizeof(NodeOp) : 0) +
+	       (tips_smem ? (size_t)L * kTcRows : 0);
+}
+
+template <uint32_t kG>
+static cudaError_t launch_prune20tc_g(const Tc20Params &p, bool narrow, int smem,
+				      cudaStream_t s)
+{
+	auto kern = narrow ? prune20tc_kernel<uint32_t, kG> : prune20tc_kernel<size_t, kG>;
 	cudaError_t e = cudaFuncSetAttribute(
 		kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 	if (e != cudaSuccess)
 		return e;
-	kern<<<dim3(p.ldp / kTcRows, p.C), 128, smem, s>>>(p);
-	e = cudaGetLastError();
+	kern<<<dim3(p.ldp / kTcRows, p.C), 128 * kG, smem, s>>>(p);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s)
+{
+	if (p.C == 0 || p.C > 8 || p.ldp % kTcRows || p.n == 0 ||
+	    (p.groups != 1 && p.groups != 2))
+		return cudaErrorInvalidValue;
+	const bool narrow = (uint64_t)p.L * 2 * p.C * p.ldp < (1ull << 31);
+	const int smem = (int)prune20tc_smem(p.groups, p.ops_smem != 0, p.n,
+					     p.tips_smem != 0, p.L);
+	cudaError_t e = p.groups == 2 ? launch_prune20tc_g<2>(p, narrow, smem, s)
+				      : launch_prune20tc_g<1>(p, narrow, smem, s);
 	if (e != cudaSuccess)
 		return e;
 	finish20_kernel<<<p.ldp / kTcRows, 128, 0, s>>>(p);

@@ -12,34 +12,78 @@
 // 2 S^2 per internal child and (pattern, category); the tensor core
 // executes 3 x (32/20) x (24/20) times that.
 //
-// Work: one CTA per (pattern tile, category), 128 threads, thread p owns
-// pattern p of the tile (tensor-memory lane p).  The CTA walks the whole
-// children-first list; per entry the threads stage the internal children's
-// partials (split) and the two tables' operand blocks in shared memory,
-// thread 0 issues the MMAs and commits them to an mbarrier, and after the
-// wait every thread reads its row of each product from tensor memory,
-// multiplies the two children (a tip child is a table-row lookup),
-// renormalises by a power of two and stores the partial.  The root's
+// Work: one CTA per (pattern tile, category) with kG groups of 128 threads;
+// thread t of a group owns pattern t of the tile (tensor-memory lane t).
+// The list is walked run by run (NodeOp::pad = entries left in the run, so
+// the entries of a run are mutually independent): group g takes entries
+// g, g + kG, ... of each run, and the whole CTA synchronises between runs.
+// Per entry a group stages its internal children's partials (split) and the
+// two tables' operand blocks in its own shared memory, thread 0 of the group
+// issues the MMAs into the group's tensor-memory columns and commits them to
+// the group's mbarrier, and after the wait every thread reads its row of
+// each product from tensor memory, multiplies the two children (a tip child
+// is a table-row lookup), renormalises by a power of two and stores the
+// partial.  Several groups (and CTAs) per SM keep the tensor pipe and the
+// memory system busy while one entry's round trip is in flight.  The root's
 // pi . x and exponent go to per-category buffers; finish20_kernel mixes the
 // categories and folds the weighted sum.
 //
 // Shared-memory operand layout: K-major, no swizzle, core matrices of 8
-// rows x 16 bytes; element (row, k) at (row / 8) * 768 + (k / 4) * 128 +
-// (row % 8) * 16 + (k % 4) * 4 bytes: LBO = 128 (next 4 k), SBO = 768
-// (next 8 rows).  A block: 128 rows x 24 k (12,288 B); B block: 32 rows x
-// 24 k (3,072 B).
+// rows x 16 bytes.  B block (32 rows x 24 k, 3,072 B): element (row, k) at
+// (row / 8) * 768 + (k / 4) * 128 + (row % 8) * 16 + (k % 4) * 4 bytes,
+// LBO = 128 (next 4 k), SBO = 768 (next 8 rows); its K padding k = 20..23
+// is zero.  A block (128 rows x 20 k, 10,240 B): the same with SBO = 640,
+// five K chunks per group of 8 rows; the MMA's sixth chunk (k = 20..23) of
+// row group r is therefore read from row group r + 1's first chunk (for the
+// last row group: the next block), finite values that meet B's zero padding.
+// A group's area is its four A blocks [left hi, left lo, right hi, right lo]
+// followed by its four B blocks, all zeroed at the start.
 
 constexpr uint32_t kTcRows = 128;           // patterns per tile (M)
 constexpr uint32_t kTcN = 32;               // states padded (N)
 constexpr uint32_t kTcK = 24;               // states padded (K)
-constexpr uint32_t kTcA = kTcRows * kTcK;   // floats per A block
+constexpr uint32_t kTcSboA = 640;           // bytes per 8 rows of an A block
+constexpr uint32_t kTcA = kTcRows / 8 * kTcSboA / 4; // floats per A block (2,560)
 constexpr uint32_t kTcB = kTcN * kTcK;      // floats per B block (768)
-constexpr uint32_t kTcSmem = 4 * kTcA * 4 + 4 * kTcB * 4; // 61,440 B
+constexpr uint32_t kTcGroup = 4 * kTcA + 4 * kTcB; // floats per group (53,248 B)
 constexpr uint32_t kTcWaitLimit = 1u << 22; // polls, far beyond an MMA
 
-__host__ __device__ __forceinline__ uint32_t tc_off(uint32_t row, uint32_t k)
+// offset (floats) of element (row, k < 20) in an A block
+__host__ __device__ __forceinline__ uint32_t tc_off_a(uint32_t row, uint32_t k)
 {
-	return (row >> 3) * 192u + (k >> 2) * 32u + (row & 7u) * 4u + (k & 3u);
+	return (row >> 3) * (kTcSboA / 4) + (k >> 2) * 32u + (row & 7u) * 4u + (k & 3u);
+}
+
+// Named barrier of one 128-thread group: id 1 for group 0, 2 for group 1
+// (0 is __syncthreads).  Immediate ids keep the CTA's barrier count at 3.
+__device__ __forceinline__ void group_sync(uint32_t g)
+{
+	if (g == 0)
+		asm volatile("bar.sync 1, 128;" ::: "memory");
+	else
+		asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+// Same barrier, returning whether any of the group's threads passed v.
+__device__ __forceinline__ bool group_any(uint32_t g, bool v)
+{
+	uint32_t r;
+	if (g == 0)
+		asm volatile("{\n\t.reg .pred p, q;\n\t"
+			     "setp.ne.u32 p, %1, 0;\n\t"
+			     "bar.red.or.pred q, 1, 128, p;\n\t"
+			     "selp.u32 %0, 1, 0, q;\n\t}"
+			     : "=r"(r)
+			     : "r"((uint32_t)v)
+			     : "memory");
+	else
+		asm volatile("{\n\t.reg .pred p, q;\n\t"
+			     "setp.ne.u32 p, %1, 0;\n\t"
+			     "bar.red.or.pred q, 2, 128, p;\n\t"
+			     "selp.u32 %0, 1, 0, q;\n\t}"
+			     : "=r"(r)
+			     : "r"((uint32_t)v)
+			     : "memory");
+	return r != 0;
 }
 
 // One block per table (entry, side, category), 768 threads: P in FP64 (as
@@ -94,52 +138,67 @@ __global__ void __launch_bounds__(768) ptab20tc_kernel(PtabParams prm, float *tc
 	blk[kTcB + t] = lo;
 }
 
-template <typename Idx>
-__global__ void __launch_bounds__(128) prune20tc_kernel(Tc20Params prm)
+template <typename Idx, uint32_t kG>
+__global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params prm)
 {
+	static_assert(kG == 1 || kG == 2, "one or two groups per CTA");
 	constexpr int S = kS20;
+	constexpr uint32_t kRowBytes = kTcRows * S * 4;  // a side's 128 partial rows
+	constexpr uint32_t kOpBytes = 2 * kTcB * 4;      // its hi and lo B blocks
+	constexpr uint32_t kTipBytes = (S + 1) * S * 4;  // a tip side's table
+	static_assert(kRowBytes == kTcA * 4 && kTipBytes <= kOpBytes, "copy areas");
 	extern __shared__ uint8_t tc_smem_raw[];
-	float *sA = reinterpret_cast<float *>(((uintptr_t)tc_smem_raw + 1023) &
-					      ~(uintptr_t)1023);
-	float *sB = sA + 4 * kTcA; // [side][hi, lo][768]
+	float *sBase = reinterpret_cast<float *>(((uintptr_t)tc_smem_raw + 1023) &
+						 ~(uintptr_t)1023);
 	// then the list (when it fits) and the tile's tip codes
-	NodeOp *sOps = reinterpret_cast<NodeOp *>(sB + 4 * kTcB);
+	NodeOp *sOps = reinterpret_cast<NodeOp *>(sBase + kG * kTcGroup);
 	uint8_t *sTips = reinterpret_cast<uint8_t *>(sOps + (prm.ops_smem ? prm.n : 0));
-	__shared__ __align__(8) uint64_t mbar;
+	__shared__ __align__(8) uint64_t mbar[kG]; // MMA completion, per group
+	__shared__ __align__(8) uint64_t lbar[kG]; // input copies, per group
 	__shared__ uint32_t holder;
-	const uint32_t t = threadIdx.x, warp = t >> 5;
+	const uint32_t g = threadIdx.x >> 7, t = threadIdx.x & 127u;
+	const uint32_t warp = threadIdx.x >> 5;
+	float *sA = sBase + g * kTcGroup; // [side][hi, lo][2,560]
+	float *sB = sA + 4 * kTcA;         // [side][hi, lo][768]
 	const uint32_t c = blockIdx.y, C = prm.C;
 	const uint32_t p = blockIdx.x * kTcRows + t;
 	const Idx stride = (Idx)C * prm.ldp;
-	const Idx col = (Idx)c * prm.ldp + p;
-	const uint32_t mb = tc::smem_u32(&mbar);
-	for (uint32_t k = t; prm.ops_smem && k < prm.n; k += 128)
+	const Idx col0 = (Idx)c * prm.ldp + blockIdx.x * kTcRows;
+	const Idx col = col0 + t;
+	const uint32_t mb = tc::smem_u32(&mbar[g]);
+	const uint32_t lb = tc::smem_u32(&lbar[g]);
+
+	// zero the operand areas: the A blocks' sixth K chunks read
+	// neighbouring rows, which must hold finite values from the start
+	float4 *z4 = reinterpret_cast<float4 *>(sBase);
+	for (uint32_t k = threadIdx.x; k < kG * kTcGroup / 4; k += blockDim.x)
+		z4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+	for (uint32_t k = threadIdx.x; prm.ops_smem && k < prm.n; k += blockDim.x)
 		sOps[k] = prm.ops[k];
 	if (prm.tips_smem) {
 		// 4-byte loads: the tile's 128 codes of every leaf
 		uint32_t *s32 = reinterpret_cast<uint32_t *>(sTips);
-		for (uint32_t k = t; k < prm.L * 32u; k += 128) {
+		for (uint32_t k = threadIdx.x; k < prm.L * 32u; k += blockDim.x) {
 			const uint32_t leaf = k >> 5, w4 = k & 31u;
 			s32[k] = *reinterpret_cast<const uint32_t *>(
 				prm.tips + (size_t)leaf * prm.ldp + blockIdx.x * kTcRows + 4 * w4);
 		}
 	}
 	const NodeOp *ops = prm.ops_smem ? sOps : prm.ops;
-
-	// K padding (k = 20..23) of the four A blocks stays zero
-#pragma unroll
-	for (uint32_t b = 0; b < 4; b++)
-		*reinterpret_cast<float4 *>(sA + b * kTcA + tc_off(t, 20)) =
-			make_float4(0.f, 0.f, 0.f, 0.f);
-	if (t == 0)
-		tc::mbar_init(mb, 1);
+	if (threadIdx.x == 0)
+		for (uint32_t k = 0; k < kG; k++) {
+			tc::mbar_init(tc::smem_u32(&mbar[k]), 1);
+			tc::mbar_init(tc::smem_u32(&lbar[k]), 1);
+		}
 	if (warp == 0)
-		tc::tmem_alloc(tc::smem_u32(&holder), 64);
+		tc::tmem_alloc(tc::smem_u32(&holder), 64 * kG);
+	tc::fence_proxy_async_smem(); // the zeroed areas before the first copies
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
-	const uint32_t tmem = holder;
-	const uint32_t lane_base = (32u * warp) << 16;
+	// this group's accumulators: columns [64 g, 64 g + 64), left then right
+	const uint32_t tmem = holder + 64u * g;
+	const uint32_t lane_base = (32u * (warp & 3u)) << 16;
 	constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
 	// operand descriptors of K step 0: [child][hi, lo]
 	uint64_t dA[2][2], dB[2][2];
@@ -147,174 +206,228 @@ __global__ void __launch_bounds__(128) prune20tc_kernel(Tc20Params prm)
 	for (uint32_t j = 0; j < 2; j++)
 #pragma unroll
 		for (uint32_t h = 0; h < 2; h++) {
-			dA[j][h] = tc::smem_desc(tc::smem_u32(sA + (2 * j + h) * kTcA), 128, 768);
+			dA[j][h] = tc::smem_desc(tc::smem_u32(sA + (2 * j + h) * kTcA), 128,
+						 kTcSboA);
 			dB[j][h] = tc::smem_desc(tc::smem_u32(sB + (2 * j + h) * kTcB), 128, 768);
 		}
 
-	// Inputs of one entry, fetched into registers ahead of their use: for
-	// an internal side the child's partial row, scale and this side's
-	// operand blocks (three float4 per thread); for a tip side the table
-	// row of the tip's code.
-	struct Inputs {
-		float x[2][S];
-		float4 b[2][3];
-		int32_t sc[2];
-	};
-	auto fetch = [&](uint32_t e, Inputs &in) {
+	// Inputs of entry e, copied by thread 0 of the group: an internal
+	// side's 128 partial rows (contiguous) into its A-lo block, where they
+	// wait to be split, and its operand blocks into its B blocks; a tip
+	// side's table into its B blocks.
+	auto issue = [&](uint32_t e) {
 		const NodeOp op = ops[e];
 		const uint32_t ids[2] = {op.left, op.right};
+		uint32_t bytes = 0;
+#pragma unroll
+		for (uint32_t j = 0; j < 2; j++)
+			bytes += (ids[j] & kTipBit) ? kTipBytes : kRowBytes + kOpBytes;
+		tc::mbar_expect_tx(lb, bytes);
 #pragma unroll
 		for (uint32_t j = 0; j < 2; j++) {
 			const size_t tid_tab = (size_t)(2 * e + j) * C + c;
+			const uint32_t bdst = tc::smem_u32(sB + j * 2 * kTcB);
 			if (ids[j] & kTipBit) {
-				const uint32_t leaf = ids[j] & ~kTipBit;
-				const uint8_t code =
-					prm.tips_smem ? sTips[leaf * kTcRows + t]
-						      : prm.tips[(size_t)leaf * prm.ldp + p];
-				load20<true>(prm.tab + (tid_tab * (S + 1) + code) * S, in.x[j]);
-				in.sc[j] = 0;
+				tc::bulk_g2s(bdst, prm.tab + tid_tab * (S + 1) * S, kTipBytes, lb);
 			} else {
-				const Idx ix = (Idx)ids[j] * stride + col;
-				load20<false>(prm.partials + (size_t)ix * S, in.x[j]);
-				in.sc[j] = prm.scales[ix];
-				const float4 *src = reinterpret_cast<const float4 *>(
-					prm.tc_tab + tid_tab * 2 * kTcB);
-#pragma unroll
-				for (uint32_t q = 0; q < 3; q++)
-					in.b[j][q] = __ldg(src + t + 128 * q);
+				const Idx ix0 = (Idx)ids[j] * stride + col0;
+				tc::bulk_g2s(tc::smem_u32(sA + (2 * j + 1) * kTcA),
+					     prm.partials + (size_t)ix0 * S, kRowBytes, lb);
+				tc::bulk_g2s(bdst, prm.tc_tab + tid_tab * 2 * kTcB, kOpBytes, lb);
 			}
 		}
 	};
+	auto run_len = [&](uint32_t e0) {
+		const uint32_t r = ops[e0].pad;
+		return r == 0 ? 1u : min(r, prm.n - e0);
+	};
 
-	float y[S];
-#pragma unroll
-	for (int i = 0; i < S; i++)
-		y[i] = 0.f;
-	int32_t cnt = 0;
-	uint32_t phase = 0;
-	bool failed = false;
-	Inputs cur, nxt;
-	if (prm.n)
-		fetch(0, cur);
-	for (uint32_t e = 0; e < prm.n; ++e) {
-		const NodeOp op = ops[e];
-		const uint32_t ids[2] = {op.left, op.right};
-		const bool any = !(ids[0] & kTipBit) || !(ids[1] & kTipBit);
-		// stage the internal sides: split partials, operand blocks
-#pragma unroll
-		for (uint32_t j = 0; j < 2; j++) {
-			if (ids[j] & kTipBit)
-				continue;
-			float *ah = sA + (2 * j) * kTcA, *al = ah + kTcA;
-#pragma unroll
-			for (uint32_t q = 0; q < 5; q++) {
-				float h[4], l[4];
-#pragma unroll
-				for (int u = 0; u < 4; u++)
-					tc::split_tf32(cur.x[j][4 * q + u], h[u], l[u]);
-				*reinterpret_cast<float4 *>(ah + tc_off(t, 4 * q)) =
-					make_float4(h[0], h[1], h[2], h[3]);
-				*reinterpret_cast<float4 *>(al + tc_off(t, 4 * q)) =
-					make_float4(l[0], l[1], l[2], l[3]);
+	// output rows pass through the left A-hi block (raw [128][20] layout)
+	float *stage = sA;
+	uint32_t lphase = 0, mphase = 0;
+	bool failed = false, pending = false;
+	uint32_t e0 = 0, r = run_len(0);
+	if (g < r) {
+		if (t == 0)
+			issue(g);
+		pending = true;
+	}
+	for (;;) {
+		for (uint32_t e = e0 + g; e < e0 + r; e += kG) {
+			const NodeOp op = ops[e];
+			const uint32_t ids[2] = {op.left, op.right};
+			const bool any = !(ids[0] & kTipBit) || !(ids[1] & kTipBit);
+			const bool ok_in = tc::mbar_wait(lb, lphase, kTcWaitLimit);
+			lphase ^= 1u;
+			pending = false;
+			if (group_any(g, !ok_in)) {
+				failed = true;
+				break;
 			}
-			float4 *dst = reinterpret_cast<float4 *>(sB + j * 2 * kTcB);
+			// this thread's rows: a tip side's final value from its table,
+			// an internal side's partial row from the copied block
+			float v[2][S];
+			int32_t sc[2];
 #pragma unroll
-			for (uint32_t q = 0; q < 3; q++)
-				dst[t + 128 * q] = cur.b[j][q];
-		}
-		if (any) {
-			tc::fence_proxy_async_smem();
-			tc::fence_before_sync();
-			__syncthreads();
-			tc::fence_after_sync();
-			if (t == 0) {
+			for (uint32_t j = 0; j < 2; j++) {
+				const float *row;
+				if (ids[j] & kTipBit) {
+					const uint32_t leaf = ids[j] & ~kTipBit;
+					const uint32_t code =
+						prm.tips_smem ? sTips[leaf * kTcRows + t]
+							      : prm.tips[(size_t)leaf * prm.ldp + p];
+					row = sB + j * 2 * kTcB + min(code, (uint32_t)S) * S;
+					sc[j] = 0;
+				} else {
+					row = sA + (2 * j + 1) * kTcA + t * S;
+					sc[j] = prm.scales[(Idx)ids[j] * stride + col];
+				}
+				const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+				for (int q = 0; q < 5; q++) {
+					const float4 a = r4[q];
+					v[j][4 * q] = a.x;
+					v[j][4 * q + 1] = a.y;
+					v[j][4 * q + 2] = a.z;
+					v[j][4 * q + 3] = a.w;
+				}
+			}
+			// every copied row read, the previous entry's output stored
+			group_sync(g);
+			const bool next = e + kG < e0 + r;
+			if (!any) {
+				if (next) {
+					if (t == 0)
+						issue(e + kG);
+					pending = true;
+				}
+			} else {
+				// stage the internal sides' split rows
 #pragma unroll
 				for (uint32_t j = 0; j < 2; j++) {
 					if (ids[j] & kTipBit)
 						continue;
-					// the start address sits in the low bits (>> 4):
-					// the next K step (+256 B) adds 16
+					float *ah = sA + (2 * j) * kTcA, *al = ah + kTcA;
 #pragma unroll
-					for (uint32_t s = 0; s < 3; s++) {
-						// x_hi P_hi, x_hi P_lo, x_lo P_hi
-						tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
-							     dB[j][0] + 16 * s, idesc, s != 0);
-						tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
-							     dB[j][1] + 16 * s, idesc, 1);
-						tc::mma_tf32(tmem + 32 * j, dA[j][1] + 16 * s,
-							     dB[j][0] + 16 * s, idesc, 1);
+					for (uint32_t q = 0; q < 5; q++) {
+						float h[4], l[4];
+#pragma unroll
+						for (int u = 0; u < 4; u++)
+							tc::split_tf32(v[j][4 * q + u], h[u], l[u]);
+						*reinterpret_cast<float4 *>(ah + tc_off_a(t, 4 * q)) =
+							make_float4(h[0], h[1], h[2], h[3]);
+						*reinterpret_cast<float4 *>(al + tc_off_a(t, 4 * q)) =
+							make_float4(l[0], l[1], l[2], l[3]);
 					}
 				}
-				tc::mma_commit(mb);
-			}
-		}
-		// the next entry's inputs travel while the MMAs run, unless that
-		// entry reads this one's output (fetched after the store below)
-		const bool more = e + 1 < prm.n;
-		bool next_dep = false;
-		if (more) {
-			const NodeOp nop = ops[e + 1];
-			next_dep = nop.left == op.out || nop.right == op.out;
-			if (!next_dep)
-				fetch(e + 1, nxt);
-		}
-		float ab[2][S];
-		if (any) {
-			const bool ok = tc::mbar_wait(mb, phase, kTcWaitLimit);
-			phase ^= 1u;
-			if (__syncthreads_or(!ok)) {
-				failed = true;
-				break;
-			}
-			tc::fence_after_sync();
+				tc::fence_proxy_async_smem();
+				tc::fence_before_sync();
+				group_sync(g);
+				tc::fence_after_sync();
+				if (t == 0) {
 #pragma unroll
-			for (uint32_t j = 0; j < 2; j++) {
-				if (ids[j] & kTipBit)
-					continue;
-				const uint32_t ta = tmem + lane_base + 32 * j;
-				tc::tmem_ld16(ta, ab[j]);
-				tc::tmem_ld4(ta + 16, ab[j] + 16);
-			}
-			tc::tmem_wait_ld();
-		}
+					for (uint32_t j = 0; j < 2; j++) {
+						if (ids[j] & kTipBit)
+							continue;
+						// the start address sits in the low bits (>> 4):
+						// the next K step (+256 B) adds 16
 #pragma unroll
-		for (uint32_t j = 0; j < 2; j++)
-			if (ids[j] & kTipBit)
+						for (uint32_t s = 0; s < 3; s++) {
+							// x_hi P_hi, x_hi P_lo, x_lo P_hi
+							tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
+								     dB[j][0] + 16 * s, idesc, s != 0);
+							tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
+								     dB[j][1] + 16 * s, idesc, 1);
+							tc::mma_tf32(tmem + 32 * j, dA[j][1] + 16 * s,
+								     dB[j][0] + 16 * s, idesc, 1);
+						}
+					}
+					tc::mma_commit(mb);
+				}
+				const bool ok = tc::mbar_wait(mb, mphase, kTcWaitLimit);
+				mphase ^= 1u;
+				if (group_any(g, !ok)) {
+					failed = true;
+					break;
+				}
+				// operands consumed: the group's next entry's inputs
+				// travel during this epilogue
+				if (next) {
+					if (t == 0)
+						issue(e + kG);
+					pending = true;
+				}
+				tc::fence_after_sync();
+#pragma unroll
+				for (uint32_t j = 0; j < 2; j++) {
+					if (ids[j] & kTipBit)
+						continue;
+					const uint32_t ta = tmem + lane_base + 32 * j;
+					tc::tmem_ld16(ta, v[j]);
+					tc::tmem_ld4(ta + 16, v[j] + 16);
+				}
+				tc::tmem_wait_ld();
+			}
+			float y[S];
+#pragma unroll
+			for (int i = 0; i < S; i++)
+				y[i] = v[0][i] * v[1][i];
+			const int32_t cnt = sc[0] + sc[1] + rescale_pow2_20(y);
+			prm.scales[(Idx)op.out * stride + col] = cnt;
+			if (e + 1 == prm.n) {
+				double dot = 0.0;
 #pragma unroll
 				for (int i = 0; i < S; i++)
-					ab[j][i] = cur.x[j][i];
+					dot = fma(prm.pi[i], (double)y[i], dot);
+				prm.root_val[(size_t)c * prm.ldp + p] = dot;
+				prm.root_exp[(size_t)c * prm.ldp + p] = cnt;
+			}
+			// the output rows through shared memory, then 16-byte stores
+			// of consecutive addresses by consecutive threads
+			float4 *srow = reinterpret_cast<float4 *>(stage + t * S);
 #pragma unroll
-		for (int i = 0; i < S; i++)
-			y[i] = ab[0][i] * ab[1][i];
-		cnt = cur.sc[0] + cur.sc[1] + rescale_pow2_20(y);
-		const Idx ox = (Idx)op.out * stride + col;
-		store20(prm.partials + (size_t)ox * S, y);
-		prm.scales[ox] = cnt;
-		// the next entry overwrites shared memory and tensor memory
+			for (int q = 0; q < 5; q++)
+				srow[q] = make_float4(y[4 * q], y[4 * q + 1], y[4 * q + 2], y[4 * q + 3]);
+			group_sync(g);
+			const float4 *s4 = reinterpret_cast<const float4 *>(stage);
+			float4 *d4 = reinterpret_cast<float4 *>(
+				prm.partials + (size_t)((Idx)op.out * stride + col0) * S);
+#pragma unroll
+			for (uint32_t q = 0; q < 5; q++)
+				d4[t + 128 * q] = s4[t + 128 * q];
+		}
+		// the run's outputs are visible to every group, and to the bulk
+		// copies of the next run, before those read them
+		tc::fence_proxy_async_global();
 		tc::fence_before_sync();
-		__syncthreads();
-		if (more) {
-			if (next_dep) // this thread's own row, stored just above
-				fetch(e + 1, nxt);
-			cur = nxt;
+		const int stop = __syncthreads_or(failed);
+		tc::fence_after_sync();
+		if (stop) {
+			failed = true;
+			break;
+		}
+		e0 += r;
+		if (e0 >= prm.n)
+			break;
+		r = run_len(e0);
+		if (g < r) {
+			if (t == 0)
+				issue(e0 + g);
+			pending = true;
 		}
 	}
 	if (failed) {
-		if (t == 0)
+		// copies still in flight land before the CTA leaves
+		if (pending && t == 0)
+			tc::mbar_wait(lb, lphase, kTcWaitLimit);
+		if (threadIdx.x == 0)
 			atomicExch(prm.status, 1u);
-	} else {
-		double dot = 0.0;
-#pragma unroll
-		for (int i = 0; i < S; i++)
-			dot = fma(prm.pi[i], (double)y[i], dot);
-		prm.root_val[(size_t)c * prm.ldp + p] = dot;
-		prm.root_exp[(size_t)c * prm.ldp + p] = cnt;
 	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
 	if (warp == 0)
-		tc::tmem_dealloc(tmem, 64);
+		tc::tmem_dealloc(holder, 64 * kG);
 }
 
 // Category mixing of the root (FP32 form: values with power-of-two

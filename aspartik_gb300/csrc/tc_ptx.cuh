@@ -120,6 +120,34 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity,
 	return false;
 }
 
+// Arm the mbarrier for one phase: one arrival that also expects `bytes`
+// of asynchronous copies to complete on it.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar_saddr, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar_saddr),
+		     "r"(bytes)
+		     : "memory");
+}
+
+// Bulk copy (no tensor map) of `bytes` from global to this CTA's shared
+// memory, completing on the mbarrier.  Both addresses 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst_saddr, const void *src, uint32_t bytes,
+					 uint32_t mbar_saddr)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+		     "[%0], [%1], %2, [%3];" ::"r"(dst_saddr),
+		     "l"(src), "r"(bytes), "r"(mbar_saddr)
+		     : "memory");
+}
+
+// Generic-proxy global writes ordered before later asynchronous-proxy
+// (bulk copy) reads of them.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+	asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // 32 lanes x 16 consecutive 32-bit columns: this thread's lane, columns
 // taddr .. taddr + 15.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])

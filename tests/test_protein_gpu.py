@@ -163,3 +163,59 @@ def test_tensor_core_path_matches_cuda_core_walk(rng):
             g.accept()
     for g in (tc, cc, g64):
         g.close()
+
+
+def make20_env(c, K, **env):
+    """FP32 calculator built with the given environment switches."""
+    import os
+
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update({k: str(v) for k, v in env.items()})
+    try:
+        return make20(c, "f32", K)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("taxa,sites,K", [(40, 700, 4), (300, 400, 2), (600, 200, 1)])
+def test_tensor_core_groups_agree(rng, taxa, sites, K):
+    """One and two 128-thread groups per CTA compute every entry with the
+    same arithmetic and only order independent entries differently, so
+    their likelihoods are bit-identical, whole tree and dirty paths; both
+    meet the FP32 bar against the FP64 form.  The 600-taxon list does not
+    fit shared memory beside two groups' operand areas and is read from
+    global memory."""
+    c = protein_case(taxa, sites, seed=53 + taxa, alpha=0.7 if K > 1 else None,
+                     num_categories=K, gaps=0.02)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    g1, g2 = make20_env(c, K, B3G_TC20_GROUPS=1), make20_env(c, K, B3G_TC20_GROUPS=2)
+    g64 = make20(c, "f64", K)
+    for g in (g1, g2, g64):
+        g.set_reversible(c.rates, c.pi)
+        if K > 1:
+            g.set_gamma(0.7)
+        g.propose_lengths(*whole(tree), 1.0)
+    a, b, ref = g1.log_likelihood(), g2.log_likelihood(), g64.log_likelihood()
+    assert a == b
+    assert a == pytest.approx(ref, rel=F32_TOL)
+    np.testing.assert_array_equal(g1.site_log_likelihoods(), g2.site_log_likelihoods())
+    for g in (g1, g2, g64):
+        g.accept()
+    tree.accept()
+    for step in range(6):
+        random_move(tree, rng)
+        inc = lists_and_lengths(tree)
+        for g in (g1, g2, g64):
+            g.propose_lengths(*inc, 1.0)
+        a, b, ref = g1.log_likelihood(), g2.log_likelihood(), g64.log_likelihood()
+        assert a == b, step
+        assert a == pytest.approx(ref, rel=F32_TOL), step
+        tree.accept()
+        for g in (g1, g2, g64):
+            g.accept()
+    for g in (g1, g2, g64):
+        g.close()
