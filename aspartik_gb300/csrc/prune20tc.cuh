@@ -1,6 +1,6 @@
 // prune20tc.cuh -- 20-state pruning on the tensor cores (FP32 chosen form).
 // Included by kernels4.cu inside its anonymous namespace after prune20.cuh
-// (uses rescale_pow2_20, load20/store20 and block_fold).
+// (uses rescale_pow2_20 and block_fold).
 //
 // An internal child's contribution for a tile of 128 patterns and one
 // category is a small GEMM: out[p][i] = sum_k x[p][k] P[i][k], M = 128
