@@ -187,6 +187,8 @@ SIGNATURES = {
     "b3g_mcmc_run": (ct.c_int, [_vp, ct.c_uint64]),
     "b3g_mcmc_trace": (ct.c_int, [_vp, ct.c_uint32, _f64p, ct.c_uint64,
                                   ct.POINTER(ct.c_uint64)]),
+    "b3g_mcmc_chain_trace": (ct.c_int, [_vp, ct.c_uint32, ct.c_uint32, _f64p, ct.c_uint64,
+                                        ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_operator_stats": (ct.c_int, [_vp, ct.c_uint32, ct.POINTER(ct.c_uint64), _f64p]),
     "b3g_mcmc_swaps": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_dump": (ct.c_int, [_vp, _u8p, ct.c_uint64, ct.POINTER(ct.c_uint64)]),

@@ -751,23 +751,37 @@ void Mcmc::tune()
 
 void Mcmc::record()
 {
+	// the trace fields of one chain
+	auto fields = [&](const Chain &ch, double f[8]) {
+		const DatedTree &tr = *ch.tree;
+		double length = 0.0;
+		for (uint32_t v = 0; v < tr.num_nodes(); ++v)
+			if (v != tr.root())
+				length += tr.edge_length(v);
+		f[0] = ch.lnl_cache;
+		f[1] = ch.prior_cache;
+		f[2] = ch.lnl_cache + ch.prior_cache;
+		f[3] = tr.root_height();
+		f[4] = cfg_.model == 0 ? ch.kappa.v : ch.rates.v[0];
+		f[5] = ch.alpha.v;
+		f[6] = length;
+		f[7] = cfg_.clock_categories ? ch.clock_sd.v : 0.0;
+	};
 	const Chain *cold = chains_[0].get();
 	for (const auto &c : chains_)
 		if (c->beta > cold->beta)
 			cold = c.get();
 	const DatedTree &t = *cold->tree;
-	double length = 0.0;
-	for (uint32_t v = 0; v < t.num_nodes(); ++v)
-		if (v != t.root())
-			length += t.edge_length(v);
-	trace_[0].push_back(cold->lnl_cache);
-	trace_[1].push_back(cold->prior_cache);
-	trace_[2].push_back(cold->lnl_cache + cold->prior_cache);
-	trace_[3].push_back(t.root_height());
-	trace_[4].push_back(cfg_.model == 0 ? cold->kappa.v : cold->rates.v[0]);
-	trace_[5].push_back(cold->alpha.v);
-	trace_[6].push_back(length);
-	trace_[7].push_back(cfg_.clock_categories ? cold->clock_sd.v : 0.0);
+	double f[8];
+	fields(*cold, f);
+	for (uint32_t k = 0; k < 8; ++k)
+		trace_[k].push_back(f[k]);
+	chain_trace_.resize(chains_.size() * 8);
+	for (size_t i = 0; i < chains_.size(); ++i) {
+		fields(*chains_[i], f);
+		for (uint32_t k = 0; k < 8; ++k)
+			chain_trace_[i * 8 + k].push_back(f[k]);
+	}
 	// the whole sample for trace files: tree and parameters
 	sample_steps_.push_back(step_);
 	for (uint32_t v = 0; v < t.num_nodes(); ++v) {

@@ -191,6 +191,13 @@ class Mcmc {
 	{
 		return trace_[field];
 	}
+	// the same fields for each chain in chain order (chain i's state,
+	// whatever temperature MC3 swaps have given it)
+	const std::vector<double> &chain_trace(uint32_t chain, uint32_t field) const
+	{
+		return chain_trace_.at((size_t)chain * 8 + field);
+	}
+	size_t chain_trace_size() const { return chain_trace_.size(); }
 	void op_stats(uint32_t op, uint64_t out[4], double *tuning) const;
 	// samples: steps[n], parents[n][nodes], heights[n][nodes],
 	// parameters[n][kSampleParams]
@@ -246,6 +253,7 @@ class Mcmc {
 	uint32_t tune_rounds_ = 0;
 	Rng swap_rng_;
 	std::vector<double> trace_[8];
+	std::vector<std::vector<double>> chain_trace_; // [chain * 8 + field]
 	// per sample: the step, the cold chain's tree (parents and heights of
 	// every node) and its parameters (kSampleParams values)
 	std::vector<uint64_t> sample_steps_;

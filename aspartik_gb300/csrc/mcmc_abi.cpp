@@ -173,6 +173,28 @@ B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
 	});
 }
 
+B3G_API b3g_status b3g_mcmc_chain_trace(b3g_mcmc *mcmc, uint32_t chain,
+					uint32_t field, double *out, uint64_t capacity,
+					uint64_t *count)
+{
+	return guarded([&] {
+		if (field > 7 || !count)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "bad trace field");
+		const b3g::Mcmc &m = *mcmc_of(mcmc);
+		if (chain >= m.num_chains())
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "no such chain");
+		*count = 0;
+		if ((size_t)chain * 8 + field >= m.chain_trace_size())
+			return; // nothing recorded yet
+		const auto &t = m.chain_trace(chain, field);
+		*count = t.size();
+		if (out)
+			std::copy(t.begin(),
+				  t.begin() + std::min<uint64_t>(capacity, t.size()),
+				  out);
+	});
+}
+
 B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
 					   uint64_t *counts, double *tuning)
 {

@@ -295,6 +295,8 @@ void Mcmc::load(const uint8_t *state, size_t size)
 	tuned_ = true;
 	for (auto &t : trace_)
 		t.clear();
+	for (auto &t : chain_trace_)
+		t.clear();
 	sample_steps_.clear();
 	sample_parents_.clear();
 	sample_heights_.clear();

@@ -111,13 +111,21 @@ class Mcmc:
     def run(self, steps: int):
         check(lib.b3g_mcmc_run(self._h, int(steps)))
 
-    def trace(self, name: str) -> np.ndarray:
+    def trace(self, name: str, chain: int | None = None) -> np.ndarray:
+        """Samples of one trace field: the cold chain's, or chain `chain`'s
+        (chain order; independent replicates when heat = 0)."""
         fid = TRACE_FIELDS.index(name)
         n = ct.c_uint64()
-        check(lib.b3g_mcmc_trace(self._h, fid, None, 0, ct.byref(n)))
+        if chain is None:
+            check(lib.b3g_mcmc_trace(self._h, fid, None, 0, ct.byref(n)))
+            out = np.empty(n.value)
+            check(lib.b3g_mcmc_trace(self._h, fid, nat.as_ptr(out, ct.c_double), n.value,
+                                     ct.byref(n)))
+            return out
+        check(lib.b3g_mcmc_chain_trace(self._h, int(chain), fid, None, 0, ct.byref(n)))
         out = np.empty(n.value)
-        check(lib.b3g_mcmc_trace(self._h, fid, nat.as_ptr(out, ct.c_double), n.value,
-                                 ct.byref(n)))
+        check(lib.b3g_mcmc_chain_trace(self._h, int(chain), fid,
+                                       nat.as_ptr(out, ct.c_double), n.value, ct.byref(n)))
         return out
 
     def samples(self) -> dict:

@@ -413,8 +413,11 @@ def mcmc_ess(wl, steps: int, device: int) -> dict:
     steps for every arm; ESS is the minimum over the lnL, root-height and
     first-exchangeability traces (Geyer 1992) on the last 80% of samples (past
     the pilot); time is the wall time of the whole run, pilot and training
-    included."""
-    from aspartik_gb300.ess import min_ess
+    included.  A fourth arm runs the chosen form batched: 8 independent
+    replicates stepping together, each scalar's ESS by the multi-chain
+    estimator (between-chain variance included; the sum of the per-chain
+    values is reported beside it)."""
+    from aspartik_gb300.ess import ess, min_ess, multi_chain_ess
     from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
 
     out = {}
@@ -443,8 +446,41 @@ def mcmc_ess(wl, steps: int, device: int) -> dict:
         if pilot:
             out[name]["delayed_acceptance"] = m.da_stats()
         m.close()
+    # the chosen form batched: independent replicates (heat 0, no swaps) on
+    # their own streams; ESS per scalar over the replicates by the
+    # multi-chain estimator, which counts their disagreement against them
+    R = 8
+    s = McmcSettings(model="gtr", precision="f32", num_categories=wl["spec"]["categories"],
+                     num_chains=R, heat=0.0, swap_every=0, seed=4, sample_every=10,
+                     weights=dict(GTR_WEIGHTS), device=device)
+    m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
+    m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
+                     alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
+    t0 = time.perf_counter()
+    m.run(steps)
+    dt = time.perf_counter() - t0
+    keep = (steps // 10) // 5
+    names = ("lnl", "root_height", "kappa_or_rate0")
+    chains_tr = {n: [m.trace(n, chain=k)[keep:] for k in range(R)] for n in names}
+    combined = {n: multi_chain_ess(chains_tr[n], burn_in=0.0) for n in names}
+    summed = {n: sum(ess(x, burn_in=0.0) for x in chains_tr[n]) for n in names}
+    e = min(combined.values())
+    out["chosen_f32_replicates"] = {
+        "chains": R, "steps": steps, "seconds": round(dt, 3),
+        "us_per_step": round(dt / steps * 1e6, 2),
+        "chain_steps_per_s": round(R * steps / dt, 1),
+        "ess_min": round(e, 2), "ess": {k: round(v, 2) for k, v in combined.items()},
+        "ess_summed_per_chain": {k: round(v, 2) for k, v in summed.items()},
+        "ess_per_s": round(e / dt, 3), "check_rel": m.check()}
+    m.close()
     base = max(out["plain_f64"]["ess_per_s"], 1e-12)
     out["ess_per_s_ratio_chosen_vs_plain"] = round(out["chosen_f32"]["ess_per_s"] / base, 3)
+    # (no ESS ratio for the replicates: the multi-chain estimator also
+    # charges the replicates' disagreement, which one plain chain's own
+    # estimate cannot see, so the two ESS figures are not like for like)
+    out["chain_steps_per_s_ratio_chosen_replicates_vs_plain"] = round(
+        out["chosen_f32_replicates"]["chain_steps_per_s"] * out["plain_f64"]["seconds"]
+        / steps, 3)
     out["ess_per_s_ratio_chosen_da_vs_plain"] = round(
         out["chosen_f32_da"]["ess_per_s"] / base, 3)
     out["mean_lnl_rel_diff_chosen_vs_plain"] = abs(

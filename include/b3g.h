@@ -402,6 +402,12 @@ B3G_API b3g_status b3g_mcmc_samples(b3g_mcmc *mcmc, uint64_t *steps,
 B3G_API b3g_status b3g_mcmc_trace(b3g_mcmc *mcmc, uint32_t field,
 				  double *out, uint64_t capacity,
 				  uint64_t *count);
+/* The same for one chain (0 .. num_chains - 1) in chain order, e.g. for
+ * the summed ESS of independent replicates; with MC3 swaps a chain's trace
+ * follows its state through the temperatures. */
+B3G_API b3g_status b3g_mcmc_chain_trace(b3g_mcmc *mcmc, uint32_t chain,
+					uint32_t field, double *out,
+					uint64_t capacity, uint64_t *count);
 /* counts = {accepts, rejects, aborts, prior rejects} of one operator. */
 B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
 					   uint64_t *counts, double *tuning);

@@ -90,3 +90,29 @@ def test_chosen_and_plain_forms_agree_on_the_posterior():
         a, b = out["f64"][k], out["f32"][k]
         se = np.sqrt(a.var() / ess(a, 0.0) + b.var() / ess(b, 0.0))
         assert abs(a.mean() - b.mean()) < 5 * se, k
+
+
+def test_chain_traces_of_independent_replicates():
+    """Heat 0 without swaps runs independent replicates: every chain has a
+    full trace of its own state, the reported cold chain is chain 0 (all at
+    beta 1), the replicates' random streams differ, and each chain's lnL
+    trace is its cached likelihood (incremental = full after the run)."""
+    c = dna_case(16, 300, seed=18, model="gtr", alpha=0.5, num_categories=4)
+    m = make(c, model="gtr", precision="f32", num_categories=4, num_chains=4, heat=0.0,
+             swap_every=0, sample_every=10)
+    m.set_parameters(rates=np.ones(6), frequencies=c.pi, alpha=0.5, birth_rate=2.0)
+    m.run(2000)
+    assert m.check() < 1e-12
+    for name in ("lnl", "root_height", "kappa_or_rate0"):
+        np.testing.assert_array_equal(m.trace(name, chain=0), m.trace(name))
+        for k in range(4):
+            assert m.trace(name, chain=k).size == 200
+    lnl = [m.trace("lnl", chain=k) for k in range(4)]
+    assert all(np.isfinite(t).all() for t in lnl)
+    assert not np.array_equal(lnl[0], lnl[1])
+    assert m.swaps() == (0, 0)
+    from aspartik_gb300._native import B3GError
+
+    with pytest.raises(B3GError):
+        m.trace("lnl", chain=4)
+    m.close()
