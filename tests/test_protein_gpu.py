@@ -219,3 +219,47 @@ def test_tensor_core_groups_agree(rng, taxa, sites, K):
             g.accept()
     for g in (g1, g2, g64):
         g.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2])
+def test_tensor_core_single_entry_lists_and_eight_categories(groups):
+    """Root-only dirty lists (one entry: one run, the second group idle),
+    then lists of the root's internal child and the root, on the tensor
+    cores with eight Gamma categories and with one pattern (a single
+    tile, 127 padded rows), each against the FP64 form."""
+    for taxa, sites, K in ((24, 400, 8), (12, 1, 2)):
+        c = protein_case(taxa, sites, seed=61 + K, alpha=0.6, num_categories=K)
+        tree = O.DatedTree(c.tree.parents, c.tree.heights)
+        tc = make20_env(c, K, B3G_TC20_GROUPS=groups)
+        g64 = make20(c, "f64", K)
+        for g in (tc, g64):
+            g.set_reversible(c.rates, c.pi)
+            g.set_gamma(0.6)
+            g.propose_lengths(*whole(tree), 1.0)
+            g.accept()
+        tree.accept()
+        root = tree.root()
+        l, r = tree.children_of(root)
+        top = max(tree.heights[l], tree.heights[r])
+        for step, h in enumerate((top + 0.3, top + 0.05, top + 1.1)):
+            tree.set_height(root, h)
+            inc = lists_and_lengths(tree)
+            assert len(inc[0]) == 1
+            for g in (tc, g64):
+                g.propose_lengths(*inc, 1.0)
+            assert tc.log_likelihood() == pytest.approx(g64.log_likelihood(), rel=F32_TOL), step
+            tree.accept()
+            for g in (tc, g64):
+                g.accept()
+        inner = next((v for v in (l, r) if v >= tree.num_leaves), None)
+        if inner is not None:
+            a, b = tree.children_of(inner)
+            lo, hi = max(tree.heights[a], tree.heights[b]), tree.heights[root]
+            tree.set_height(inner, lo + 0.5 * (hi - lo))
+            inc = lists_and_lengths(tree)
+            assert len(inc[0]) == 2
+            for g in (tc, g64):
+                g.propose_lengths(*inc, 1.0)
+            assert tc.log_likelihood() == pytest.approx(g64.log_likelihood(), rel=F32_TOL)
+        tc.close()
+        g64.close()
