@@ -87,10 +87,10 @@ __global__ void __launch_bounds__(256) gemm_kernel(const float *__restrict__ A,
 	}
 }
 
-// dZ = dA * gelu'(Z)
-__global__ void gelu_backward_kernel(const float *__restrict__ dA,
-				     const float *__restrict__ Z,
-				     float *__restrict__ dZ, uint32_t count)
+// dZ = dA * gelu'(Z), element by element; dZ may be dA (in place), so
+// neither is restrict-qualified
+__global__ void gelu_backward_kernel(const float *dA, const float *__restrict__ Z,
+				     float *dZ, uint32_t count)
 {
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < count)
