@@ -442,7 +442,7 @@ size_t orc_deduplicate(const uint8_t *msa, size_t L, size_t N,
 		       uint8_t *leaves, uint32_t *weights,
 		       uint32_t *site_to_pattern)
 {
-	uint8_t *cols = malloc(N * L ? N * L : 1); /* site-major copy */
+	uint8_t *cols = malloc(N * L > 0 ? N * L : 1); /* site-major copy */
 	for (size_t s = 0; s < N; s++)
 		for (size_t l = 0; l < L; l++)
 			cols[s * L + l] = msa[l * N + s];
