@@ -63,29 +63,6 @@ __device__ __forceinline__ void group_sync(uint32_t g)
 	else
 		asm volatile("bar.sync 2, 128;" ::: "memory");
 }
-// Same barrier, returning whether any of the group's threads passed v.
-__device__ __forceinline__ bool group_any(uint32_t g, bool v)
-{
-	uint32_t r;
-	if (g == 0)
-		asm volatile("{\n\t.reg .pred p, q;\n\t"
-			     "setp.ne.u32 p, %1, 0;\n\t"
-			     "bar.red.or.pred q, 1, 128, p;\n\t"
-			     "selp.u32 %0, 1, 0, q;\n\t}"
-			     : "=r"(r)
-			     : "r"((uint32_t)v)
-			     : "memory");
-	else
-		asm volatile("{\n\t.reg .pred p, q;\n\t"
-			     "setp.ne.u32 p, %1, 0;\n\t"
-			     "bar.red.or.pred q, 2, 128, p;\n\t"
-			     "selp.u32 %0, 1, 0, q;\n\t}"
-			     : "=r"(r)
-			     : "r"((uint32_t)v)
-			     : "memory");
-	return r != 0;
-}
-
 // One block per table (entry, side, category), 768 threads: P in FP64 (as
 // ptab20_kernel), then the FP32 tip rows [21][20] (transposed, ones row)
 // and the hi/lo operand blocks B[i][k] = P[i][k] in the layout above.
@@ -257,13 +234,12 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 			const NodeOp op = ops[e];
 			const uint32_t ids[2] = {op.left, op.right};
 			const bool any = !(ids[0] & kTipBit) || !(ids[1] & kTipBit);
-			const bool ok_in = tc::mbar_wait(lb, lphase, kTcWaitLimit);
+			// a wait that gives up only marks the thread failed: the group
+			// keeps to its barriers and the run's closing barrier stops the
+			// CTA (the values computed meanwhile are discarded)
+			failed |= !tc::mbar_wait(lb, lphase, kTcWaitLimit);
 			lphase ^= 1u;
 			pending = false;
-			if (group_any(g, !ok_in)) {
-				failed = true;
-				break;
-			}
 			// this thread's rows: a tip side's final value from its table,
 			// an internal side's partial row from the copied block
 			float v[2][S];
@@ -344,12 +320,8 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 					}
 					tc::mma_commit(mb);
 				}
-				const bool ok = tc::mbar_wait(mb, mphase, kTcWaitLimit);
+				failed |= !tc::mbar_wait(mb, mphase, kTcWaitLimit);
 				mphase ^= 1u;
-				if (group_any(g, !ok)) {
-					failed = true;
-					break;
-				}
 				// operands consumed: the group's next entry's inputs
 				// travel during this epilogue
 				if (next) {
