@@ -127,7 +127,8 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	use_tc20_ = f32_ && S_ == 20;
 	if (const char *env = std::getenv("B3G_TC20"))
 		use_tc20_ = use_tc20_ && std::atoi(env) != 0;
-	// groups of 128 threads per tensor-core CTA (B3G_TC20_GROUPS = 1 or 2)
+	// groups of 128 threads per tensor-core CTA (B3G_TC20_GROUPS = 1 or 2;
+	// default: chosen per launch from the grid size)
 	if (const char *env = std::getenv("B3G_TC20_GROUPS")) {
 		const int gr = std::atoi(env);
 		if (gr == 1 || gr == 2)
@@ -710,10 +711,17 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		tp.L = L_;
 		// the list, then the tile's tip codes, in shared memory when they
 		// fit beside the operand areas at 4 / groups CTAs per SM
-		tp.groups = tc20_groups_;
-		const size_t budget = smem_budget(256u * tc20_groups_);
+		// two groups (on independent entries of a run) unless the grid
+		// holds six or more CTAs per SM, where one group per CTA and up to
+		// four CTAs per SM hide the per-entry latency as well (measured:
+		// two groups faster at 1 and 4.1 CTAs per SM, one at 10.2)
+		const uint32_t groups =
+			tc20_groups_ ? tc20_groups_
+				     : ((ldp_ / 128u) * C_ < 6u * num_sms_ ? 2u : 1u);
+		tp.groups = groups;
+		const size_t budget = smem_budget(256u * groups);
 		const size_t ops_bytes = (size_t)n * sizeof(NodeOp);
-		size_t used = prune20tc_smem(tc20_groups_, false, n, false, L_);
+		size_t used = prune20tc_smem(groups, false, n, false, L_);
 		tp.ops_smem = used + ops_bytes <= budget ? 1u : 0u;
 		used += tp.ops_smem ? ops_bytes : 0;
 		tp.tips_smem = used + (size_t)L_ * 128u <= budget ? 1u : 0u;

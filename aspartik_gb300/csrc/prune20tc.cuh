@@ -8,7 +8,9 @@
 // tcgen05 MMAs of kind::tf32 with FP32 accumulation in tensor memory, in the
 // 3xTF32 split form: x = x_hi + x_lo, P = P_hi + P_lo (TF32 heads and
 // tails, each rounded to nearest) and out = x_hi P_hi + x_hi P_lo +
-// x_lo P_hi, which keeps FP32-level accuracy without a bias.  The algorithmic flops are
+// x_lo P_hi, which keeps FP32-level accuracy without a bias: per K step one
+// N = 64 MMA x_hi [P_hi; P_lo] and one N = 32 MMA adding x_lo P_hi to the
+// first half, the halves summed in the epilogue.  The algorithmic flops are
 // 2 S^2 per internal child and (pattern, category); the tensor core
 // executes 3 x (32/20) x (24/20) times that.
 //
@@ -168,15 +170,19 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 			tc::mbar_init(tc::smem_u32(&lbar[k]), 1);
 		}
 	if (warp == 0)
-		tc::tmem_alloc(tc::smem_u32(&holder), 64 * kG);
+		tc::tmem_alloc(tc::smem_u32(&holder), 128 * kG);
 	tc::fence_proxy_async_smem(); // the zeroed areas before the first copies
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
-	// this group's accumulators: columns [64 g, 64 g + 64), left then right
-	const uint32_t tmem = holder + 64u * g;
+	// this group's accumulators: columns [128 g, 128 g + 128), 64 per side:
+	// [0, 32) x_hi P_hi + x_lo P_hi, [32, 64) x_hi P_lo
+	const uint32_t tmem = holder + 128u * g;
 	const uint32_t lane_base = (32u * (warp & 3u)) << 16;
+	// the hi and lo B blocks are adjacent (SBO 768 throughout), so one
+	// N = 64 MMA multiplies x_hi by both
 	constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
+	constexpr uint32_t idesc2 = tc::idesc_tf32(kTcRows, 2 * kTcN);
 	// operand descriptors of K step 0: [child][hi, lo]
 	uint64_t dA[2][2], dB[2][2];
 #pragma unroll
@@ -309,12 +315,10 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 						// the next K step (+256 B) adds 16
 #pragma unroll
 						for (uint32_t s = 0; s < 3; s++) {
-							// x_hi P_hi, x_hi P_lo, x_lo P_hi
-							tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
-								     dB[j][0] + 16 * s, idesc, s != 0);
-							tc::mma_tf32(tmem + 32 * j, dA[j][0] + 16 * s,
-								     dB[j][1] + 16 * s, idesc, 1);
-							tc::mma_tf32(tmem + 32 * j, dA[j][1] + 16 * s,
+							// x_hi [P_hi; P_lo], then x_lo P_hi
+							tc::mma_tf32(tmem + 64 * j, dA[j][0] + 16 * s,
+								     dB[j][0] + 16 * s, idesc2, s != 0);
+							tc::mma_tf32(tmem + 64 * j, dA[j][1] + 16 * s,
 								     dB[j][0] + 16 * s, idesc, 1);
 						}
 					}
@@ -334,11 +338,17 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 				for (uint32_t j = 0; j < 2; j++) {
 					if (ids[j] & kTipBit)
 						continue;
-					const uint32_t ta = tmem + lane_base + 32 * j;
+					const uint32_t ta = tmem + lane_base + 64 * j;
+					float lo[S];
 					tc::tmem_ld16(ta, v[j]);
 					tc::tmem_ld4(ta + 16, v[j] + 16);
+					tc::tmem_ld16(ta + 32, lo);
+					tc::tmem_ld4(ta + 48, lo + 16);
+					tc::tmem_wait_ld();
+#pragma unroll
+					for (int i = 0; i < S; i++)
+						v[j][i] += lo[i];
 				}
-				tc::tmem_wait_ld();
 			}
 			float y[S];
 #pragma unroll
@@ -399,7 +409,7 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 	__syncthreads();
 	tc::fence_after_sync();
 	if (warp == 0)
-		tc::tmem_dealloc(holder, 64 * kG);
+		tc::tmem_dealloc(holder, 128 * kG);
 }
 
 // Category mixing of the root (FP32 form: values with power-of-two
