@@ -183,16 +183,17 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 	// N = 64 MMA multiplies x_hi by both
 	constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
 	constexpr uint32_t idesc2 = tc::idesc_tf32(kTcRows, 2 * kTcN);
-	// operand descriptors of K step 0: [child][hi, lo]
-	uint64_t dA[2][2], dB[2][2];
+	// operand descriptors of K step 0: A [child][hi, lo]; B [child], its hi
+	// block (the N = 64 form reaches the lo block after it)
+	uint64_t dA[2][2], dB[2];
 #pragma unroll
-	for (uint32_t j = 0; j < 2; j++)
+	for (uint32_t j = 0; j < 2; j++) {
 #pragma unroll
-		for (uint32_t h = 0; h < 2; h++) {
+		for (uint32_t h = 0; h < 2; h++)
 			dA[j][h] = tc::smem_desc(tc::smem_u32(sA + (2 * j + h) * kTcA), 128,
 						 kTcSboA);
-			dB[j][h] = tc::smem_desc(tc::smem_u32(sB + (2 * j + h) * kTcB), 128, 768);
-		}
+		dB[j] = tc::smem_desc(tc::smem_u32(sB + 2 * j * kTcB), 128, 768);
+	}
 
 	// Inputs of entry e, copied by thread 0 of the group: an internal
 	// side's 128 partial rows (contiguous) into its A-lo block, where they
@@ -317,9 +318,9 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 						for (uint32_t s = 0; s < 3; s++) {
 							// x_hi [P_hi; P_lo], then x_lo P_hi
 							tc::mma_tf32(tmem + 64 * j, dA[j][0] + 16 * s,
-								     dB[j][0] + 16 * s, idesc2, s != 0);
+								     dB[j] + 16 * s, idesc2, s != 0);
 							tc::mma_tf32(tmem + 64 * j, dA[j][1] + 16 * s,
-								     dB[j][0] + 16 * s, idesc, 1);
+								     dB[j] + 16 * s, idesc, 1);
 						}
 					}
 					tc::mma_commit(mb);
