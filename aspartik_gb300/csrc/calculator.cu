@@ -131,8 +131,10 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 	// default: chosen per launch from the grid size)
 	if (const char *env = std::getenv("B3G_TC20_GROUPS")) {
 		const int gr = std::atoi(env);
-		if (gr == 1 || gr == 2)
+		if (gr == 1 || gr == 2) {
 			tc20_groups_ = static_cast<uint32_t>(gr);
+			tc20_groups_fixed_ = true;
+		}
 	}
 	use_direct_ = f32_ && S_ == 4 && (C_ == 1 || C_ == 2 || C_ == 4);
 	if (const char *env = std::getenv("B3G_DIRECT"))
@@ -1146,8 +1148,22 @@ uint32_t Calculator::autotune(const uint32_t *internals,
 	if (S_ == 20) {
 		if (!d_tc_tab_) // built without tensor-core buffers
 			return 0;
+		// tensor cores with one and with two thread groups per CTA
+		// (unless B3G_TC20_GROUPS fixed it), then the CUDA-core walk
 		use_tc20_ = true;
-		const float tc = trial();
+		float tc = INFINITY;
+		uint32_t best_groups = tc20_groups_;
+		for (const uint32_t gr : {1u, 2u}) {
+			if (tc20_groups_fixed_ && gr != tc20_groups_)
+				continue;
+			tc20_groups_ = gr;
+			const float t = trial();
+			if (t < tc) {
+				tc = t;
+				best_groups = gr;
+			}
+		}
+		tc20_groups_ = best_groups;
 		use_tc20_ = false;
 		const float cc = trial();
 		use_tc20_ = tc <= cc;

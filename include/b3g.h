@@ -211,7 +211,8 @@ B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
  * (normally the whole tree) with each launch configuration of this
  * calculator's form and keeps the fastest: patterns per tile of the
  * run-synchronous walk (32, 64 or 128; four-state FP32), or tensor cores
- * against CUDA cores (20-state FP32).  Every trial proposal is rejected, so
+ * (one or two thread groups per CTA) against CUDA cores (20-state FP32).
+ * Every trial proposal is rejected, so
  * call it between steps; the accepted state is unchanged.  `choice`
  * receives the tile, or 1 (tensor cores) / 0 (CUDA cores); the FP64 form
  * has nothing to tune and returns 0. */
