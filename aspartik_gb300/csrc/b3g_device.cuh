@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "index_width.hpp"
+
 namespace b3g {
 
 constexpr uint32_t kTipBit = 0x80000000u;
@@ -78,6 +80,9 @@ struct PruneParams {
 	uint32_t scale_ln;
 	uint32_t num_leaves; // rows of tips
 	uint32_t tips_smem;  // stage the block's tip codes in shared memory
+	// 64-bit element indices whatever num_leaves says (the slot ids come
+	// from a caller whose buffers may hold more than 2 * num_leaves slots)
+	uint32_t wide_index;
 	// run-synchronous walk (prune4_runs_kernel): runs[0..n_runs] are the
 	// first entries of the runs of mutually independent entries, then n
 	const uint32_t *runs;

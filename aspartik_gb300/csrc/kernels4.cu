@@ -566,7 +566,9 @@ __global__ void __launch_bounds__(512) prune4_kernel(PruneParams prm)
 	T y = v4_make<T, R>(0, 0, 0, 0);
 	int32_t cnt = 0;
 	for (uint32_t i = 0; i < prm.n;) {
-		const uint32_t avail = prm.ops[i].pad;
+		// a run never reaches past the end of the list, whatever the
+		// entry says
+		const uint32_t avail = min(prm.ops[i].pad, prm.n - i);
 		// FP64 partials take twice the registers: batches of at most 2
 		constexpr uint32_t kMaxU = sizeof(R) == 4 ? 4u : 2u;
 		if (kMaxU >= 4 && avail >= 4) {
@@ -665,7 +667,7 @@ __global__ void __launch_bounds__(512) prune4_plain_kernel(PruneParams prm)
 	double4_32a y = v4_make<double4_32a, double>(0, 0, 0, 0);
 	int32_t cnt = 0;
 	for (uint32_t i = 0; i < prm.n;) {
-		if (prm.ops[i].pad >= 2) {
+		if (prm.ops[i].pad >= 2 && i + 1 < prm.n) {
 			plain_batch<2>(prm, partials, ptab, i, p, c, y, cnt);
 			i += 2;
 		} else {
@@ -711,7 +713,8 @@ static cudaError_t launch_prune4_t(const PruneParams &p, uint32_t tile,
 	if (p.tips_smem)
 		smem += (size_t)p.num_leaves * tile;
 	// 32-bit element indices when every slot index fits
-	const bool narrow = (uint64_t)p.num_leaves * 2 * p.C * p.ldp < (1ull << 31);
+	const bool narrow =
+		!p.wide_index && narrow_index((uint64_t)p.num_leaves * 2, p.C, p.ldp);
 	auto kern = narrow ? prune4_kernel<VT, kPow2, uint32_t>
 			   : prune4_kernel<VT, kPow2, size_t>;
 	if (smem > 48 * 1024) {

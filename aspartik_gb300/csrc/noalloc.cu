@@ -135,6 +135,8 @@ extern "C" B3G_API b3g_status b3g_prune_noalloc(const b3g_prune_buffers *b,
 	pp.scale_threshold = std::exp(-static_cast<double>(b->scale_ln));
 	pp.scale_mult = std::exp(static_cast<double>(b->scale_ln));
 	pp.log_inv_c = std::log(1.0 / static_cast<double>(C));
+	// the slot ids index buffers of unknown size: 64-bit element indices
+	pp.wide_index = b3g::noalloc_narrow_index(C, b->ldp) ? 0u : 1u;
 	e = b3g::launch_prune4(pp, b->precision == B3G_PRECISION_F32, tile, s);
 	if (e != cudaSuccess)
 		return fail(B3G_ERR_CUDA,
