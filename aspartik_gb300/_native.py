@@ -79,7 +79,7 @@ class PruneBuffers(ct.Structure):
     ]
 
 
-OP_COUNT = 10
+OP_COUNT = 14
 
 
 class McmcConfig(ct.Structure):
@@ -179,6 +179,7 @@ SIGNATURES = {
     "b3g_batch_run": (ct.c_int, [_vp]),
     "b3g_batch_log_likelihoods": (ct.c_int, [_vp, _f64p]),
     "b3g_batch_last_ms": (ct.c_int, [_vp, _f32p]),
+    "b3g_mcmc_set_tuning": (ct.c_int, [_vp, ct.c_uint32, ct.c_double]),
     "b3g_mcmc_create": (ct.c_int, [ct.POINTER(McmcConfig), ct.c_uint32, ct.c_uint32, _u8p,
                                    _u32p, _u32p, _f64p, ct.POINTER(_vp)]),
     "b3g_mcmc_destroy": (None, [_vp]),

@@ -436,7 +436,13 @@ void Mcmc::propose(Chain &ch)
 					t.replace_child(gp, parent, sibling);
 					t.replace_child(new_parent, new_child, parent);
 				}
-				ch.hastings = -std::log(double(dest.size()));
+				// The forward move picks one of |dest| destinations and
+				// the reverse (upward) move is deterministic, so
+				// q(x | x') / q(x' | x) = |dest|.  The reference's
+				// _subtree_slide.py:94 returns -log(len(destinations))
+				// here, which biases the tree; that sign is not copied
+				// (BEAST's SubtreeSlideOperator uses +log).
+				ch.hastings = std::log(double(dest.size()));
 			}
 		}
 		t.set_height(parent, new_h);
@@ -471,6 +477,54 @@ void Mcmc::propose(Chain &ch)
 		ch.hastings = -std::log(s);
 		clock_rates(ch);
 		t.mark_all_edges_updated();
+		break;
+	}
+	case kOpNodeSlide: { // _node_slide.py: uniform between parent and children
+		if (t.num_internals() < 2) {
+			ch.status = 1;
+			break;
+		}
+		// random_nonroot_internal (tree.rs:799-809)
+		uint32_t node;
+		do
+			node = t.num_leaves() + ch.rng.below(t.num_internals());
+		while (node == t.root());
+		const double upper = t.height(t.parent_of(node));
+		const double lower = std::max(t.height(t.left(node)), t.height(t.right(node)));
+		t.set_height(node, (upper - lower) * ch.rng.uniform() + lower);
+		break;
+	}
+	case kOpRootSlide: { // _root.py: root height scaled above its older child
+		const uint32_t root = t.root();
+		const double s = scale_factor();
+		const double lower = std::max(t.height(t.left(root)), t.height(t.right(root)));
+		t.set_height(root, (t.height(root) - lower) * s + lower);
+		ch.hastings = -std::log(s);
+		break;
+	}
+	case kOpUpDown: { // _updown.py with up = the tree, down = the birth rate
+		const double s = scale_factor();
+		t.scale(s);
+		ch.birth_rate.set(ch.birth_rate.v / s);
+		// log(s) (dims up - dims down - 2): DatedTree::scale counts the
+		// internals, Real::scale one value (tree.rs:335-348, real.rs:31)
+		ch.hastings = std::log(s) * (double(t.num_internals()) - 1.0 - 2.0);
+		break;
+	}
+	case kOpWideExchange: { // _tree_exchange.py BeastWideExchange
+		const uint32_t a = random_nonroot(t, ch.rng);
+		uint32_t b;
+		do
+			b = random_nonroot(t, ch.rng);
+		while (b == a);
+		const uint32_t pa = t.parent_of(a), pb = t.parent_of(b);
+		if (pa != pb && a != pb && b != pa && t.height(a) < t.height(pb) &&
+		    t.height(b) < t.height(pa)) {
+			if (!t.swap_parents(a, b))
+				ch.status = 1;
+		} else {
+			ch.status = 1;
+		}
 		break;
 	}
 	default:
@@ -738,15 +792,40 @@ void Mcmc::tune()
 	const double r = 1.0 / std::sqrt(static_cast<double>(tune_rounds_));
 	for (uint32_t k = 0; k < kOpCount; ++k) {
 		OpStats &o = ops_[k];
-		if (k == kOpNarrowExchange)
+		if (k == kOpNarrowExchange || k == kOpNodeSlide || k == kOpWideExchange)
 			continue; // not tunable
 		const double n = double(o.window_accepts + o.window_rejects);
 		if (n == 0.0)
 			continue;
 		const double acc = double(o.window_accepts) / n;
-		o.tuning = std::clamp(o.tuning + r * (0.234 - acc), 0.01, 0.99);
+		if (k == kOpSubtreeSlide) {
+			// SubtreeSlide's factor multiplies the slide, so a larger
+			// value is a bolder move: it grows when the acceptance is
+			// above the target and shrinks below it, in log space (as
+			// BEAST tunes its size), down to the node spacings of large
+			// trees.  The reference applies the scale operators' rule
+			// (operators/mod.rs:165-193, a larger factor being a smaller
+			// move) to it as well, which drives a rarely accepted slide
+			// to ever larger moves; that direction is not copied.
+			o.tuning = std::clamp(o.tuning * std::exp(4.0 * r * (acc - 0.234)),
+					      1e-6, 10.0);
+		} else {
+			o.tuning = std::clamp(o.tuning + r * (0.234 - acc), 0.01, 0.99);
+		}
 		o.window_accepts = o.window_rejects = 0;
 	}
+}
+
+void Mcmc::set_tuning(uint32_t op, double tuning)
+{
+	if (op >= kOpCount)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "bad operator");
+	const bool sub = op == kOpSubtreeSlide;
+	if (!std::isfinite(tuning) || tuning < (sub ? 1e-6 : 0.01) ||
+	    tuning > (sub ? 10.0 : 0.99))
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "tuning out of range (SubtreeSlide 1e-6..10, others 0.01..0.99)");
+	ops_[op].tuning = tuning;
 }
 
 void Mcmc::record()

@@ -5,8 +5,9 @@
 // likelihood -> Metropolis-Hastings -> accept or reject of every parameter,
 // the tree and the likelihood.  Operators follow python/aspartik/b3/
 // operators (TreeScale, ScaleReal, SubtreeSlide, BeastNarrowExchange,
-// DeltaExchange) and the priors python/aspartik/b3/config/__init__.py:
-// 660-800 (Yule, LogNormal, SymmetricDirichlet).  Beyond the reference it
+// BeastWideExchange, NodeSlide, RootSlide, UpDown, DeltaExchange) and the
+// priors python/aspartik/b3/config/__init__.py:660-800 (Yule, LogNormal,
+// SymmetricDirichlet).  Beyond the reference it
 // runs several chains at once (independent replicates or Metropolis-coupled
 // temperatures) and evaluates the proposals of all chains before reading
 // any result back, so their GPU work overlaps.
@@ -96,6 +97,10 @@ enum OpKind : uint32_t {
 	kOpDeltaFreqs,
 	kOpRelaxedCategory, // one edge's relaxed-clock category
 	kOpScaleClockSd,    // the relaxed clock's LogNormal sd
+	kOpNodeSlide,       // one internal height between parent and children
+	kOpRootSlide,       // the root height, scaled above its older child
+	kOpUpDown,          // tree heights up, birth rate down (or reverse)
+	kOpWideExchange,    // parents of two random nodes swapped
 	kOpCount
 };
 
@@ -199,6 +204,9 @@ class Mcmc {
 	}
 	size_t chain_trace_size() const { return chain_trace_.size(); }
 	void op_stats(uint32_t op, uint64_t out[4], double *tuning) const;
+	// the operator's tuning parameter (a start value, e.g. carried over
+	// from a burn-in run)
+	void set_tuning(uint32_t op, double tuning);
 	// samples: steps[n], parents[n][nodes], heights[n][nodes],
 	// parameters[n][kSampleParams]
 	uint64_t num_samples() const { return sample_steps_.size(); }

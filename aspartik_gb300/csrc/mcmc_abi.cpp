@@ -205,6 +205,12 @@ B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
 	});
 }
 
+B3G_API b3g_status b3g_mcmc_set_tuning(b3g_mcmc *mcmc, uint32_t op,
+				       double tuning)
+{
+	return guarded([&] { mcmc_of(mcmc)->set_tuning(op, tuning); });
+}
+
 B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
 				  uint64_t *accepted)
 {

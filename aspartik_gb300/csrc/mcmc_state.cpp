@@ -7,7 +7,7 @@
 // the reference's (its own operators, xoshiro256** RNGs, several chains), so
 // the layout is its own; it holds everything later steps depend on:
 //
-//   "B3GMCST1", u32 version = 1, u32 chains, leaves, model, categories,
+//   "B3GMCST1", u32 version = 2, u32 chains, leaves, model, categories,
 //   clock categories, precision, reserved
 //   u64 step, swaps tried, swaps accepted; u32 tuning rounds, reserved
 //   u64 swap RNG state[4]
@@ -16,7 +16,9 @@
 //   per chain: u32 index, run-walk tile, run-walk block, reserved; f64 beta,
 //   lnL, prior, kappa, alpha, birth rate, clock sd; u32 n, f64 rates[n];
 //   u32 n, f64 frequencies[n]; u64 RNG state[4]; u32 parents[2L-1];
-//   f64 heights[2L-1]; with a relaxed clock u32 edge categories[2L-1]
+//   u32 children[2L-2] (each internal's children in the order the
+//   operators walk them); f64 heights[2L-1]; with a relaxed clock u32 edge
+//   categories[2L-1]
 //   u64 FNV-1a hash of everything before it
 //
 // Native byte order; a checkpoint is read back on the same kind of host.
@@ -35,7 +37,7 @@ namespace b3g {
 namespace {
 
 constexpr char kMagic[8] = {'B', '3', 'G', 'M', 'C', 'S', 'T', '1'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2; // 2: fourteen operator kinds, child order
 
 uint64_t fnv1a(const uint8_t *p, size_t n)
 {
@@ -131,6 +133,7 @@ std::vector<uint8_t> Mcmc::dump() const
 		ch.rng.get_state(rs);
 		w.put_n(rs, 4);
 		w.put_n(ch.tree->parents().data(), ch.tree->num_nodes());
+		w.put_n(ch.tree->children().data(), ch.tree->children().size());
 		w.put_n(ch.tree->heights().data(), ch.tree->num_nodes());
 		if (cfg_.clock_categories)
 			w.put_n(ch.edge_cat.data(), ch.tree->num_nodes());
@@ -192,7 +195,7 @@ void Mcmc::load(const uint8_t *state, size_t size)
 		double v[7];
 		std::vector<double> rates, freqs;
 		uint64_t rs[4];
-		std::vector<uint32_t> parents, cats;
+		std::vector<uint32_t> parents, children, cats;
 		std::vector<double> heights;
 		std::unique_ptr<DatedTree> tree;
 	};
@@ -213,8 +216,10 @@ void Mcmc::load(const uint8_t *state, size_t size)
 		r.get_n(sv.freqs.data(), n);
 		r.get_n(sv.rs, 4);
 		sv.parents.resize(nodes);
+		sv.children.resize(nodes - 1);
 		sv.heights.resize(nodes);
 		r.get_n(sv.parents.data(), nodes);
+		r.get_n(sv.children.data(), nodes - 1);
 		r.get_n(sv.heights.data(), nodes);
 		if (cfg_.clock_categories) {
 			sv.cats.resize(nodes);
@@ -229,6 +234,9 @@ void Mcmc::load(const uint8_t *state, size_t size)
 		if (!sv.tree->validate())
 			throw Error(B3G_ERR_INVALID_ARGUMENT,
 				    "checkpoint holds an invalid tree");
+		if (!sv.tree->set_child_order(sv.children.data()))
+			throw Error(B3G_ERR_INVALID_ARGUMENT,
+				    "checkpoint's child order contradicts its parents");
 		for (uint32_t v = 0; v < (uint32_t)sv.cats.size(); ++v)
 			if (sv.cats[v] >= cfg_.clock_categories &&
 			    v != sv.tree->root())

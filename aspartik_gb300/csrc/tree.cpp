@@ -47,6 +47,18 @@ DatedTree::DatedTree(const uint32_t *parents, const double *heights,
 		throw std::invalid_argument("invalid tree (heights or links)");
 }
 
+bool DatedTree::set_child_order(const uint32_t *children)
+{
+	for (uint32_t k = 0; k < children_.size(); k += 2) {
+		const uint32_t a = children[k], b = children[k + 1];
+		const uint32_t x = children_[k], y = children_[k + 1];
+		if (!((a == x && b == y) || (a == y && b == x)))
+			return false;
+	}
+	children_.assign(children, children + children_.size());
+	return true;
+}
+
 uint32_t DatedTree::other_child(uint32_t parent, uint32_t child) const
 {
 	const uint32_t l = left(parent), r = right(parent);

@@ -60,6 +60,13 @@ class DatedTree {
 	void accept();
 	void reject();
 
+	// children[2 (v - L) + k], k = 0, 1: the order of every internal's
+	// children (operators walk children in this order, so it is part of a
+	// chain's state)
+	const std::vector<uint32_t> &children() const { return children_; }
+	// Sets that order; returns false, changing nothing, unless every
+	// internal's pair is its two children under parents().
+	bool set_child_order(const uint32_t *children);
 	const std::vector<uint32_t> &parents() const { return parents_; }
 	const std::vector<double> &heights() const { return heights_; }
 	double root_height() const { return heights_[root_]; }

@@ -18,14 +18,21 @@ from ._native import check, lib
 MODELS = {"hky": 0, "gtr": 1}
 OPERATORS = ["tree_scale", "subtree_slide", "narrow_exchange", "scale_kappa",
              "scale_alpha", "scale_birth_rate", "delta_rates", "delta_frequencies",
-             "relaxed_category", "scale_clock_sd"]
+             "relaxed_category", "scale_clock_sd", "node_slide", "root_slide", "up_down",
+             "wide_exchange"]
 TRACE_FIELDS = ["lnl", "prior", "posterior", "root_height", "kappa_or_rate0", "alpha",
                 "tree_length", "clock_sd"]
 
-# the operator mix of the reference's config recipe for a Yule + GTR model
-# (python/aspartik/b3/config/__init__.py:660-730, 853-858)
-GTR_WEIGHTS = dict(tree_scale=3, subtree_slide=30, narrow_exchange=30, scale_alpha=1,
-                   scale_birth_rate=3, delta_rates=1, delta_frequencies=1)
+# the operator mix of the reference's config recipe for a Yule + GTR model:
+# the tree operators of its "beauti1_classic" mix (TreeScale 3, SubtreeSlide
+# 30, BeastNarrowExchange 30, BeastWideExchange 3, RootSlide 3, NodeSlide 30;
+# python/aspartik/b3/config/__init__.py:849-858), UpDown of the tree against
+# the Yule birth rate (the pairing of the "beauti1_default" mix, :835-845,
+# with the birth rate in place of the clock rate) and the parameter
+# operators of the recipe (:660-730)
+GTR_WEIGHTS = dict(tree_scale=3, subtree_slide=30, narrow_exchange=30, wide_exchange=3,
+                   root_slide=3, node_slide=30, up_down=3, scale_alpha=1, scale_birth_rate=3,
+                   delta_rates=1, delta_frequencies=1)
 # branch-length scale and kappa moves only
 HKY_SCALE_KAPPA_WEIGHTS = dict(tree_scale=3, scale_kappa=1)
 
@@ -156,6 +163,12 @@ class Mcmc:
             out[name] = dict(accepts=counts[0], rejects=counts[1], aborts=counts[2],
                              prior_rejects=counts[3], tuning=tuning.value)
         return out
+
+    def set_tuning(self, tunings: dict) -> None:
+        """Start values of operators' tuning parameters by name (e.g. the
+        ``tuning`` entries of another run's ``operator_stats``)."""
+        for name, value in tunings.items():
+            check(lib.b3g_mcmc_set_tuning(self._h, OPERATORS.index(name), float(value)))
 
     def swaps(self) -> tuple[int, int]:
         t, a = ct.c_uint64(), ct.c_uint64()

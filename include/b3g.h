@@ -299,7 +299,11 @@ B3G_API b3g_status b3g_hetero_reject(b3g_hetero *h);
  * likelihood work), device likelihood, Metropolis-Hastings, accept/reject
  * of tree, parameters and calculator -- with the operators of
  * python/aspartik/b3/operators (TreeScale, SubtreeSlide, BeastNarrowExchange,
- * ScaleReal, DeltaExchange) and the priors of the reference's config
+ * BeastWideExchange, NodeSlide, RootSlide, UpDown, ScaleReal, DeltaExchange;
+ * SubtreeSlide's downward Hastings term is +log of the destination count,
+ * where the reference's Python operator has -log, and its slide size is
+ * tuned toward 0.234 acceptance, growing when accepted more often, where
+ * the reference's tuning rule drives it the other way) and the priors of the reference's config
  * recipe (Yule, LogNormal, SymmetricDirichlet).  Several chains run at once
  * (replicates, or Metropolis-coupled temperatures beta_i = 1/(1 + heat*i));
  * every chain's device work of a step is queued before any result is read.
@@ -320,7 +324,11 @@ enum {
 	B3G_OP_DELTA_FREQUENCIES = 7,
 	B3G_OP_RELAXED_CATEGORY = 8, /* one edge's relaxed-clock rate category */
 	B3G_OP_SCALE_CLOCK_SD = 9,   /* the relaxed clock's LogNormal sd */
-	B3G_OP_COUNT = 10
+	B3G_OP_NODE_SLIDE = 10,      /* NodeSlide (operators/_node_slide.py) */
+	B3G_OP_ROOT_SLIDE = 11,      /* RootSlide (operators/_root.py) */
+	B3G_OP_UP_DOWN = 12,         /* UpDown(tree, birth rate), _updown.py */
+	B3G_OP_WIDE_EXCHANGE = 13,   /* BeastWideExchange, _tree_exchange.py */
+	B3G_OP_COUNT = 14
 };
 
 /* Trace fields of the cold chain, sampled every sample_every steps. */
@@ -412,6 +420,12 @@ B3G_API b3g_status b3g_mcmc_chain_trace(b3g_mcmc *mcmc, uint32_t chain,
 /* counts = {accepts, rejects, aborts, prior rejects} of one operator. */
 B3G_API b3g_status b3g_mcmc_operator_stats(b3g_mcmc *mcmc, uint32_t op,
 					   uint64_t *counts, double *tuning);
+/* Sets one operator's tuning parameter, e.g. to the values a burn-in run
+ * reached (operators' set_tuning, python/aspartik/b3/__init__.py:109-119):
+ * 0.01..0.99 for the scale and delta operators, 1e-6..10 for SubtreeSlide
+ * (its slide size). */
+B3G_API b3g_status b3g_mcmc_set_tuning(b3g_mcmc *mcmc, uint32_t op,
+				       double tuning);
 B3G_API b3g_status b3g_mcmc_swaps(b3g_mcmc *mcmc, uint64_t *tried,
 				  uint64_t *accepted);
 /* counts = {pilot pairs, stage-1 rejects, stage-2 accepts, stage-2 rejects,
