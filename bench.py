@@ -710,6 +710,68 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def reference_cuda(wl, workload: str, reps: int = 20) -> dict:
+    """The reference's own FP64 CUDA calculators on the same GPU: the
+    kernels of crates/b3/src/calculator/cuda_partials and cuda_propagations
+    (its default GPU calculator), compiled unchanged from the reference tree
+    into oracle/_ref by oracle/build.py::build_ref and driven as the
+    reference's calculators drive them (oracle/ref_cuda.py).  One
+    evaluation of the reference's GammaLikelihood is one whole-tree
+    calculator evaluation per Gamma category (likelihood/gamma.rs:97-169);
+    device time of the launches with the inputs resident, and GB/s by the
+    FP64 byte formula with one-byte scale flags."""
+    try:
+        from oracle import oracle as O
+        from oracle import ref_cuda
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference CUDA driver not importable: {e}"}
+    if not (ref_cuda.available() and ref_cuda.propagations_available()):
+        return {"unavailable": "reference CUDA kernels not built (oracle/_ref)"}
+    spec = wl["spec"]
+    C = spec["categories"]
+    model = O.gtr(wl["rates"], wl["pi"])
+    cats = O.gamma_categories(spec["alpha"], C) if spec["alpha"] else np.ones(1)
+    internals, children, lengths = wl["top"].full()
+    P = int(wl["leaves"].shape[1])
+    L = int(wl["leaves"].shape[0])
+    per_cat, per_cat_prop = [], []
+    part = ref_cuda.RefCudaPartials(0)
+    try:
+        part.setup(ref_cuda.dna_codes_to_ref(wl["leaves"]), 30)
+        for r in cats:
+            mats = np.array([[model.transition(d * r) for d in pair] for pair in lengths])
+            part.propose(internals, children, mats, wl["pi"])
+            part.result()
+            part.time_last(3)  # warm-up
+            per_cat.append(part.time_last(reps))
+    finally:
+        part.close()
+    prop = ref_cuda.RefCudaPropagations(0)
+    try:
+        prop.setup(wl["leaves"], 30)
+        for r in cats:
+            nodes, k, pch, pmats = ref_cuda.propagation_inputs(wl["tree"], model, r, L)
+            prop.propose(nodes, k, pch, pmats, wl["pi"])
+            prop.result()
+            prop.time_last(3)
+            per_cat_prop.append(prop.time_last(reps))
+    finally:
+        prop.close()
+    ms, ms_prop = float(sum(per_cat)), float(sum(per_cat_prop))
+    B64 = schedule.algorithmic_bytes(wl["top"], internals, P, C, 4, w=8, e_b=1, w_p=8)
+    return {"workload": workload, "patterns": P, "categories": C,
+            "partials": {"kernel_ms_per_category": [round(x, 4) for x in per_cat],
+                         "ms_per_evaluation": round(ms, 4),
+                         "GB_s": round(B64 / (ms * 1e-3) / 1e9, 2)},
+            "propagations": {"kernel_ms_per_category": [round(x, 4) for x in per_cat_prop],
+                             "ms_per_evaluation": round(ms_prop, 4),
+                             "GB_s": round(B64 / (ms_prop * 1e-3) / 1e9, 2)},
+            "note": "reference CUDA calculators, FP64: partials (one launch per category, one "
+                    "thread per pattern) and propagations, the default (leaf, propagation "
+                    "and root kernels per category, four threads per pattern); device time, "
+                    "inputs resident, whole tree; GB/s by the FP64 byte formula"}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -739,6 +801,15 @@ def run_reference(args):
     sample = (f"whole-tree evaluations over {Pu} of {P} patterns x {C} categories per step; "
               f"cpu4-restated (reference Rust not buildable): FP64, e^30 rescaling, "
               f"{thr} threads")
+    # beside it, the reference's own CUDA calculators on this GPU
+    ref_gpu = {"unavailable": "no CUDA device"}
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            ref_gpu = reference_cuda(wl, args.workload)
+    except Exception as e:  # noqa: BLE001
+        ref_gpu = {"unavailable": f"{type(e).__name__}: {e}"}
     print(json.dumps({
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -754,6 +825,7 @@ def run_reference(args):
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_cuda": ref_gpu,
     }))
 
 

@@ -15,6 +15,7 @@ beside the oracle.
 
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -41,26 +42,35 @@ def build(verbose: bool = False) -> Path:
     return LIB
 
 
-# the reference tree, read only at build time in the development container;
-# the GPU machine receives the built cubin
-REF_CALC = Path("/root/reference/crates/b3/src/calculator")
-# (reference source directory, wrapper, output): the two CUDA calculators
+# The reference tree is read only at build time: the argument of
+# build_ref, else the B3G_REFERENCE_ROOT environment variable, else the
+# development container's checkout.  The GPU machine receives the built
+# cubins.
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+# (calculator directory under crates/b3/src/calculator, wrapper, output)
 REF_BUILDS = [
-    (REF_CALC / "cuda_partials", HERE / "ref_cuda_partials.cu",
-     HERE / "_ref" / "ref_partials.cubin"),
-    (REF_CALC / "cuda_propagations", HERE / "ref_cuda_propagations.cu",
+    ("cuda_partials", HERE / "ref_cuda_partials.cu", HERE / "_ref" / "ref_partials.cubin"),
+    ("cuda_propagations", HERE / "ref_cuda_propagations.cu",
      HERE / "_ref" / "ref_propagations.cubin"),
 ]
 REF_CUBIN = REF_BUILDS[0][2]
 
 
-def build_ref(verbose: bool = False) -> list[Path]:
+def reference_root(root: str | os.PathLike | None = None) -> Path:
+    return Path(root or os.environ.get("B3G_REFERENCE_ROOT") or DEFAULT_REFERENCE_ROOT)
+
+
+def build_ref(verbose: bool = False, root: str | os.PathLike | None = None) -> list[Path]:
     """Compile the reference's CUDA calculator kernels for sm_103a into
-    ``oracle/_ref/``; where the reference sources are absent the prebuilt
-    cubins, if any, are used as they are.  Returns the cubins present."""
+    ``oracle/_ref/`` from the reference tree at ``root`` (see
+    ``reference_root``); where the reference sources are absent the
+    prebuilt cubins, if any, are used as they are.  Returns the cubins
+    present."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    calc = reference_root(root) / "crates" / "b3" / "src" / "calculator"
     out = []
-    for src_dir, wrapper, cubin in REF_BUILDS:
+    for name, wrapper, cubin in REF_BUILDS:
+        src_dir = calc / name
         srcs = [src_dir / "kernels.cu", src_dir / "typedefs.h"]
         if not all(p.exists() for p in srcs):
             if cubin.exists():

@@ -394,3 +394,18 @@ class RefCudaPropagations(_RefModule):
 
     def result(self) -> np.ndarray:
         return self._download("likelihoods", np.empty(self.P, dtype=np.float64))
+
+
+def propagation_inputs(tree, model, rate, L):
+    """The lists of the reference's propagations calculator for a full
+    evaluation (tree.rs:436-454): every leaf, then the internals
+    children-first with the root last; the children of those internals; P
+    of the edge above every node but the root."""
+    from oracle import oracle as O
+
+    t = O.DatedTree(tree.parents, tree.heights)
+    t.mark_all_edges_updated()
+    internals, children = t.partials_lists()
+    nodes = np.concatenate([np.arange(L, dtype=np.uint32), np.asarray(internals, np.uint32)])
+    mats = np.array([model.transition(t.edge_length(int(v)) * rate) for v in nodes[:-1]])
+    return nodes, L, np.asarray(children, np.uint32), mats

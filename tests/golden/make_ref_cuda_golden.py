@@ -34,19 +34,6 @@ CASES = [
 ]
 
 
-def propagation_inputs(tree, model, rate, L):
-    """The lists of the reference's propagations calculator for a full
-    evaluation (tree.rs:436-454): every leaf, then the internals
-    children-first with the root last; the children of those internals; P
-    of the edge above every node but the root."""
-    t = O.DatedTree(tree.parents, tree.heights)
-    t.mark_all_edges_updated()
-    internals, children = t.partials_lists()
-    nodes = np.concatenate([np.arange(L, dtype=np.uint32), np.asarray(internals, np.uint32)])
-    mats = np.array([model.transition(t.edge_length(int(v)) * rate) for v in nodes[:-1]])
-    return nodes, L, np.asarray(children, np.uint32), mats
-
-
 def inputs(case):
     _, L, N, model_name, seed, rh, gaps, amb, rate, scale_ln = case
     c = dna_case(L, N, seed=seed, model=model_name, root_height=rh, gaps=gaps, ambiguous=amb)
@@ -56,7 +43,7 @@ def inputs(case):
     internals, children = t.partials_lists()
     lengths = np.array([[t.edge_length(int(a)), t.edge_length(int(b))] for a, b in children])
     mats = np.array([[model.transition(d * rate) for d in pair] for pair in lengths])
-    prop = propagation_inputs(c.tree, model, rate, L)
+    prop = ref_cuda.propagation_inputs(c.tree, model, rate, L)
     return c.leaves, np.asarray(internals), np.asarray(children), mats, model.pi, scale_ln, prop
 
 

@@ -367,3 +367,46 @@ def test_full_size_forms_agree_and_dirty_equals_full(big_case, rng):
         tree.accept()
         g64.accept()
         g32.accept()
+
+
+# --------------------------------------------------------------------------
+# the configurations' sizes against the oracle: 64 taxa x 10,000 sites and
+# 256 taxa x 20,000 sites, GTR + Gamma4 (exchangeabilities ~ Gamma(2, 1),
+# frequencies ~ Dirichlet(5, 5, 5, 5), alpha 0.5, Yule tree of root height 1)
+
+@pytest.mark.parametrize("L,N,seed", [(64, 10000, 2), (256, 20000, 4)])
+def test_configuration_sizes_match_oracle(L, N, seed, rng):
+    """Whole tree, then dirty paths with accept and reject: both forms
+    against the restated GammaLikelihood (four cpu4 calculators) at every
+    step, FP64 within 1e-10 and FP32 within 1e-6."""
+    from tests.test_oracle import random_move
+
+    c = dna_case(L, N, seed=seed, model="gtr", root_height=1.0, alpha=0.5,
+                 num_categories=4, pi_conc=5.0)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    ref = O.GammaLikelihood(c.leaves, c.weights, tree, O.gtr(c.rates, c.pi), 4, 0.5)
+    gpus = {p: make_gpu(c.leaves, c.weights, 4, p) for p in ("f64", "f32")}
+    tol = {"f64": F64_TOL, "f32": F32_TOL}
+    for p, g in gpus.items():
+        g.set_reversible(c.rates, c.pi)
+        g.set_gamma(0.5)
+        g.propose_lengths(*lists_and_lengths(full(c.tree.parents, c.tree.heights)), 1.0)
+        assert g.log_likelihood() == pytest.approx(ref.cache, rel=tol[p]), p
+        g.accept()
+    for step in range(6):
+        random_move(tree, rng)
+        lists = lists_and_lengths(tree)
+        want = ref.likelihood()
+        for p, g in gpus.items():
+            g.propose_lengths(*lists, 1.0)
+            assert g.log_likelihood() == pytest.approx(want, rel=tol[p]), (step, p)
+        if step % 2 == 0:
+            tree.accept(); ref.accept()  # noqa: E702
+            for g in gpus.values():
+                g.accept()
+        else:
+            tree.reject(); ref.reject()  # noqa: E702
+            for g in gpus.values():
+                g.reject()
+    for g in gpus.values():
+        g.close()

@@ -62,17 +62,13 @@ def test_reference_kernel_matches_oracle_and_library(ref, case):
     assert np.isfinite(want_ref).all()
     np.testing.assert_allclose(oracle, want_ref, rtol=1e-12, atol=0.0)
     # the reference's default GPU calculator (propagations) on the same inputs
-    import sys
-
-    sys.path.insert(0, "tests/golden")
-    from make_ref_cuda_golden import propagation_inputs
     from oracle import ref_cuda
 
     if ref_cuda.propagations_available():
         prop = ref_cuda.RefCudaPropagations(0)
         try:
             prop.setup(c.leaves, scale_ln)
-            nodes, k, pch, pmats = propagation_inputs(c.tree, model, rate, L)
+            nodes, k, pch, pmats = ref_cuda.propagation_inputs(c.tree, model, rate, L)
             prop.propose(nodes, k, pch, pmats, model.pi)
             got_prop = prop.result()
         finally:
