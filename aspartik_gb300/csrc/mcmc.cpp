@@ -298,6 +298,14 @@ uint32_t random_nonroot(const DatedTree &t, Rng &rng)
 	return v;
 }
 
+// Moves whose likelihood is a whole-tree evaluation: every edge length or
+// the substitution model changes.
+bool is_global_move(uint32_t op)
+{
+	return op == kOpTreeScale || op == kOpUpDown || op == kOpScaleKappa ||
+	       op == kOpScaleAlpha || op == kOpDeltaRates || op == kOpDeltaFreqs;
+}
+
 } // namespace
 
 // One proposal per operator kind, restating python/aspartik/b3/operators.
@@ -316,8 +324,13 @@ void Mcmc::propose(Chain &ch)
 	ch.op = op;
 	ch.hastings = 0.0;
 	ch.status = 0;
-	ch.local = false;
+	ch.screenable = false;
 	ch.screened = false;
+	// delayed acceptance screens the moves that need a whole-tree
+	// evaluation; their surrogate inputs before the move
+	const bool global = cfg_.da_pilot_steps && is_global_move(op);
+	if (global)
+		features(ch, ch.feat_old);
 	const double f = ops_[op].tuning;
 	auto scale_factor = [&]() {
 		// sample_range(f, 1 / f, Uniform(0, 1)) (operators/_util.py)
@@ -366,13 +379,8 @@ void Mcmc::propose(Chain &ch)
 		const uint32_t gp = t.parent_of(parent);
 		const uint32_t uncle = t.other_child(gp, parent);
 		if (t.height(uncle) < t.height(parent)) {
-			features(ch, parent, ch.feat_old);
-			if (!t.swap_parents(node, uncle)) {
+			if (!t.swap_parents(node, uncle))
 				ch.status = 1;
-			} else {
-				features(ch, parent, ch.feat_new);
-				ch.local = true;
-			}
 		} else {
 			ch.status = 1;
 		}
@@ -387,7 +395,6 @@ void Mcmc::propose(Chain &ch)
 		const uint32_t parent = t.parent_of(node);
 		const uint32_t gp = t.parent_of(parent);
 		const uint32_t sibling = t.other_child(parent, node);
-		features(ch, parent, ch.feat_old);
 		// distribution Uniform(-0.5, 0.5) times the tuning factor
 		const double delta = (ch.rng.uniform() - 0.5) * f;
 		const double old_h = t.height(parent);
@@ -446,8 +453,6 @@ void Mcmc::propose(Chain &ch)
 			}
 		}
 		t.set_height(parent, new_h);
-		features(ch, parent, ch.feat_new);
-		ch.local = true;
 		break;
 	}
 	case kOpRelaxedCategory: { // one edge's class (clock.rs:107-112)
@@ -530,6 +535,10 @@ void Mcmc::propose(Chain &ch)
 	default:
 		ch.status = 1;
 	}
+	if (global && ch.status == 0) {
+		features(ch, ch.feat_new);
+		ch.screenable = true;
+	}
 }
 
 // The body of DnaLikelihood/GammaLikelihood::likelihood (dna.rs:68-100,
@@ -564,21 +573,22 @@ void Mcmc::launch(Chain &ch)
 	ch.launched = true;
 }
 
-// Surrogate inputs around `center` (see kDaInputs).
-void Mcmc::features(const Chain &ch, uint32_t center, float *out) const
+// Surrogate inputs of the chain's current state (see kDaInputs).
+void Mcmc::features(const Chain &ch, float *out) const
 {
 	const DatedTree &t = *ch.tree;
-	auto lg = [](double x) { return (float)std::log(std::max(x, 1e-12)); };
-	const uint32_t p = t.parent_of(center);
-	out[0] = p != kTombstone ? lg(t.edge_length(center)) : 0.0f;
-	out[1] = lg(t.edge_length(t.left(center)));
-	out[2] = lg(t.edge_length(t.right(center)));
-	out[3] = out[4] = 0.0f;
-	if (p != kTombstone) {
-		out[3] = lg(t.edge_length(t.other_child(p, center)));
-		if (t.parent_of(p) != kTombstone)
-			out[4] = lg(t.edge_length(p));
+	auto lg = [](double x) { return (float)std::log(std::max(x, 1e-300)); };
+	double inner = 0.0, outer = 0.0;
+	for (uint32_t v = 0; v < t.num_nodes(); ++v) {
+		if (v == t.root())
+			continue;
+		(t.is_leaf(v) ? outer : inner) += t.edge_length(v);
 	}
+	out[0] = lg(inner + outer);
+	out[1] = lg(t.root_height());
+	out[2] = lg(inner);
+	out[3] = lg(outer);
+	out[4] = cfg_.num_categories > 1 ? lg(ch.alpha.v) : 0.0f;
 	for (uint32_t k = 0; k < 6; ++k)
 		out[5 + k] = cfg_.model == 1 ? lg(ch.rates.v[k])
 					     : (k == 0 ? lg(ch.kappa.v) : 0.0f);
@@ -695,7 +705,7 @@ void Mcmc::finish(Chain &ch)
 				accept = ratio > std::log(ch.rng.uniform());
 			}
 			// pilot pairs for the surrogate
-			if (ch.local && cfg_.da_pilot_steps && !surrogate_ &&
+			if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
 			    da_.fallback == 0 && std::isfinite(dlnl)) {
 				pilot_old_.insert(pilot_old_.end(), ch.feat_old,
 						  ch.feat_old + kDaInputs);
@@ -887,7 +897,7 @@ void Mcmc::run(uint64_t steps)
 			ch->prior_new = prior(*ch);
 			if (ch->prior_new == kNegInf)
 				ch->status = 2; // mcmc.rs:331-335
-			else if (da_active_ && ch->local)
+			else if (da_active_ && ch->screenable)
 				screen(*ch);
 		}
 		// every chain's device work is queued before any result is read

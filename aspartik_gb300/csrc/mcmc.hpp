@@ -130,10 +130,11 @@ struct McmcConfig {
 	uint32_t clock_categories; // 0: strict clock
 };
 
-// Inputs of the surrogate: 5 branch lengths around the node a tree move
-// changes (its parent edge, its two child edges, its sibling's edge and its
-// parent's edge, log scale) and 9 model parameters (log exchangeabilities
-// or log kappa, three frequencies).
+// Inputs of the surrogate, for the moves that re-evaluate the whole tree
+// (tree scale, up-down, kappa, alpha, exchangeabilities, frequencies): 5
+// length summaries of the tree (log of the tree length, the root height,
+// the internal and the external edge lengths' sums, and log alpha) and 9
+// model parameters (log exchangeabilities or log kappa, three frequencies).
 constexpr uint32_t kDaInputs = 14;
 
 // Parameters of one sample: kappa, alpha, birth rate, 6 exchangeabilities,
@@ -170,7 +171,7 @@ struct Chain {
 	uint32_t op = 0;
 	double hastings = 0.0;
 	int status = 0; // 0 pending, 1 abort, 2 prior reject, 3 stage-1 reject
-	bool local = false;   // a tree move around one node (surrogate inputs)
+	bool screenable = false; // a whole-tree move with surrogate inputs
 	bool screened = false; // passed stage one of delayed acceptance
 	double da_delta = 0.0; // surrogate f(x_new) - f(x_old)
 	float feat_old[kDaInputs], feat_new[kDaInputs];
@@ -244,7 +245,7 @@ class Mcmc {
 	void tune();
 	void record();
 	double send_model(Chain &ch, bool mark_all);
-	void features(const Chain &ch, uint32_t center, float *out) const;
+	void features(const Chain &ch, float *out) const;
 	void screen(Chain &ch);
 	void train_surrogate();
 

@@ -7,10 +7,13 @@
 //     gelu(x) = x/2 (1 + tanh(u)),  u = sqrt(2/pi) (x + 0.044715 x^3).
 // Products go through one shared-memory tiled FP32 GEMM kernel with
 // optional transposes; Adam (Kingma and Ba, 2015) updates the parameters.
+#include <cooperative_groups.h>
+
 #include "calculator.hpp"
 #include "mlp.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -18,6 +21,8 @@
 
 namespace b3g {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr float kGeluC = 0.7978845608028654f; // sqrt(2 / pi)
 constexpr float kGeluA = 0.044715f;
@@ -165,60 +170,127 @@ __global__ void gather_rows_kernel(const float *__restrict__ src,
 	out[i] = src[(size_t)idx[r] * cols + c];
 }
 
-// f(x_new) - f(x_old) for one pair in one block of `hidden` threads: each
-// thread owns one unit of every hidden layer, activations live in shared
-// memory.  pair = [x_new (in), x_old (in)], result in pair[2 * in].
-__global__ void mlp_delta_kernel(const float *__restrict__ params,
-				 float *__restrict__ pair, uint32_t in,
-				 uint32_t hidden)
+// f(x_new) - f(x_old) for one pair, by a cluster of kDeltaCluster CTAs.
+// Every CTA holds all activations of the current layer in shared memory and
+// computes its own slice of the next layer's units: warp w of the CTA takes
+// kDeltaRows consecutive units at a time and reads their rows of W with all
+// loads issued before any product (float4 loads where the rows allow),
+// reduces both inputs' dot products across the warp in a fixed order, and
+// lanes 0..7 / 8..15 write the two GELU outputs into the eight CTAs' shared
+// memory (DSMEM); a cluster barrier ends the layer.  So one inference reads
+// its weights through eight SMs instead of one, with many loads in flight
+// (one block walking the rows one after another waits an L2 round trip per
+// row).  The pair is read from and the result written to host-mapped
+// memory: pair = [x_new (in), x_old (in)], result at out (by CTA 0).
+constexpr uint32_t kDeltaCluster = 8;
+constexpr uint32_t kDeltaRows = 4;
+
+__device__ __forceinline__ float dot4(float4 w, float4 x)
 {
-	extern __shared__ float sh[];
-	float *a = sh;               // [2][hidden]
-	float *b = sh + 2 * hidden;  // [2][hidden]
-	const uint32_t j = threadIdx.x;
-	for (uint32_t k = j; k < 2 * in; k += blockDim.x)
+	return fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, w.w * x.w)));
+}
+
+__global__ void __cluster_dims__(kDeltaCluster, 1, 1) __launch_bounds__(256)
+	mlp_delta_kernel(const float *__restrict__ params, const float *pair, float *out,
+			 uint32_t in, uint32_t hidden)
+{
+	extern __shared__ __align__(16) float sh[];
+	cg::cluster_group cluster = cg::this_cluster();
+	const uint32_t rank = cluster.block_rank();
+	const uint32_t width_max = max(in, hidden);
+	float *a = sh;                 // [2][width] current layer (inputs first)
+	float *b = sh + 2 * width_max; // [2][hidden] next layer
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	const uint32_t warps = blockDim.x >> 5;
+	for (uint32_t k = threadIdx.x; k < 2 * in; k += blockDim.x)
 		a[k] = pair[k];
-	__syncthreads();
+	// this CTA's units of every hidden layer
+	const uint32_t per = (hidden + kDeltaCluster - 1) / kDeltaCluster;
+	const uint32_t o_begin = rank * per, o_end = min(hidden, o_begin + per);
+	cluster.sync(); // every CTA has started before any DSMEM write
 	const float *W = params;
 	uint32_t width = in;
 	for (int layer = 0; layer < 3; ++layer) {
 		const float *bias = W + (size_t)hidden * width;
-		const float *w = W + (size_t)j * width;
-		float z0 = bias[j], z1 = bias[j];
-		for (uint32_t k = 0; k < width; ++k) {
-			const float wk = w[k];
-			z0 = fmaf(wk, a[k], z0);
-			z1 = fmaf(wk, a[width + k], z1);
+		const bool vec = (width & 3u) == 0 && ((uintptr_t)W & 15u) == 0;
+		for (uint32_t o0 = o_begin + warp * kDeltaRows; o0 < o_end;
+		     o0 += warps * kDeltaRows) {
+			float z0[kDeltaRows], z1[kDeltaRows];
+#pragma unroll
+			for (uint32_t r = 0; r < kDeltaRows; ++r)
+				z0[r] = z1[r] = 0.0f;
+			if (vec) {
+				for (uint32_t k = 4 * lane; k < width; k += 128) {
+					float4 wv[kDeltaRows];
+#pragma unroll
+					for (uint32_t r = 0; r < kDeltaRows; ++r)
+						wv[r] = o0 + r < o_end
+								? __ldg(reinterpret_cast<const float4 *>(
+									  W + (size_t)(o0 + r) * width + k))
+								: make_float4(0.f, 0.f, 0.f, 0.f);
+					const float4 x0 = *reinterpret_cast<const float4 *>(a + k);
+					const float4 x1 = *reinterpret_cast<const float4 *>(a + width + k);
+#pragma unroll
+					for (uint32_t r = 0; r < kDeltaRows; ++r) {
+						z0[r] += dot4(wv[r], x0);
+						z1[r] += dot4(wv[r], x1);
+					}
+				}
+			} else {
+				for (uint32_t k = lane; k < width; k += 32) {
+					float wv[kDeltaRows];
+#pragma unroll
+					for (uint32_t r = 0; r < kDeltaRows; ++r)
+						wv[r] = o0 + r < o_end
+								? __ldg(W + (size_t)(o0 + r) * width + k)
+								: 0.0f;
+					const float x0 = a[k], x1 = a[width + k];
+#pragma unroll
+					for (uint32_t r = 0; r < kDeltaRows; ++r) {
+						z0[r] = fmaf(wv[r], x0, z0[r]);
+						z1[r] = fmaf(wv[r], x1, z1[r]);
+					}
+				}
+			}
+#pragma unroll
+			for (uint32_t r = 0; r < kDeltaRows; ++r) {
+				for (int off = 16; off > 0; off >>= 1) {
+					z0[r] += __shfl_xor_sync(0xffffffffu, z0[r], off);
+					z1[r] += __shfl_xor_sync(0xffffffffu, z1[r], off);
+				}
+				const uint32_t o = o0 + r;
+				if (o < o_end && lane < 2 * kDeltaCluster) {
+					const float bo = __ldg(bias + o);
+					const bool second = lane >= kDeltaCluster;
+					float *dst = cluster.map_shared_rank(b, lane % kDeltaCluster);
+					dst[(second ? hidden : 0u) + o] =
+						gelu((second ? z1[r] : z0[r]) + bo);
+				}
+			}
 		}
-		__syncthreads();
-		b[j] = gelu(z0);
-		b[hidden + j] = gelu(z1);
-		__syncthreads();
-		for (uint32_t k = j; k < 2 * hidden; k += blockDim.x)
-			a[k] = b[k];
-		__syncthreads();
+		cluster.sync(); // the layer is complete in every CTA
+		float *t = a;
+		a = b;
+		b = t;
 		W = bias + hidden;
 		width = hidden;
 	}
-	// output unit: W [1][hidden], b [1]
-	__shared__ float s0[32], s1[32];
-	float p0 = W[j] * a[j], p1 = W[j] * a[hidden + j];
-	for (int off = 16; off > 0; off >>= 1) {
-		p0 += __shfl_down_sync(0xffffffffu, p0, off);
-		p1 += __shfl_down_sync(0xffffffffu, p1, off);
-	}
-	if ((j & 31u) == 0) {
-		s0[j >> 5] = p0;
-		s1[j >> 5] = p1;
-	}
-	__syncthreads();
-	if (j == 0) {
+	// output unit: W [1][hidden]; its bias cancels in the difference
+	if (rank == 0 && warp == 0) {
 		float y0 = 0.0f, y1 = 0.0f;
-		for (uint32_t w2 = 0; w2 < (hidden + 31) / 32; ++w2) {
-			y0 += s0[w2];
-			y1 += s1[w2];
+		for (uint32_t k = lane; k < hidden; k += 32) {
+			const float wk = __ldg(W + k);
+			y0 = fmaf(wk, a[k], y0);
+			y1 = fmaf(wk, a[hidden + k], y1);
 		}
-		pair[2 * in] = y0 - y1; // the biases cancel
+		for (int off = 16; off > 0; off >>= 1) {
+			y0 += __shfl_xor_sync(0xffffffffu, y0, off);
+			y1 += __shfl_xor_sync(0xffffffffu, y1, off);
+		}
+		if (lane == 0) {
+			*(volatile float *)out = y0 - y1;
+			__threadfence_system();
+		}
 	}
 }
 
@@ -267,10 +339,12 @@ Mlp::Mlp(uint32_t in_dim, uint32_t hidden, uint64_t seed, int device)
 	check_cuda(cudaMemcpy(d_params_, p.data(), bytes, cudaMemcpyHostToDevice), "params");
 	check_cuda(cudaMemset(d_m_, 0, bytes), "adam m");
 	check_cuda(cudaMemset(d_v_, 0, bytes), "adam v");
-	check_cuda(cudaMalloc(&d_pair_, sizeof(float) * (2 * in_ + 4)), "pair");
+	// inference pair and result in host-mapped memory: no copies, no
+	// stream synchronisation per screened proposal
 	check_cuda(cudaHostAlloc((void **)&h_pair_, sizeof(float) * (2 * in_ + 4),
-				 cudaHostAllocDefault),
-		   "pinned pair");
+				 cudaHostAllocMapped),
+		   "mapped pair");
+	check_cuda(cudaHostGetDevicePointer((void **)&d_pair_, h_pair_, 0), "mapped pair");
 }
 
 Mlp::~Mlp()
@@ -291,7 +365,6 @@ Mlp::~Mlp()
 	cudaFree(d_dy_);
 	cudaFree(d_delta_);
 	cudaFree(d_loss_);
-	cudaFree(d_pair_);
 	cudaFreeHost(h_pair_);
 	if (stream_)
 		cudaStreamDestroy(stream_);
@@ -500,21 +573,46 @@ float Mlp::train(const float *x_new, const float *x_old, const float *delta,
 	return static_cast<float>(epoch_loss);
 }
 
+namespace {
+// a NaN payload the kernel never writes
+constexpr uint32_t kDeltaSentinel = 0x7fb3a5e1u;
+} // namespace
+
 float Mlp::delta(const float *x_new, const float *x_old)
 {
+	volatile uint32_t *word = reinterpret_cast<volatile uint32_t *>(h_pair_ + 2 * in_);
 	std::memcpy(h_pair_, x_new, sizeof(float) * in_);
 	std::memcpy(h_pair_ + in_, x_old, sizeof(float) * in_);
-	check_cuda(cudaMemcpyAsync(d_pair_, h_pair_, sizeof(float) * 2 * in_,
-				   cudaMemcpyHostToDevice, stream_),
-		   "pair");
-	const size_t smem = sizeof(float) * 4 * std::max(hidden_, in_);
-	mlp_delta_kernel<<<1, hidden_, smem, stream_>>>(d_params_, d_pair_, in_, hidden_);
+	*word = kDeltaSentinel;
+	std::atomic_thread_fence(std::memory_order_seq_cst);
+	const size_t smem = sizeof(float) * 2 * (std::max(hidden_, in_) + hidden_);
+	mlp_delta_kernel<<<kDeltaCluster, 256, smem, stream_>>>(d_params_, d_pair_,
+								 d_pair_ + 2 * in_, in_, hidden_);
 	check_cuda(cudaGetLastError(), "surrogate inference");
-	check_cuda(cudaMemcpyAsync(h_pair_ + 2 * in_, d_pair_ + 2 * in_, sizeof(float),
-				   cudaMemcpyDeviceToHost, stream_),
-		   "delta");
-	check_cuda(cudaStreamSynchronize(stream_), "sync");
-	return h_pair_[2 * in_];
+	// poll the mapped word; every 64 polls ask the stream, so that an error
+	// surfaces and a finished kernel that wrote nothing ends the wait
+	for (uint32_t k = 1;; ++k) {
+		uint32_t bits = *word;
+		if (bits != kDeltaSentinel) {
+			float v;
+			std::memcpy(&v, &bits, sizeof(v));
+			return v;
+		}
+		if ((k & 63u) == 0) {
+			const cudaError_t e = cudaStreamQuery(stream_);
+			if (e == cudaSuccess) {
+				bits = *word;
+				if (bits == kDeltaSentinel)
+					throw Error(B3G_ERR_CUDA,
+						    "surrogate inference finished without a result");
+				float v;
+				std::memcpy(&v, &bits, sizeof(v));
+				return v;
+			}
+			if (e != cudaErrorNotReady)
+				check_cuda(e, "surrogate inference");
+		}
+	}
 }
 
 } // namespace b3g

@@ -356,12 +356,14 @@ typedef struct b3g_mcmc_config {
 	int32_t device;
 	double op_weights[B3G_OP_COUNT];
 	/* Delayed acceptance (no counterpart in the reference): after
-	 * da_pilot_steps exact steps a surrogate (14 inputs: 5 branch lengths
-	 * around the moved node and 9 model parameters; da_hidden units per
-	 * hidden layer) is trained for da_epochs on the pilot's tree-move pairs
-	 * and screens later subtree-slide and narrow-exchange proposals; the
-	 * exact likelihood stays the second-stage test, so the target
-	 * distribution is unchanged.  Screening stops for good when the RMS of
+	 * da_pilot_steps exact steps a surrogate (14 inputs: log tree length,
+	 * root height, internal and external edge-length sums and alpha, and
+	 * 9 model parameters; da_hidden units per hidden layer) is trained for
+	 * da_epochs on the pilot's pairs of the moves that re-evaluate the
+	 * whole tree (tree scale, up-down, kappa, alpha, exchangeabilities,
+	 * frequencies) and screens those moves afterwards; the exact
+	 * likelihood stays the second-stage test, so the target distribution
+	 * is unchanged.  Screening stops for good when the RMS of
 	 * (exact - surrogate) over the last 200 screened proposals exceeds
 	 * da_drift_limit (0: never).  da_pilot_steps = 0 turns it off. */
 	uint32_t da_pilot_steps;
