@@ -405,89 +405,192 @@ def protein20(device: int, steps: int, warmup: int, seed: int = 4, L: int = 128,
     return out
 
 
-def mcmc_ess(wl, steps: int, device: int) -> dict:
-    """ESS per second of the cold chain on the workload: the plain FP64 form,
-    the FP32 chosen form, and the chosen form with delayed-acceptance
-    screening (pilot = the first fifth of the steps, then the surrogate is
-    trained and screens tree moves).  Same data, seed, moves and number of
-    steps for every arm; ESS is the minimum over the lnL, root-height and
-    first-exchangeability traces (Geyer 1992) on the last 80% of samples (past
-    the pilot); time is the wall time of the whole run, pilot and training
-    included.  A fourth arm runs the chosen form batched: 8 independent
-    replicates stepping together, each scalar's ESS by the multi-chain
-    estimator (between-chain variance included; the sum of the per-chain
-    values is reported beside it)."""
-    from aspartik_gb300.ess import ess, min_ess, multi_chain_ess
-    from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
+ESS_FIELDS = ("lnl", "root_height", "kappa_or_rate0")
 
-    out = {}
-    arms = (("plain_f64", "f64", 0), ("chosen_f32", "f32", 0),
-            ("chosen_f32_da", "f32", steps // 5))
-    for name, precision, pilot in arms:
-        s = McmcSettings(model="gtr", precision=precision,
-                         num_categories=wl["spec"]["categories"], seed=4, sample_every=10,
-                         weights=dict(GTR_WEIGHTS), device=device, da_pilot_steps=pilot,
-                         da_epochs=20, da_hidden=256, da_drift_limit=20.0)
-        m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
-        m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
-                         alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
-        t0 = time.perf_counter()
-        m.run(steps)
-        dt = time.perf_counter() - t0
-        keep = (steps // 10) // 5
-        traces = {k: m.trace(k)[keep:] for k in ("lnl", "root_height", "kappa_or_rate0")}
-        e, per = min_ess(traces, burn_in=0.0)
-        out[name] = {"steps": steps, "seconds": round(dt, 3),
-                     "us_per_step": round(dt / steps * 1e6, 2),
-                     "ess_min": round(e, 2), "ess": {k: round(v, 2) for k, v in per.items()},
-                     "ess_per_s": round(e / dt, 3),
-                     "mean_lnl": float(np.mean(traces["lnl"])),
-                     "check_rel": m.check()}
-        if pilot:
-            out[name]["delayed_acceptance"] = m.da_stats()
-        m.close()
-    # the chosen form batched: independent replicates (heat 0, no swaps) on
-    # their own streams; ESS per scalar over the replicates by the
-    # multi-chain estimator, which counts their disagreement against them
-    R = 8
-    s = McmcSettings(model="gtr", precision="f32", num_categories=wl["spec"]["categories"],
-                     num_chains=R, heat=0.0, swap_every=0, seed=4, sample_every=10,
-                     weights=dict(GTR_WEIGHTS), device=device)
-    m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
-    m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
-                     alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
+
+def mcmc_settings(wl, precision: str, **kw):
+    from aspartik_gb300.mcmc import GTR_WEIGHTS, HKY_SCALE_KAPPA_WEIGHTS, McmcSettings
+
+    spec = wl["spec"]
+    weights = GTR_WEIGHTS if spec["model"] == "gtr" else HKY_SCALE_KAPPA_WEIGHTS
+    kw.setdefault("weights", dict(weights))
+    return McmcSettings(model=spec["model"], precision=precision,
+                        num_categories=spec["categories"], sample_every=10, **kw)
+
+
+def start_parameters(wl) -> dict:
+    """The simulated tree and parameters."""
+    return dict(parents=wl["tree"].parents, heights=wl["tree"].heights,
+                rates=wl["rates"] if wl["spec"]["model"] == "gtr" else None, freqs=wl["pi"],
+                kappa=2.0, alpha=wl["spec"]["alpha"] or 1.0, birth=1.0)
+
+
+def burn_in(wl, steps: int, device: int) -> tuple[dict, dict, float]:
+    """A chosen-form chain from the simulated tree and parameters; its final
+    state and operator tunings start every measured arm, so that each arm
+    samples near stationarity from its first step."""
+    from aspartik_gb300.mcmc import Mcmc
+
+    st = start_parameters(wl)
+    m = Mcmc(wl["leaves"], wl["weights"], st["parents"], st["heights"],
+             mcmc_settings(wl, "f32", seed=3, device=device))
+    m.set_parameters(kappa=st["kappa"], rates=st["rates"], frequencies=st["freqs"],
+                     alpha=st["alpha"], birth_rate=st["birth"])
     t0 = time.perf_counter()
     m.run(steps)
     dt = time.perf_counter() - t0
-    keep = (steps // 10) // 5
-    names = ("lnl", "root_height", "kappa_or_rate0")
-    chains_tr = {n: [m.trace(n, chain=k)[keep:] for k in range(R)] for n in names}
-    combined = {n: multi_chain_ess(chains_tr[n], burn_in=0.0) for n in names}
-    summed = {n: sum(ess(x, burn_in=0.0) for x in chains_tr[n]) for n in names}
-    e = min(combined.values())
-    out["chosen_f32_replicates"] = {
-        "chains": R, "steps": steps, "seconds": round(dt, 3),
-        "us_per_step": round(dt / steps * 1e6, 2),
-        "chain_steps_per_s": round(R * steps / dt, 1),
-        "ess_min": round(e, 2), "ess": {k: round(v, 2) for k, v in combined.items()},
-        "ess_summed_per_chain": {k: round(v, 2) for k, v in summed.items()},
-        "ess_per_s": round(e / dt, 3), "check_rel": m.check()}
+    smp = m.samples()
+    tunings = {k: v["tuning"] for k, v in m.operator_stats().items()}
     m.close()
+    start = dict(parents=smp["parents"][-1], heights=smp["heights"][-1],
+                 rates=smp["rates"][-1] if wl["spec"]["model"] == "gtr" else None,
+                 freqs=smp["frequencies"][-1], kappa=float(smp["kappa"][-1]),
+                 alpha=float(smp["alpha"][-1]), birth=float(smp["birth_rate"][-1]))
+    return start, tunings, dt
+
+
+def mcmc_arm(wl, start, tunings, precision: str, steps: int, device: int, chains: int = 1,
+             da_pilot: int = 0, burn_frac: float = 0.05, seed: int = 4) -> dict:
+    """One arm of the ESS/s comparison: `chains` chains (independent
+    replicates stepping together) from `start`, `steps` steps, wall time of
+    the whole run (pilot and surrogate training included).  ESS of lnL, root
+    height and the first exchangeability (kappa for HKY) by Geyer's initial
+    monotone sequence (one chain) or the multi-chain estimator of BDA3 11.5
+    (replicates: their disagreement counts against them), after dropping the
+    first `burn_frac` of the samples."""
+    from aspartik_gb300.ess import min_ess, multi_chain_ess
+    from aspartik_gb300.mcmc import Mcmc
+
+    kw = dict(seed=seed, device=device, num_chains=chains, heat=0.0, swap_every=0)
+    if da_pilot:
+        kw.update(da_pilot_steps=da_pilot, da_epochs=100, da_hidden=256, da_drift_limit=20.0)
+    m = Mcmc(wl["leaves"], wl["weights"], start["parents"], start["heights"],
+             mcmc_settings(wl, precision, **kw))
+    m.set_parameters(kappa=start["kappa"], rates=start["rates"], frequencies=start["freqs"],
+                     alpha=start["alpha"], birth_rate=start["birth"])
+    if tunings:
+        m.set_tuning(tunings)
+    t0 = time.perf_counter()
+    m.run(steps)
+    dt = time.perf_counter() - t0
+    n = m.trace("lnl").size
+    keep = int(n * burn_frac)
+    if chains == 1:
+        traces = {k: m.trace(k)[keep:] for k in ESS_FIELDS}
+        e, per = min_ess(traces, burn_in=0.0)
+    else:
+        per = {k: multi_chain_ess([m.trace(k, chain=c)[keep:] for c in range(chains)],
+                                  burn_in=0.0) for k in ESS_FIELDS}
+        e = min(per.values())
+        traces = {"lnl": np.concatenate([m.trace("lnl", chain=c)[keep:]
+                                         for c in range(chains)])}
+    out = {"chains": chains, "steps": steps, "seconds": round(dt, 3),
+           "us_per_step": round(dt / steps * 1e6, 2),
+           "chain_steps_per_s": round(chains * steps / dt, 1),
+           "ess_min": round(e, 1), "ess": {k: round(v, 1) for k, v in per.items()},
+           "ess_per_s": round(e / dt, 3), "mean_lnl": float(np.mean(traces["lnl"])),
+           "check_rel": m.check()}
+    if da_pilot:
+        out["delayed_acceptance"] = m.da_stats()
+    m.close()
+    return out
+
+
+def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
+    """ESS per second, chosen form against the plain FP64 form, on the
+    workload, every arm started from the same burned-in state and operator
+    tunings (a chosen-form chain of chosen_steps / 7.5 steps from the
+    simulated tree and parameters, not timed in any arm):
+      plain_f64                one chain, FP64 partials (the drop-in's
+                               arithmetic), 0.4 x chosen_steps steps
+      chosen_f32               one chain, FP32 power-of-two-scaled partials
+      chosen_f32_da            one chain with delayed acceptance: the first
+                               10^5 steps are the pilot, then the surrogate
+                               (trained on the GPU) screens the moves that
+                               re-evaluate the whole tree
+      chosen_f32_da_replicates the chosen form in full: 8 independent
+                               replicates stepping together (all chains'
+                               evaluations of a step queued before any
+                               result is read) with delayed acceptance,
+                               chosen_steps / 7.5 steps, multi-chain ESS
+    Moves: the driver's GTR mix (tree scale 3, subtree slide 30, narrow
+    exchange 30, wide exchange 3, root slide 3, node slide 30, up-down 3,
+    alpha scale 1, birth-rate scale 3, delta exchange of rates 1 and of
+    frequencies 1)."""
+    burn = int(chosen_steps / 7.5)
+    start, tunings, burn_s = burn_in(wl, burn, device)
+    out = {"burn_in": {"steps": burn, "seconds": round(burn_s, 3), "form": "f32",
+                       "tunings": {k: round(v, 6) for k, v in tunings.items()}}}
+    out["plain_f64"] = mcmc_arm(wl, start, tunings, "f64", int(0.4 * chosen_steps), device)
+    out["chosen_f32"] = mcmc_arm(wl, start, tunings, "f32", chosen_steps, device)
+    out["chosen_f32_da"] = mcmc_arm(wl, start, tunings, "f32", chosen_steps, device,
+                                    da_pilot=min(100_000, chosen_steps // 5))
+    rep = int(chosen_steps / 7.5)
+    out["chosen_f32_da_replicates"] = mcmc_arm(wl, start, tunings, "f32", rep, device,
+                                               chains=8, da_pilot=rep // 8)
     base = max(out["plain_f64"]["ess_per_s"], 1e-12)
-    out["ess_per_s_ratio_chosen_vs_plain"] = round(out["chosen_f32"]["ess_per_s"] / base, 3)
-    # (no ESS ratio for the replicates: the multi-chain estimator also
-    # charges the replicates' disagreement, which one plain chain's own
-    # estimate cannot see, so the two ESS figures are not like for like)
-    out["chain_steps_per_s_ratio_chosen_replicates_vs_plain"] = round(
-        out["chosen_f32_replicates"]["chain_steps_per_s"] * out["plain_f64"]["seconds"]
-        / steps, 3)
-    out["ess_per_s_ratio_chosen_da_vs_plain"] = round(
-        out["chosen_f32_da"]["ess_per_s"] / base, 3)
+    for arm in ("chosen_f32", "chosen_f32_da", "chosen_f32_da_replicates"):
+        out[f"ess_per_s_ratio_{arm}_vs_plain"] = round(out[arm]["ess_per_s"] / base, 3)
+    out["ess_min_all_arms"] = min(out[a]["ess_min"] for a in
+                                  ("plain_f64", "chosen_f32", "chosen_f32_da",
+                                   "chosen_f32_da_replicates"))
     out["mean_lnl_rel_diff_chosen_vs_plain"] = abs(
         out["chosen_f32"]["mean_lnl"] - out["plain_f64"]["mean_lnl"]) / abs(
         out["plain_f64"]["mean_lnl"])
-    out["moves"] = ("GTR+Gamma4: tree scale 3, subtree slide 30, narrow exchange 30, "
-                    "alpha scale 1, birth-rate scale 3, delta exchange rates 1, freqs 1")
+    out["ess_fields"] = list(ESS_FIELDS)
+    return out
+
+
+def config_block(name: str, device: int, mcmc_steps: int, reps: int = 50) -> dict:
+    """One of the smaller configurations on its own: whole-tree evaluation
+    time of both forms (device time, CUDA events), the log-likelihood of
+    each against the restated cpu4 (oracle/b3oracle.c, the CPU baseline of
+    this block, timed on all host threads), and the ESS/s of the chosen form
+    against the plain FP64 form over `mcmc_steps` steps from the simulated
+    tree (10% burn-in dropped)."""
+    wl = make_workload(name)
+    spec = wl["spec"]
+    top = wl["top"]
+    P = int(wl["leaves"].shape[1])
+    C = spec["categories"]
+    full = top.full()
+    out = {"taxa": spec["taxa"], "sites": spec["sites"], "patterns": P, "categories": C,
+           "model": spec["model"]}
+    lnl = {}
+    for precision, w in (("f32", 4), ("f64", 8)):
+        calc = make_calc(wl, precision, device)
+        if precision == "f32":
+            calc.propose_lengths(*full, 1.0)
+            calc.log_likelihood()
+            calc.accept()
+            calc.autotune(*full, 1.0)
+        ms, _, prune_ms, _ = device_throughput(calc, full, reps, 5, 1)
+        lnl[precision] = calc.log_likelihood()
+        calc.close()
+        B = schedule.algorithmic_bytes(top, full[0], P, C, 4, w=w, e_b=4, w_p=w)
+        out[f"whole_tree_{precision}"] = {
+            "ms_per_eval": round(ms / reps, 5), "kernel_ms": round(prune_ms, 5),
+            "GB_s": round(B / (ms / reps * 1e-3) / 1e9, 2), "bytes_per_eval": B,
+            "lnl": lnl[precision]}
+    cores = os.cpu_count() or 1
+    ref = CpuReference(wl, cores)
+    ref.evaluate()
+    t_cpu, cpu_lnl = ref.evaluate()
+    out["cpu_baseline"] = {"kind": "port", "cores": ref.threads,
+                           "ms_per_eval": round(t_cpu * 1e3, 3), "lnl": cpu_lnl,
+                           "sample": "one whole-tree evaluation of the full alignment; "
+                                     "cpu4-restated, FP64, e^30 rescaling"}
+    out["lnl_rel_err_f64_vs_oracle"] = abs(lnl["f64"] - cpu_lnl) / abs(cpu_lnl)
+    out["lnl_rel_err_f32_vs_oracle"] = abs(lnl["f32"] - cpu_lnl) / abs(cpu_lnl)
+    if mcmc_steps > 0:
+        st = start_parameters(wl)
+        arms = {p: mcmc_arm(wl, st, None, p, mcmc_steps, device, burn_frac=0.1)
+                for p in ("f64", "f32")}
+        out["mcmc"] = {"steps": mcmc_steps, "plain_f64": arms["f64"], "chosen_f32": arms["f32"],
+                       "ess_per_s_ratio_chosen_vs_plain": round(
+                           arms["f32"]["ess_per_s"] / max(arms["f64"]["ess_per_s"], 1e-12), 3),
+                       "moves": "tree scale 3, kappa scale 1" if spec["model"] == "hky" else
+                       "the GTR mix of the MCMC leg (NNI = narrow exchange, subtree slide)"}
     return out
 
 
@@ -525,24 +628,25 @@ def dedup_leg(device: int, seed: int = 4) -> dict:
 def mc3(wl, steps: int, device: int, chains: int = 8) -> dict:
     """Metropolis-coupled MCMC on the workload: `chains` FP32 chains at
     beta_i = 1 / (1 + 0.1 i), swap attempts every 10 steps, the moves of
-    mcmc_ess; every step stages all chains' proposals and evaluates them with
-    one CUDA-graph replay of the batched kernels."""
+    mcmc_ess.  Every chain launches its own evaluations on its own stream and
+    all chains' evaluations of a step are queued before any result is read
+    (the driver's default; the batched CUDA-graph launch is opt-in,
+    B3G_MCMC_BATCH=1)."""
     from aspartik_gb300.ess import min_ess
-    from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
+    from aspartik_gb300.mcmc import Mcmc
 
-    s = McmcSettings(model="gtr", precision="f32", num_categories=wl["spec"]["categories"],
-                     num_chains=chains, heat=0.1, swap_every=10, seed=4, sample_every=10,
-                     weights=dict(GTR_WEIGHTS), device=device)
+    s = mcmc_settings(wl, "f32", num_chains=chains, heat=0.1, swap_every=10, seed=4,
+                      device=device)
     m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
     m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
                      alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)
-    m.run(min(200, steps))  # warm-up (operator tuning, first graph replays)
+    m.run(min(200, steps))  # warm-up (operator tuning)
     t0 = time.perf_counter()
     m.run(steps)
     dt = time.perf_counter() - t0
     tried, accepted = m.swaps()
     keep = (steps // 10) // 5
-    traces = {k: m.trace(k)[keep:] for k in ("lnl", "root_height", "kappa_or_rate0")}
+    traces = {k: m.trace(k)[keep:] for k in ESS_FIELDS}
     e, _ = min_ess(traces, burn_in=0.0)
     out = {"chains": chains, "steps": steps, "seconds": round(dt, 3),
            "us_per_step": round(dt / steps * 1e6, 2),
@@ -625,8 +729,14 @@ def run_ours(args):
     lnl64 = c64.log_likelihood()
     c64.close()
 
-    mcmc = None if args.mcmc_steps <= 0 else mcmc_ess(wl, args.mcmc_steps, device)
-    mc3_out = None if args.mcmc_steps <= 0 else mc3(wl, max(1000, args.mcmc_steps // 4), device)
+    # the MCMC legs run once, on the single-GPU run (replicas add nothing)
+    long_legs = world == 1 and args.mcmc_steps > 0
+    mcmc = mcmc_ess(wl, args.mcmc_steps, device) if long_legs else None
+    mc3_out = mc3(wl, 5000, device) if long_legs else None
+    configs = None
+    if long_legs and args.workload == DEFAULT_WORKLOAD:
+        configs = {"dna16x1000_hky": config_block("dna16x1000_hky", device, 10_000),
+                   "dna64x10000_gtr_g4": config_block("dna64x10000_gtr_g4", device, 100_000)}
     dedup = None if args.no_cpu else dedup_leg(device)
     prot = prot_big = None
     if not args.no_protein:
@@ -701,6 +811,7 @@ def run_ours(args):
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
         "mc3": mc3_out,
+        "configs": configs,
         "dedup": dedup,
         "batched": batch,
         "protein20": prot,
@@ -839,8 +950,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-chains leg")
     ap.add_argument("--no-protein", action="store_true", help="skip the 20-state leg")
-    ap.add_argument("--mcmc-steps", type=int, default=20000,
-                    help="MCMC steps per form for the ESS/s comparison (0 = skip)")
+    ap.add_argument("--mcmc-steps", type=int, default=1_500_000,
+                    help="steps of the chosen-form MCMC arms of the ESS/s comparison; the "
+                         "plain arm runs 0.4x, burn-in and replicates 1/7.5x (0 = skip the "
+                         "MCMC legs and the smaller configurations)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
