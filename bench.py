@@ -145,6 +145,15 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 
+T_START = time.perf_counter()
+
+
+def progress(what: str) -> None:
+    """One line per finished leg on stderr (the JSON line stays alone on
+    stdout)."""
+    print(f"[bench {time.perf_counter() - T_START:7.1f} s] {what}", file=sys.stderr, flush=True)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -249,11 +258,15 @@ class CpuReference:
         self.threads = self.calcs[0].num_threads()
 
     def evaluate(self):
+        """One evaluation, accepted: every propose is followed by an accept,
+        as the reference's call order requires (two proposals in one epoch
+        would double-count its scale sums, cpu4.rs:403-433)."""
         t0 = time.perf_counter()
         per = []
         for calc, m in zip(self.calcs, self.mats):
             calc.propose(self.internals, self.children, m, self.pi)
             per.append(calc.likelihoods())
+            calc.accept()
         per = np.array(per)
         mx = per.max(axis=0)
         site = mx + np.log(np.exp(per - mx).sum(axis=0)) + np.log(1.0 / len(self.calcs))
@@ -521,13 +534,18 @@ def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
     start, tunings, burn_s = burn_in(wl, burn, device)
     out = {"burn_in": {"steps": burn, "seconds": round(burn_s, 3), "form": "f32",
                        "tunings": {k: round(v, 6) for k, v in tunings.items()}}}
+    progress("MCMC burn-in")
     out["plain_f64"] = mcmc_arm(wl, start, tunings, "f64", int(0.4 * chosen_steps), device)
+    progress("MCMC plain FP64 arm")
     out["chosen_f32"] = mcmc_arm(wl, start, tunings, "f32", chosen_steps, device)
+    progress("MCMC chosen FP32 arm")
     out["chosen_f32_da"] = mcmc_arm(wl, start, tunings, "f32", chosen_steps, device,
                                     da_pilot=min(100_000, chosen_steps // 5))
+    progress("MCMC delayed-acceptance arm")
     rep = int(chosen_steps / 7.5)
     out["chosen_f32_da_replicates"] = mcmc_arm(wl, start, tunings, "f32", rep, device,
                                                chains=8, da_pilot=rep // 8)
+    progress("MCMC replicates arm")
     base = max(out["plain_f64"]["ess_per_s"], 1e-12)
     for arm in ("chosen_f32", "chosen_f32_da", "chosen_f32_da_replicates"):
         out[f"ess_per_s_ratio_{arm}_vs_plain"] = round(out[arm]["ess_per_s"] / base, 3)
@@ -684,6 +702,7 @@ def run_ours(args):
     ms, t_tr, t_pr, nlaunch = device_throughput(calc, full, args.steps, args.warmup, world)
     kernels_per_eval = calc.last_launches()
     clk = clocks.stop()
+    progress("whole-tree throughput")
     ms_max = allreduce_max(ms, world)
     value = world * args.steps * B32 / (ms_max * 1e-3) / 1e9
     achieved = B32 / (t_pr * 1e-3) / 1e9
@@ -721,6 +740,7 @@ def run_ours(args):
     dbytes = sum(schedule.algorithmic_bytes(top, p[0], P, C, 4, w=4, e_b=4, w_p=4) for p in paths)
     mean_path = float(np.mean([len(p[0]) for p in paths]))
     calc.close()
+    progress("e2e and dirty path")
 
     # plain FP64 form, same workload
     c64 = make_calc(wl, "f64", device)
@@ -728,22 +748,30 @@ def run_ours(args):
     ms64, _, pr64, _ = device_throughput(c64, full, k64, args.warmup, world)
     lnl64 = c64.log_likelihood()
     c64.close()
+    progress("plain FP64 whole tree")
 
     # the MCMC legs run once, on the single-GPU run (replicas add nothing)
     long_legs = world == 1 and args.mcmc_steps > 0
     mcmc = mcmc_ess(wl, args.mcmc_steps, device) if long_legs else None
     mc3_out = mc3(wl, 5000, device) if long_legs else None
+    if long_legs:
+        progress("MC3")
     configs = None
     if long_legs and args.workload == DEFAULT_WORKLOAD:
-        configs = {"dna16x1000_hky": config_block("dna16x1000_hky", device, 10_000),
-                   "dna64x10000_gtr_g4": config_block("dna64x10000_gtr_g4", device, 100_000)}
+        configs = {"dna16x1000_hky": config_block("dna16x1000_hky", device, 10_000)}
+        progress("16-taxon configuration")
+        configs["dna64x10000_gtr_g4"] = config_block("dna64x10000_gtr_g4", device, 100_000)
+        progress("64-taxon configuration")
     dedup = None if args.no_cpu else dedup_leg(device)
+    progress("deduplication")
     prot = prot_big = None
     if not args.no_protein:
         prot = protein20(device, min(args.steps, 100), args.warmup)
         prot_big = protein20(device, min(args.steps, 20), args.warmup, N=50000,
                              forms=("f32", "f32_cuda_cores"))
+    progress("20 states")
     batch = None if args.no_batch else batched(device, min(args.steps, 200), args.warmup)
+    progress("batched chains")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
