@@ -185,7 +185,15 @@ struct DirectParams {
 	double rate[4];
 	NodeOp ops[kDirectMax];
 	double lengths[2 * kDirectMax]; // [n][2] time lengths
+	// where entry i's left (0) and right (1) child comes from (kSrc*)
+	uint8_t src[kDirectMax][2];
 };
+
+// Sources of a child in the fused short-list walk, set by the host: a tip
+// code, a clean partial (not an output of this list: loaded ahead), the
+// previous or the second previous entry's output (registers), or an older
+// output of this list (read back when needed).
+enum : uint8_t { kSrcTip = 0, kSrcClean, kSrcPrev, kSrcPrev2, kSrcEarlier };
 
 // Launchers (kernels4.cu).  Each returns the launch error.
 cudaError_t launch_ptab4(const PtabParams &p, bool f32, cudaStream_t s);

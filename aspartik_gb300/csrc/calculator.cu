@@ -817,6 +817,28 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	dp.eig[37] = dp.eig[38] = dp.eig[39] = 0.0f;
 	std::memcpy(dp.ops, h_stage_, (size_t)n * sizeof(NodeOp));
 	std::memcpy(dp.lengths, h_stage_ + off_in_, (size_t)n * 2 * sizeof(double));
+	// where each child comes from in the walk
+	for (uint32_t i = 0; i < n; ++i) {
+		const uint32_t ids[2] = {dp.ops[i].left, dp.ops[i].right};
+		for (int j = 0; j < 2; ++j) {
+			const uint32_t id = ids[j];
+			uint8_t src = kSrcClean;
+			if (id & kTipBit) {
+				src = kSrcTip;
+			} else if (i >= 1 && id == dp.ops[i - 1].out) {
+				src = kSrcPrev;
+			} else if (i >= 2 && id == dp.ops[i - 2].out) {
+				src = kSrcPrev2;
+			} else {
+				for (uint32_t k = 0; k + 2 < i; ++k)
+					if (dp.ops[k].out == id) {
+						src = kSrcEarlier;
+						break;
+					}
+			}
+			dp.src[i][j] = src;
+		}
+	}
 	// bytes that reach the device with the launch
 	last_upload_bytes_ = (uint64_t)n * (sizeof(NodeOp) + 2 * sizeof(double)) +
 			     4 * sizeof(double);
@@ -825,8 +847,9 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 		harvest(slot);
 	slot.direct = true;
 	record(slot.k0);
-	// 128-pattern tiles, 128 * C threads per block, 1024 threads per SM
-	const uint32_t ctas = std::min(ldp_ / 128u, (8u / C_) * num_sms_);
+	// 128-pattern tiles, 128 * C threads per block, 512 threads per SM (the
+	// walk's loads ahead take up to 128 registers a thread)
+	const uint32_t ctas = std::min(ldp_ / 128u, (4u / C_) * num_sms_);
 	arm_poll();
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
 	++in_flight_;

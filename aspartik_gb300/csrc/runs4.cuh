@@ -201,6 +201,9 @@ __device__ __forceinline__ void run_item2(const TileArgs &a,
 	}
 }
 
+__device__ double tile_root(const TileArgs &a, uint32_t t, const float *s_dot,
+			    const int32_t *s_cnt, double *s_red);
+
 // One pattern tile t: every run of the schedule, then the category mixing
 // of the root.  Returns the tile's weighted site sum in thread 0.  Ends with
 // the block synchronised.  s_dot/s_cnt hold tile * C entries, s_red 32;
@@ -365,7 +368,18 @@ __device__ double tile_walk(const TileArgs &a, uint32_t t, float *s_dot,
 			__syncthreads();
 		}
 	}
-	// root: category mixing per pattern (threads 0 .. tile-1)
+	return tile_root(a, t, s_dot, s_cnt, s_red);
+}
+
+// Root of tile t after its walk left pi . x and the exponent of every
+// column in s_dot / s_cnt: category mixing per pattern (threads 0 ..
+// tile-1), site values, and the tile's weighted sum in a fixed order,
+// returned in thread 0.  Ends with the block synchronised.
+__device__ double tile_root(const TileArgs &a, uint32_t t, const float *s_dot,
+			    const int32_t *s_cnt, double *s_red)
+{
+	const uint32_t tile = a.tile, C = a.C;
+	const uint32_t tid = threadIdx.x;
 	double contrib = 0.0;
 	if (tid < tile) {
 		const uint32_t pp = t * tile + tid;
@@ -570,37 +584,93 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 // ---------------------------------------------------------------------------
 // Fused evaluation of a short list in one launch (FP32, four states, kC =
 // 1, 2 or 4 categories, 128-pattern tiles: one thread per column, serial
-// walk).  Every
-// block converts the device eigensystem to FP32, builds the list's
-// transition tables in shared memory with the same arithmetic as the
+// walk).  Every block converts the device eigensystem to FP32, builds the
+// list's transition tables in shared memory with the same arithmetic as the
 // transition kernels (so results match a two-kernel evaluation bit for
 // bit), walks its tiles, and the last block writes the root lnL to the
 // device and to the host-mapped word.
+//
+// The walk is a chain: each entry needs the previous one's output, and its
+// other child is a clean partial written long ago (mostly in DRAM) or a tip
+// code.  Every clean input and tip code is known before the walk starts
+// (the host marks each child's source in DirectParams::src), so they are
+// loaded kDirectAhead entries ahead of their use, the first ones before the
+// tables are built: one DRAM round trip for the whole list instead of one
+// per entry.  The two previous outputs stay in registers; an older output
+// is read back when needed (written by the same thread earlier).
+constexpr uint32_t kDirectAhead = 4;
+
+template <typename Idx>
+__device__ __forceinline__ void direct_fetch(const DirectParams &prm, uint32_t i,
+					     const float4 *part, const int32_t *scales,
+					     const uint8_t *tips_p, Idx stride, Idx col_off,
+					     float4 (&v)[2], int32_t (&s)[2])
+{
+	const NodeOp &op = prm.ops[i];
+	const uint32_t ids[2] = {op.left, op.right};
+#pragma unroll
+	for (int j = 0; j < 2; ++j) {
+		const uint32_t src = prm.src[i][j];
+		if (src == kSrcTip) {
+			s[j] = tips_p[(size_t)(ids[j] & ~kTipBit) * prm.ldp];
+		} else if (src == kSrcClean) {
+			const Idx ix = (Idx)ids[j] * stride + col_off;
+			v[j] = part[ix];
+			s[j] = scales[ix];
+		}
+	}
+}
+
 template <typename Idx, uint32_t kC>
-__global__ void __launch_bounds__(128 * kC, 8 / kC)
+__global__ void __launch_bounds__(128 * kC, 4 / kC)
 prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 {
 	constexpr uint32_t kTile = 128, kCols = kTile * kC;
 	__shared__ float4 s_tab[kDirectMax * 2 * kC * 5];
 	__shared__ float s_eig[37];
 	__shared__ double s_rate[kC];
+	__shared__ float s_pi[4];
 	__shared__ float s_dot[kCols];
 	__shared__ int32_t s_cnt[kCols];
 	__shared__ double s_red[32];
 	__shared__ unsigned s_last;
 	const uint32_t tid = threadIdx.x;
 	const ModelDev *m = prm.model;
+	const uint32_t n = prm.n;
+	const uint32_t ntiles = prm.ldp / kTile;
+	// this thread's column
+	const uint32_t c = tid / kTile, pl = tid - c * kTile;
+	const Idx stride = (Idx)kC * prm.ldp;
+	const float4 *part = (const float4 *)prm.partials;
+	float4 *part_w = (float4 *)prm.partials;
+
+	// clean inputs of the first entries of the first tile, in flight while
+	// the tables are built
+	float4 pv[kDirectAhead][2];
+	int32_t ps[kDirectAhead][2];
+	uint32_t t = blockIdx.x;
+	if (t < ntiles) {
+		const Idx col_off = (Idx)c * prm.ldp + t * kTile + pl;
+		const uint8_t *tips_p = prm.tips + t * kTile + pl;
+#pragma unroll
+		for (uint32_t u = 0; u < kDirectAhead; ++u)
+			if (u < n)
+				direct_fetch<Idx>(prm, u, part, prm.scales, tips_p, stride,
+						  col_off, pv[u], ps[u]);
+	}
 	// from the parameters: no global-memory round trip before the tables
 	if (tid < 37)
 		s_eig[tid] = prm.eig[tid];
 	else if (tid < 37 + kC)
 		s_rate[tid - 37] = prm.rate[tid - 37];
+	else if (tid >= 64 && tid < 68)
+		s_pi[tid - 64] = (float)prm.pi[tid - 64];
 	__syncthreads();
-	if (tid < prm.n * 2 * kC) {
+	if (tid < n * 2 * kC) {
 		// table (entry, side, category), laid out as ptab4_kernel's
-		const uint32_t c = tid % kC, es = tid / kC;
+		const uint32_t cc = tid % kC, es = tid / kC;
 		float P[16];
-		transition4f_eig(m, s_eig, prm.lengths[es] * s_rate[c], P);
+		transition4f_eig(m, s_eig, prm.lengths[es] * s_rate[cc], P);
 		float *out = reinterpret_cast<float *>(s_tab + tid * 5);
 		for (int k = 0; k < 4; k++)
 			for (int j = 0; j < 4; j++)
@@ -612,7 +682,7 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 
 	TileArgs a;
 	a.tips = prm.tips;
-	a.part = (float4 *)prm.partials;
+	a.part = part_w;
 	a.scales = prm.scales;
 	a.ptab = s_tab;
 	a.pi = prm.pi;
@@ -623,15 +693,77 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	a.C = kC;
 	a.L = prm.L;
 	a.tile = kTile;
-	a.n = prm.n;
-	a.n_runs = 0; // the serial walk needs no runs
+	a.n = n;
+	a.n_runs = 0;
 	a.tips_smem = 0;
 	a.log_inv_c = prm.log_inv_c;
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
-	const uint32_t ntiles = prm.ldp / kTile;
-	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const double tsum = tile_walk<Idx, true>(a, t, s_dot, s_cnt, s_red,
-							 prm.ops, nullptr, nullptr);
+	for (; t < ntiles; t += gridDim.x) {
+		const Idx col_off = (Idx)c * prm.ldp + t * kTile + pl;
+		const uint8_t *tips_p = prm.tips + t * kTile + pl;
+		if (t != blockIdx.x) {
+#pragma unroll
+			for (uint32_t u = 0; u < kDirectAhead; ++u)
+				if (u < n)
+					direct_fetch<Idx>(prm, u, part, prm.scales, tips_p,
+							  stride, col_off, pv[u], ps[u]);
+		}
+		float4 y0 = make_float4(0.f, 0.f, 0.f, 0.f), y1 = y0;
+		int32_t c0 = 0, c1 = 0;
+		for (uint32_t i0 = 0; i0 < n; i0 += kDirectAhead) {
+#pragma unroll
+			for (uint32_t u = 0; u < kDirectAhead; ++u) {
+				const uint32_t i = i0 + u;
+				if (i < n) {
+					const NodeOp op = prm.ops[i];
+					const float4 *tl = s_tab + ((size_t)(2 * i) * kC + c) * 5;
+					const float4 *tr = tl + 5 * kC;
+					float4 in[2];
+					int32_t sc[2];
+					const uint32_t ids[2] = {op.left, op.right};
+#pragma unroll
+					for (int j = 0; j < 2; ++j) {
+						const float4 *tb = j ? tr : tl;
+						const uint32_t src = prm.src[i][j];
+						if (src == kSrcTip) {
+							in[j] = tb[ps[u][j]];
+							sc[j] = 0;
+						} else if (src == kSrcClean) {
+							in[j] = v4_apply(tb, pv[u][j]);
+							sc[j] = ps[u][j];
+						} else if (src == kSrcPrev) {
+							in[j] = v4_apply(tb, y0);
+							sc[j] = c0;
+						} else if (src == kSrcPrev2) {
+							in[j] = v4_apply(tb, y1);
+							sc[j] = c1;
+						} else {
+							const Idx ix = (Idx)ids[j] * stride + col_off;
+							in[j] = v4_apply(tb, part[ix]);
+							sc[j] = prm.scales[ix];
+						}
+					}
+					// the slot just consumed takes entry i + ahead
+					if (i + kDirectAhead < n)
+						direct_fetch<Idx>(prm, i + kDirectAhead, part,
+								  prm.scales, tips_p, stride, col_off,
+								  pv[u], ps[u]);
+					float4 y = v4_mul(in[0], in[1]);
+					const int32_t cnt = sc[0] + sc[1] + rescale_pow2(y);
+					const Idx ox = (Idx)op.out * stride + col_off;
+					part_w[ox] = y;
+					prm.scales[ox] = cnt;
+					y1 = y0;
+					c1 = c0;
+					y0 = y;
+					c0 = cnt;
+				}
+			}
+		}
+		s_dot[tid] = root_dot4(s_pi, y0);
+		s_cnt[tid] = c0;
+		__syncthreads();
+		const double tsum = tile_root(a, t, s_dot, s_cnt, s_red);
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
 	}
