@@ -103,7 +103,20 @@ class McmcConfig(ct.Structure):
         ("da_reserved", ct.c_uint32),
         ("da_drift_limit", ct.c_double),
         ("clock_categories", ct.c_uint32),
-        ("clock_reserved", ct.c_uint32),
+        ("launch", ct.c_uint32),
+    ]
+
+
+class McmcProblem(ct.Structure):
+    """b3g_mcmc_problem."""
+
+    _fields_ = [
+        ("num_leaves", ct.c_uint32),
+        ("num_patterns", ct.c_uint32),
+        ("samples", ct.c_void_p),
+        ("weights", ct.c_void_p),
+        ("parents", ct.c_void_p),
+        ("heights", ct.c_void_p),
     ]
 
 
@@ -183,6 +196,10 @@ SIGNATURES = {
     "b3g_mcmc_create": (ct.c_int, [ct.POINTER(McmcConfig), ct.c_uint32, ct.c_uint32, _u8p,
                                    _u32p, _u32p, _f64p, ct.POINTER(_vp)]),
     "b3g_mcmc_destroy": (None, [_vp]),
+    "b3g_mcmc_create_multi": (ct.c_int, [ct.POINTER(McmcConfig), ct.c_uint32,
+                                         ct.POINTER(McmcProblem), ct.POINTER(_vp)]),
+    "b3g_mcmc_launch_stats": (ct.c_int, [_vp, ct.POINTER(ct.c_uint32),
+                                         ct.POINTER(ct.c_double), ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_set_parameters": (ct.c_int, [_vp, ct.c_double, _f64p, _f64p, ct.c_double,
                                            ct.c_double]),
     "b3g_mcmc_run": (ct.c_int, [_vp, ct.c_uint64]),

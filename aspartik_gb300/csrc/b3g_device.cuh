@@ -134,6 +134,9 @@ struct MemberStep {
 	uint32_t n_runs;
 	uint32_t tips_smem;
 	uint32_t tile; // patterns per tile for this step (divides ldp)
+	// a short list (n <= kDirectMax, C of 1, 2 or 4): walked by the
+	// batched short-list kernel instead of the run walk
+	uint32_t direct;
 	double clock_rate;
 };
 
@@ -141,7 +144,9 @@ struct BatchParams {
 	const MemberDesc *members;
 	const MemberStep *steps;
 	double *lnl_out;     // [members]
-	unsigned *work_next; // work counter, zero before each launch
+	unsigned *work_next; // work counters, zero before each launch: [0] the
+			     // run walk's, [1..3] the short-list kernels' (4,
+			     // 2 and 1 categories)
 	uint32_t num_members;
 	uint32_t smem_ops_bytes;  // shared memory reserved for ops + runs
 	uint32_t smem_tips_bytes; // shared memory reserved for a tip tile
@@ -256,5 +261,10 @@ cudaError_t launch_ptab4_batch(const BatchParams &p, uint32_t max_entries,
 			       cudaStream_t s);
 cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
 				cudaStream_t s);
+// Batched short lists: every member whose step is direct and has C
+// categories (1, 2 or 4), `ctas` persistent blocks taking (member, tile)
+// items from that category count's counter.
+cudaError_t launch_prune4_direct_batch(const BatchParams &p, uint32_t C,
+				       uint32_t ctas, cudaStream_t s);
 
 } // namespace b3g

@@ -2,11 +2,14 @@
 // as a CUDA graph.
 //
 // Every member keeps its own device store.  A step is: each member stages
-// its dirty list and edge lengths (b3g_calculator_stage_lengths, host only),
-// then b3g_batch_run replays one graph: the members' staging copies, one
-// batched transition-table kernel, one persistent pruning kernel over every
-// member's pattern tiles (handed out by an atomic work counter, costliest
-// member first), and the read-back of every member's log-likelihood.
+// its dirty list and edge lengths (b3g_calculator_stage_lengths, host only)
+// into its slice of one contiguous pinned block, then b3g_batch_run replays
+// one graph: one copy of that block, the run walk for the members with long
+// lists (one batched transition-table kernel, one persistent pruning kernel
+// over their pattern tiles, handed out by an atomic work counter, costliest
+// member first), one persistent short-list kernel per category count for the
+// members with short lists (their tables built in shared memory, a serial
+// walk per column), and the read-back of every member's log-likelihood.
 #include "batch.hpp"
 
 #include <algorithm>
@@ -67,7 +70,7 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		check_cuda(cudaHostAlloc((void **)&h_lnl_, sizeof(double) * M,
 					 cudaHostAllocDefault),
 			   "pinned lnl");
-		check_cuda(cudaMalloc(&d_work_, sizeof(unsigned)), "work counter");
+		check_cuda(cudaMalloc(&d_work_, 4 * sizeof(unsigned)), "work counters");
 		size_t total_tiles = 0;
 		for (Calculator *c : members_)
 			total_tiles += c->ldp_ / c->runs_tile_;
@@ -87,7 +90,7 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 			d.partials = static_cast<float *>(c->d_partials_);
 			d.scales = c->d_scales_;
 			d.ptab = static_cast<float *>(c->d_ptab_);
-			d.stage = c->d_stage_;
+			d.stage = nullptr; // set to the member's slice below
 			d.model = c->d_model_;
 			d.weights = c->d_weights_;
 			d.site_lnl = c->d_site_;
@@ -112,6 +115,31 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 			max_entries_ = std::max<uint32_t>(max_entries_, c->I_ * 2 * c->C_);
 			if ((uint64_t)c->L_ * 2 * c->C_ * c->ldp_ >= (1ull << 31))
 				narrow = false;
+			if (c->C_ == 1 || c->C_ == 2 || c->C_ == 4)
+				direct_c_[c->C_] = true;
+		}
+		// the members' staging slices: each member's layout up to the end
+		// of its edge lengths (lengths-mode proposals only while batched)
+		std::vector<size_t> slice(M);
+		for (uint32_t k = 0; k < M; ++k) {
+			const Calculator *c = members_[order_[k]];
+			slice[k] = block_bytes_;
+			block_bytes_ += (c->off_in_ + (size_t)c->I_ * 2 * sizeof(double) + 255) &
+					~(size_t)255;
+		}
+		check_cuda(cudaHostAlloc((void **)&h_block_, block_bytes_, cudaHostAllocDefault),
+			   "pinned staging block");
+		check_cuda(cudaMalloc(&d_block_, block_bytes_), "staging block");
+		for (uint32_t k = 0; k < M; ++k) {
+			Calculator *c = members_[order_[k]];
+			// the member's own last launch must be done with its buffer
+			c->wait_stage();
+			check_cuda(cudaStreamSynchronize(c->stream_), "member stream");
+			c->own_h_stage_ = c->h_stage_;
+			c->own_d_stage_ = c->d_stage_;
+			c->h_stage_ = h_block_ + slice[k];
+			c->d_stage_ = d_block_ + slice[k];
+			desc[k].stage = c->d_stage_;
 			c->in_batch_ = true;
 		}
 		check_cuda(cudaMemcpy(d_desc_, desc.data(), sizeof(MemberDesc) * M,
@@ -141,19 +169,20 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		check_cuda(cudaMemcpyAsync(d_steps_, h_steps_, sizeof(MemberStep) * M,
 					   cudaMemcpyHostToDevice, stream_),
 			   "steps copy");
-		for (uint32_t k = 0; k < M; ++k) {
-			Calculator *c = members_[order_[k]];
-			const size_t bytes = c->off_in_ + (size_t)c->I_ * 2 * sizeof(double);
-			check_cuda(cudaMemcpyAsync(c->d_stage_, c->h_stage_, bytes,
-						   cudaMemcpyHostToDevice, stream_),
-				   "stage copy");
-		}
-		check_cuda(cudaMemsetAsync(d_work_, 0, sizeof(unsigned), stream_),
-			   "work counter");
+		check_cuda(cudaMemcpyAsync(d_block_, h_block_, block_bytes_,
+					   cudaMemcpyHostToDevice, stream_),
+			   "staging block copy");
+		check_cuda(cudaMemsetAsync(d_work_, 0, 4 * sizeof(unsigned), stream_),
+			   "work counters");
 		check_cuda(launch_ptab4_batch(bp_, max_entries_, stream_),
 			   "batched transition kernel");
 		check_cuda(launch_prune4_batch(bp_, ctas_, stream_),
 			   "batched pruning kernel");
+		for (uint32_t C : {4u, 2u, 1u})
+			if (direct_c_[C])
+				check_cuda(launch_prune4_direct_batch(
+						   bp_, C, (4u / C) * members_[0]->num_sms_, stream_),
+					   "batched short-list kernel");
 		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double) * M,
 					   cudaMemcpyDeviceToHost, stream_),
 			   "lnl copy");
@@ -177,12 +206,29 @@ void Batch::release()
 	if (stream_)
 		cudaStreamSynchronize(stream_);
 	for (Calculator *c : members_) {
+		if (c && c->own_h_stage_ &&
+		    c->h_stage_ >= h_block_ && c->h_stage_ < h_block_ + block_bytes_) {
+			// the member's own launches may still read the lent slice
+			c->wait_stage();
+			if (c->stream_)
+				cudaStreamSynchronize(c->stream_);
+			c->h_stage_ = c->own_h_stage_;
+			c->d_stage_ = c->own_d_stage_;
+			c->own_h_stage_ = nullptr;
+			c->own_d_stage_ = nullptr;
+			c->in_batch_ = false;
+			c->staged_ = false;
+		}
 		if (c && c->batch_done_ == ev1_) {
 			c->batch_done_ = nullptr;
 			c->in_batch_ = false;
 			c->staged_ = false;
 		}
 	}
+	cudaFreeHost(h_block_);
+	cudaFree(d_block_);
+	h_block_ = nullptr;
+	d_block_ = nullptr;
 	if (exec_)
 		cudaGraphExecDestroy(exec_);
 	if (graph_)
@@ -232,12 +278,17 @@ void Batch::run()
 			s.tile = c->staged_tile_;
 			s.tips_smem = c->staged_tips_smem_;
 			s.clock_rate = c->staged_clock_;
+			s.direct = (c->staged_n_ <= kDirectMax &&
+				    (c->C_ == 1 || c->C_ == 2 || c->C_ == 4))
+					   ? 1u
+					   : 0u;
 			c->staged_ = false;
 		} else {
 			s.n = 0;
 			s.n_runs = 0;
 			s.tile = c->runs_tile_;
 			s.tips_smem = 0;
+			s.direct = 0;
 			s.clock_rate = 1.0;
 		}
 	}

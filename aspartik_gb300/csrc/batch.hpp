@@ -37,6 +37,12 @@ class Batch {
 	cudaGraphExec_t exec_ = nullptr;
 	BatchParams bp_{};
 	uint32_t max_entries_ = 0, ctas_ = 0;
+	// one contiguous staging block for every member (copied by one graph
+	// node); each member's h_stage_ / d_stage_ point into it while it is
+	// in the batch
+	unsigned char *h_block_ = nullptr, *d_block_ = nullptr;
+	size_t block_bytes_ = 0;
+	bool direct_c_[5] = {}; // members with 1, 2 or 4 categories present
 	bool ran_ = false;
 	std::vector<uint8_t> evaluated_;
 };

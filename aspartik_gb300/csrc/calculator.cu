@@ -311,8 +311,10 @@ void Calculator::release()
 	cudaFree(d_lnl_);
 	cudaFree(d_model_);
 	cudaFree(d_ptab_);
-	cudaFree(d_stage_);
-	cudaFreeHost(h_stage_);
+	cudaFree(own_d_stage_ ? own_d_stage_ : d_stage_);
+	cudaFreeHost(own_h_stage_ ? own_h_stage_ : h_stage_);
+	own_d_stage_ = nullptr;
+	own_h_stage_ = nullptr;
 	cudaFreeHost(h_model_);
 	cudaFreeHost(h_lnl_);
 	d_tips_ = nullptr;
@@ -871,6 +873,9 @@ void Calculator::propose_matrices(const uint32_t *internals,
 	validate_lists(internals, children, n);
 	if (!matrices || !freqs)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "null matrices");
+	if (own_h_stage_)
+		throw Error(B3G_ERR_STATE,
+			    "a calculator in a batch takes edge-length proposals only");
 	const size_t count = (size_t)n * 2 * C_ * S_ * S_;
 	for (size_t k = 0; k < count; ++k)
 		if (!std::isfinite(matrices[k]))

@@ -201,6 +201,10 @@ class Calculator {
 
 	// pinned host staging
 	unsigned char *h_stage_ = nullptr;
+	// a batch lends h_stage_ / d_stage_ a slice of its one contiguous
+	// staging block (lengths-mode proposals only while it does); the
+	// calculator's own buffers wait here and come back when it ends
+	unsigned char *own_h_stage_ = nullptr, *own_d_stage_ = nullptr;
 	ModelDev *h_model_ = nullptr;
 	double *h_lnl_ = nullptr;
 	double *d_lnl_host_ = nullptr; // device view of h_lnl_

@@ -841,6 +841,31 @@ cudaError_t launch_prune4_batch(const BatchParams &p, uint32_t ctas,
 	return cudaGetLastError();
 }
 
+cudaError_t launch_prune4_direct_batch(const BatchParams &p, uint32_t C,
+				       uint32_t ctas, cudaStream_t s)
+{
+	const uint32_t threads = 128 * C;
+	if (C == 4) {
+		if (p.narrow)
+			prune4_direct_batch_kernel<uint32_t, 4><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_batch_kernel<size_t, 4><<<ctas, threads, 0, s>>>(p);
+	} else if (C == 2) {
+		if (p.narrow)
+			prune4_direct_batch_kernel<uint32_t, 2><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_batch_kernel<size_t, 2><<<ctas, threads, 0, s>>>(p);
+	} else if (C == 1) {
+		if (p.narrow)
+			prune4_direct_batch_kernel<uint32_t, 1><<<ctas, threads, 0, s>>>(p);
+		else
+			prune4_direct_batch_kernel<size_t, 1><<<ctas, threads, 0, s>>>(p);
+	} else {
+		return cudaErrorInvalidValue;
+	}
+	return cudaGetLastError();
+}
+
 cudaError_t launch_ptab20(const PtabParams &p, bool f32, cudaStream_t s)
 {
 	const uint32_t tables = p.n * 2u * p.C;

@@ -81,12 +81,27 @@ uint32_t Rng::below(uint32_t n)
 Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 	   const uint8_t *samples, const uint32_t *weights,
 	   const uint32_t *parents, const double *heights)
+    : Mcmc(cfg, std::vector<Problem>{Problem{L, P, samples, weights, parents, heights}})
+{
+}
+
+Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
     : cfg_(cfg), swap_rng_(cfg.seed ^ 0x5EEDu)
 {
 	if (cfg.num_chains < 1 || cfg.num_chains > 256)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "num_chains must be 1..256");
+	if (problems.empty() || cfg.num_chains % problems.size() != 0)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "num_chains must be a multiple of the number of problems");
+	num_problems_ = (uint32_t)problems.size();
+	if (num_problems_ > 1 && cfg.da_pilot_steps)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "delayed acceptance needs a single problem (one surrogate "
+			    "per alignment)");
 	if (cfg.model > 1)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "model must be 0 (HKY) or 1 (GTR)");
+	if (cfg.launch > kLaunchBatch)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
 	for (uint32_t k = 0; k < kOpCount; ++k) {
 		if (!(cfg.weights[k] >= 0.0) || !std::isfinite(cfg.weights[k]))
 			throw Error(B3G_ERR_INVALID_ARGUMENT, "bad operator weight");
@@ -97,34 +112,41 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 	// DeltaExchange starts at tuning 0.75 like the scale operators
 	for (auto &o : ops_)
 		o.tuning = 0.75;
-	b3g_config cc{};
-	cc.num_leaves = L;
-	cc.num_patterns = P;
-	cc.num_states = 4;
-	cc.num_categories = cfg.num_categories;
-	cc.precision = cfg.precision;
-	cc.scale_ln = 30;
-	cc.device = cfg.device;
+	const uint32_t group = cfg.num_chains / num_problems_;
 	for (uint32_t i = 0; i < cfg.num_chains; ++i) {
+		const Problem &pr = problems[i / group];
+		if (!pr.samples || !pr.weights || !pr.parents || !pr.heights)
+			throw Error(B3G_ERR_INVALID_ARGUMENT, "null problem array");
+		b3g_config cc{};
+		cc.num_leaves = pr.L;
+		cc.num_patterns = pr.P;
+		cc.num_states = 4;
+		cc.num_categories = cfg.num_categories;
+		cc.precision = cfg.precision;
+		cc.scale_ln = 30;
+		cc.device = cfg.device;
 		auto ch = std::make_unique<Chain>(cfg.seed + 0x9E37u * (i + 1));
 		try {
-			ch->tree = std::make_unique<DatedTree>(parents, heights, 2 * L - 1);
+			ch->tree = std::make_unique<DatedTree>(pr.parents, pr.heights,
+							       2 * pr.L - 1);
 		} catch (const std::exception &e) {
 			throw Error(B3G_ERR_INVALID_ARGUMENT, e.what());
 		}
-		ch->calc = std::make_unique<Calculator>(cc, samples);
+		ch->calc = std::make_unique<Calculator>(cc, pr.samples);
 		ch->calc->set_timing(false); // the driver reads no kernel timings
-		ch->calc->set_weights(weights);
-		ch->beta = 1.0 / (1.0 + cfg.heat * i);
+		ch->calc->set_weights(pr.weights);
+		ch->beta = 1.0 / (1.0 + cfg.heat * (i % group));
 		ch->index = i;
+		ch->problem = i / group;
 		ch->kappa.v = 2.0;
 		ch->alpha.v = 0.5;
 		ch->birth_rate.v = 1.0;
 		ch->rates.v.assign(6, 1.0);
 		ch->freqs.v.assign(4, 0.25);
 		if (cfg.clock_categories) {
-			ch->edge_cat.resize(2 * L - 1);
-			for (uint32_t v = 0; v < 2 * L - 1; ++v)
+			const uint32_t nodes = 2 * pr.L - 1;
+			ch->edge_cat.resize(nodes);
+			for (uint32_t v = 0; v < nodes; ++v)
 				ch->edge_cat[v] = v % cfg.clock_categories;
 			ch->clock_sd.v = 0.3;
 			clock_rates(*ch);
@@ -132,14 +154,15 @@ Mcmc::Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 		chains_.push_back(std::move(ch));
 	}
 	set_parameters(2.0, nullptr, nullptr, 0.5, 1.0);
-	// several FP32 chains can share one batched launch per step
-	// (B3G_MCMC_BATCH=1); by default every chain launches its own
-	// evaluations on its own stream (short lists take the fused
-	// one-kernel path) and the launches of a step run concurrently
-	bool use_batch = false;
+	// every chain of a step in one graph-replayed batched launch (FP32
+	// chosen form, several chains), or each chain's launches on its own
+	// stream, the launches of a step running concurrently
+	bool use_batch = cfg.launch == kLaunchBatch;
 	if (const char *env = std::getenv("B3G_MCMC_BATCH"))
 		use_batch = std::atoi(env) != 0;
-	if (cfg.precision == B3G_PRECISION_F32 && chains_.size() > 1 && use_batch) {
+	if (use_batch && (cfg.precision != B3G_PRECISION_F32 || chains_.size() < 2))
+		use_batch = false;
+	if (use_batch) {
 		std::vector<Calculator *> calcs;
 		for (auto &ch : chains_)
 			calcs.push_back(ch->calc.get());
@@ -257,6 +280,9 @@ void Mcmc::set_clock(double sd, const uint32_t *categories)
 		throw Error(B3G_ERR_STATE, "the chains use a strict clock");
 	if (!(sd > 0.0) || !std::isfinite(sd))
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "clock sd must be finite and > 0");
+	if (categories && num_problems_ > 1)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "per-node clock categories need a single problem");
 	for (auto &chp : chains_) {
 		Chain &ch = *chp;
 		const uint32_t nodes = ch.tree->num_nodes();
@@ -772,25 +798,27 @@ void Mcmc::finish(Chain &ch)
 // min(1, exp((b_i - b_j) (post_j - post_i))); the betas move, not the states.
 void Mcmc::swap_temperatures()
 {
-	const uint32_t n = (uint32_t)chains_.size();
-	if (n < 2)
+	const uint32_t group = (uint32_t)chains_.size() / num_problems_;
+	if (group < 2)
 		return;
-	std::vector<uint32_t> by_beta(n);
-	for (uint32_t i = 0; i < n; ++i)
-		by_beta[i] = i;
-	std::sort(by_beta.begin(), by_beta.end(), [&](uint32_t a, uint32_t b) {
-		return chains_[a]->beta > chains_[b]->beta;
-	});
-	const uint32_t k = swap_rng_.below(n - 1);
-	Chain &a = *chains_[by_beta[k]];
-	Chain &b = *chains_[by_beta[k + 1]];
-	const double pa = a.lnl_cache + a.prior_cache;
-	const double pb = b.lnl_cache + b.prior_cache;
-	const double lr = (a.beta - b.beta) * (pb - pa);
-	++swaps_tried_;
-	if (lr > std::log(swap_rng_.uniform())) {
-		std::swap(a.beta, b.beta);
-		++swaps_accepted_;
+	std::vector<uint32_t> by_beta(group);
+	for (uint32_t g = 0; g < num_problems_; ++g) {
+		for (uint32_t i = 0; i < group; ++i)
+			by_beta[i] = g * group + i;
+		std::sort(by_beta.begin(), by_beta.end(), [&](uint32_t a, uint32_t b) {
+			return chains_[a]->beta > chains_[b]->beta;
+		});
+		const uint32_t k = swap_rng_.below(group - 1);
+		Chain &a = *chains_[by_beta[k]];
+		Chain &b = *chains_[by_beta[k + 1]];
+		const double pa = a.lnl_cache + a.prior_cache;
+		const double pb = b.lnl_cache + b.prior_cache;
+		const double lr = (a.beta - b.beta) * (pb - pa);
+		++swaps_tried_;
+		if (lr > std::log(swap_rng_.uniform())) {
+			std::swap(a.beta, b.beta);
+			++swaps_accepted_;
+		}
 	}
 }
 
@@ -910,6 +938,8 @@ void Mcmc::run(uint64_t steps)
 		if (batch_ && any) {
 			batch_->run();
 			batch_->log_likelihoods(batch_lnl_.data());
+			batch_ms_ += batch_->last_ms();
+			++batch_runs_;
 		}
 		for (auto &ch : chains_)
 			finish(*ch);

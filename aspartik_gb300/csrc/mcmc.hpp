@@ -110,6 +110,20 @@ struct OpStats {
 	double tuning = 0.75;
 };
 
+// One alignment of the driver with the start tree of its chains.
+struct Problem {
+	uint32_t L, P;
+	const uint8_t *samples;
+	const uint32_t *weights;
+	const uint32_t *parents;
+	const double *heights;
+};
+
+enum : uint32_t {
+	kLaunchStreams = 0, // one launch per chain, each chain on its own stream
+	kLaunchBatch = 1,   // every chain of a step in one graph-replayed batch
+};
+
 struct McmcConfig {
 	uint32_t num_chains;
 	uint32_t num_categories;
@@ -128,6 +142,7 @@ struct McmcConfig {
 	uint32_t da_hidden;
 	double da_drift_limit;
 	uint32_t clock_categories; // 0: strict clock
+	uint32_t launch;           // kLaunch*
 };
 
 // Inputs of the surrogate, for the moves that re-evaluate the whole tree
@@ -162,6 +177,7 @@ struct Chain {
 	std::vector<double> clock_rates;
 	double beta = 1.0;
 	uint32_t index = 0;
+	uint32_t problem = 0; // the alignment, and the chain's temperature group
 	double lnl_cache = 0.0, lnl_new = 0.0;
 	double prior_cache = 0.0, prior_new = 0.0;
 	bool launched = false;   // a device evaluation is pending
@@ -185,6 +201,10 @@ class Mcmc {
 	Mcmc(const McmcConfig &cfg, uint32_t L, uint32_t P,
 	     const uint8_t *samples, const uint32_t *weights,
 	     const uint32_t *parents, const double *heights);
+	// Several alignments: num_chains / problems.size() chains per problem,
+	// chain i on problem i / that count at temperature index i % that count
+	// (MC3 swaps only between chains of one problem).
+	Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems);
 
 	void set_clock(double sd, const uint32_t *categories);
 	void set_parameters(double kappa, const double *rates,
@@ -225,6 +245,15 @@ class Mcmc {
 	void chain_state(uint32_t chain, uint32_t *parents, double *heights,
 			 double *lnl, double *beta) const;
 	uint32_t num_chains() const { return (uint32_t)chains_.size(); }
+	uint32_t chain_nodes(uint32_t chain) const
+	{
+		return chains_.at(chain)->tree->num_nodes();
+	}
+	uint32_t num_problems() const { return num_problems_; }
+	bool batched() const { return batch_ != nullptr; }
+	// device time of the batched launches so far (ms) and their count
+	double batch_device_ms() const { return batch_ms_; }
+	uint64_t batch_launches() const { return batch_runs_; }
 	// Checkpoint (mcmc_state.cpp): everything later steps depend on, between
 	// steps; load needs a driver built with the same configuration and
 	// data and continues bit for bit as the dumped run would have.
@@ -250,7 +279,10 @@ class Mcmc {
 	void train_surrogate();
 
 	McmcConfig cfg_;
+	uint32_t num_problems_ = 1;
 	std::vector<std::unique_ptr<Chain>> chains_;
+	double batch_ms_ = 0.0;
+	uint64_t batch_runs_ = 0;
 	// FP32 chosen form: every chain's proposal of a step is evaluated by
 	// one graph replay of a batch
 	std::unique_ptr<Batch> batch_;

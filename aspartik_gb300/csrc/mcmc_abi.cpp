@@ -45,6 +45,46 @@ b3g::Mcmc *mcmc_of(b3g_mcmc *m)
 
 extern "C" {
 
+namespace {
+
+b3g::McmcConfig config_of(const b3g_mcmc_config *config)
+{
+	b3g::McmcConfig c{};
+	c.num_chains = config->num_chains;
+	c.num_categories = config->num_categories;
+	c.precision = config->precision;
+	c.model = config->model;
+	c.seed = config->seed;
+	c.heat = config->heat;
+	c.swap_every = config->swap_every;
+	c.sample_every = config->sample_every;
+	c.tune_every = config->tune_every;
+	c.device = config->device;
+	std::memcpy(c.weights, config->op_weights, sizeof(c.weights));
+	if (config->da_reserved != 0)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "da_reserved must be 0");
+	if (config->da_pilot_steps &&
+	    (config->da_hidden < 32 || config->da_hidden % 32 ||
+	     config->da_hidden > 1024 || config->da_epochs < 1))
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+				 "delayed acceptance needs da_hidden a multiple "
+				 "of 32 in 32..1024 and da_epochs >= 1");
+	c.da_pilot_steps = config->da_pilot_steps;
+	c.da_epochs = config->da_epochs;
+	c.da_hidden = config->da_hidden;
+	c.da_drift_limit = config->da_drift_limit;
+	if (config->clock_categories > 64)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+				 "at most 64 relaxed-clock categories");
+	c.clock_categories = config->clock_categories;
+	if (config->launch > B3G_MCMC_LAUNCH_BATCH)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
+	c.launch = config->launch;
+	return c;
+}
+
+} // namespace
+
 B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
 				   uint32_t num_leaves, uint32_t num_patterns,
 				   const uint8_t *samples,
@@ -56,39 +96,41 @@ B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
 		if (!config || !samples || !weights || !parents || !heights || !out)
 			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null argument");
 		*out = nullptr;
-		b3g::McmcConfig c{};
-		c.num_chains = config->num_chains;
-		c.num_categories = config->num_categories;
-		c.precision = config->precision;
-		c.model = config->model;
-		c.seed = config->seed;
-		c.heat = config->heat;
-		c.swap_every = config->swap_every;
-		c.sample_every = config->sample_every;
-		c.tune_every = config->tune_every;
-		c.device = config->device;
-		std::memcpy(c.weights, config->op_weights, sizeof(c.weights));
-		if (config->da_reserved != 0)
-			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "da_reserved must be 0");
-		if (config->da_pilot_steps &&
-		    (config->da_hidden < 32 || config->da_hidden % 32 ||
-		     config->da_hidden > 1024 || config->da_epochs < 1))
-			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
-					 "delayed acceptance needs da_hidden a multiple "
-					 "of 32 in 32..1024 and da_epochs >= 1");
-		c.da_pilot_steps = config->da_pilot_steps;
-		c.da_epochs = config->da_epochs;
-		c.da_hidden = config->da_hidden;
-		c.da_drift_limit = config->da_drift_limit;
-		if (config->clock_reserved != 0)
-			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "clock_reserved must be 0");
-		if (config->clock_categories > 64)
-			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
-					 "at most 64 relaxed-clock categories");
-		c.clock_categories = config->clock_categories;
-		auto *m = new b3g::Mcmc(c, num_leaves, num_patterns, samples,
-					weights, parents, heights);
+		auto *m = new b3g::Mcmc(config_of(config), num_leaves, num_patterns,
+					samples, weights, parents, heights);
 		*out = reinterpret_cast<b3g_mcmc *>(m);
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_create_multi(const b3g_mcmc_config *config,
+					 uint32_t num_problems,
+					 const b3g_mcmc_problem *problems,
+					 b3g_mcmc **out)
+{
+	return guarded([&] {
+		if (!config || !problems || !out || num_problems < 1)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null argument");
+		*out = nullptr;
+		std::vector<b3g::Problem> ps(num_problems);
+		for (uint32_t k = 0; k < num_problems; ++k)
+			ps[k] = b3g::Problem{problems[k].num_leaves, problems[k].num_patterns,
+					     problems[k].samples, problems[k].weights,
+					     problems[k].parents, problems[k].heights};
+		auto *m = new b3g::Mcmc(config_of(config), ps);
+		*out = reinterpret_cast<b3g_mcmc *>(m);
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_launch_stats(b3g_mcmc *mcmc, uint32_t *batched,
+					 double *device_ms, uint64_t *launches)
+{
+	return guarded([&] {
+		if (!batched || !device_ms || !launches)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null output");
+		const b3g::Mcmc *m = mcmc_of(mcmc);
+		*batched = m->batched() ? 1u : 0u;
+		*device_ms = m->batch_device_ms();
+		*launches = m->batch_launches();
 	});
 }
 

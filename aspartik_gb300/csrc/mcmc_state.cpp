@@ -13,7 +13,7 @@
 //   u64 swap RNG state[4]
 //   per operator: u64 accepts, rejects, aborts, prior rejects, window
 //   accepts, window rejects; f64 tuning
-//   per chain: u32 index, run-walk tile, run-walk block, reserved; f64 beta,
+//   per chain: u32 index, run-walk tile, run-walk block, leaves; f64 beta,
 //   lnL, prior, kappa, alpha, birth rate, clock sd; u32 n, f64 rates[n];
 //   u32 n, f64 frequencies[n]; u64 RNG state[4]; u32 parents[2L-1];
 //   u32 children[2L-2] (each internal's children in the order the
@@ -120,7 +120,7 @@ std::vector<uint8_t> Mcmc::dump() const
 	for (const auto &chp : chains_) {
 		const Chain &ch = *chp;
 		const uint32_t h[4] = {ch.index, ch.calc->runs_tile(),
-				       ch.calc->runs_block(), 0u};
+				       ch.calc->runs_block(), ch.tree->num_leaves()};
 		w.put_n(h, 4);
 		const double v[7] = {ch.beta,       ch.lnl_cache, ch.prior_cache,
 				     ch.kappa.v,    ch.alpha.v,   ch.birth_rate.v,
@@ -164,7 +164,7 @@ void Mcmc::load(const uint8_t *state, size_t size)
 	if (head[0] != kVersion)
 		throw Error(B3G_ERR_INVALID_ARGUMENT,
 			    "unknown checkpoint version " + std::to_string(head[0]));
-	const uint32_t L = chains_[0]->tree->num_leaves(), nodes = 2 * L - 1;
+	const uint32_t L = chains_[0]->tree->num_leaves();
 	if (head[1] != chains_.size() || head[2] != L || head[3] != cfg_.model ||
 	    head[4] != cfg_.num_categories || head[5] != cfg_.clock_categories ||
 	    head[6] != cfg_.precision)
@@ -200,8 +200,13 @@ void Mcmc::load(const uint8_t *state, size_t size)
 		std::unique_ptr<DatedTree> tree;
 	};
 	std::vector<Saved> saved(chains_.size());
-	for (Saved &sv : saved) {
+	for (size_t i = 0; i < saved.size(); ++i) {
+		Saved &sv = saved[i];
+		const uint32_t nodes = chains_[i]->tree->num_nodes();
 		r.get_n(sv.h, 4);
+		if (sv.h[3] != chains_[i]->tree->num_leaves())
+			throw Error(B3G_ERR_INVALID_ARGUMENT,
+				    "checkpoint of a different alignment (leaves)");
 		r.get_n(sv.v, 7);
 		uint32_t n = r.get<uint32_t>();
 		if (n > 6)

@@ -601,23 +601,141 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 constexpr uint32_t kDirectAhead = 4;
 
 template <typename Idx>
-__device__ __forceinline__ void direct_fetch(const DirectParams &prm, uint32_t i,
+__device__ __forceinline__ void direct_fetch(const NodeOp *ops, const uint8_t (*src)[2],
+					     uint32_t i, uint32_t ldp,
 					     const float4 *part, const int32_t *scales,
 					     const uint8_t *tips_p, Idx stride, Idx col_off,
 					     float4 (&v)[2], int32_t (&s)[2])
 {
-	const NodeOp &op = prm.ops[i];
+	const NodeOp &op = ops[i];
 	const uint32_t ids[2] = {op.left, op.right};
 #pragma unroll
 	for (int j = 0; j < 2; ++j) {
-		const uint32_t src = prm.src[i][j];
-		if (src == kSrcTip) {
-			s[j] = tips_p[(size_t)(ids[j] & ~kTipBit) * prm.ldp];
-		} else if (src == kSrcClean) {
+		const uint32_t sr = src[i][j];
+		if (sr == kSrcTip) {
+			s[j] = tips_p[(size_t)(ids[j] & ~kTipBit) * ldp];
+		} else if (sr == kSrcClean) {
 			const Idx ix = (Idx)ids[j] * stride + col_off;
 			v[j] = part[ix];
 			s[j] = scales[ix];
 		}
+	}
+}
+
+// The first kDirectAhead entries' clean inputs of tile t for this thread's
+// column (c, pl).
+template <typename Idx, uint32_t kC>
+__device__ __forceinline__ void direct_prefetch(const NodeOp *ops, const uint8_t (*src)[2],
+						uint32_t n, uint32_t ldp, const uint8_t *tips,
+						const float4 *part, const int32_t *scales,
+						uint32_t t, float4 (&pv)[kDirectAhead][2],
+						int32_t (&ps)[kDirectAhead][2])
+{
+	constexpr uint32_t kTile = 128;
+	const uint32_t c = threadIdx.x / kTile, pl = threadIdx.x - c * kTile;
+	const Idx stride = (Idx)kC * ldp;
+	const Idx col_off = (Idx)c * ldp + t * kTile + pl;
+	const uint8_t *tips_p = tips + t * kTile + pl;
+#pragma unroll
+	for (uint32_t u = 0; u < kDirectAhead; ++u)
+		if (u < n)
+			direct_fetch<Idx>(ops, src, u, ldp, part, scales, tips_p, stride,
+					  col_off, pv[u], ps[u]);
+}
+
+// The serial walk of tile t (one thread per column) after direct_prefetch:
+// leaves pi . x and the exponent of the root in s_dot / s_cnt (not
+// synchronised).
+template <typename Idx, uint32_t kC>
+__device__ __forceinline__ void direct_walk(const NodeOp *ops, const uint8_t (*src)[2],
+					    uint32_t n, uint32_t ldp, const uint8_t *tips,
+					    float4 *part, int32_t *scales, const float4 *s_tab,
+					    const float *s_pi, uint32_t t, float *s_dot,
+					    int32_t *s_cnt, float4 (&pv)[kDirectAhead][2],
+					    int32_t (&ps)[kDirectAhead][2])
+{
+	constexpr uint32_t kTile = 128;
+	const uint32_t tid = threadIdx.x;
+	const uint32_t c = tid / kTile, pl = tid - c * kTile;
+	const Idx stride = (Idx)kC * ldp;
+	const Idx col_off = (Idx)c * ldp + t * kTile + pl;
+	const uint8_t *tips_p = tips + t * kTile + pl;
+	float4 y0 = make_float4(0.f, 0.f, 0.f, 0.f), y1 = y0;
+	int32_t c0 = 0, c1 = 0;
+	for (uint32_t i0 = 0; i0 < n; i0 += kDirectAhead) {
+#pragma unroll
+		for (uint32_t u = 0; u < kDirectAhead; ++u) {
+			const uint32_t i = i0 + u;
+			if (i < n) {
+				const NodeOp op = ops[i];
+				const float4 *tl = s_tab + ((size_t)(2 * i) * kC + c) * 5;
+				const float4 *tr = tl + 5 * kC;
+				float4 in[2];
+				int32_t sc[2];
+				const uint32_t ids[2] = {op.left, op.right};
+#pragma unroll
+				for (int j = 0; j < 2; ++j) {
+					const float4 *tb = j ? tr : tl;
+					const uint32_t sr = src[i][j];
+					if (sr == kSrcTip) {
+						in[j] = tb[ps[u][j]];
+						sc[j] = 0;
+					} else if (sr == kSrcClean) {
+						in[j] = v4_apply(tb, pv[u][j]);
+						sc[j] = ps[u][j];
+					} else if (sr == kSrcPrev) {
+						in[j] = v4_apply(tb, y0);
+						sc[j] = c0;
+					} else if (sr == kSrcPrev2) {
+						in[j] = v4_apply(tb, y1);
+						sc[j] = c1;
+					} else {
+						const Idx ix = (Idx)ids[j] * stride + col_off;
+						in[j] = v4_apply(tb, part[ix]);
+						sc[j] = scales[ix];
+					}
+				}
+				// the slot just consumed takes entry i + ahead
+				if (i + kDirectAhead < n)
+					direct_fetch<Idx>(ops, src, i + kDirectAhead, ldp, part,
+							  scales, tips_p, stride, col_off, pv[u],
+							  ps[u]);
+				float4 y = v4_mul(in[0], in[1]);
+				const int32_t cnt = sc[0] + sc[1] + rescale_pow2(y);
+				const Idx ox = (Idx)op.out * stride + col_off;
+				part[ox] = y;
+				scales[ox] = cnt;
+				y1 = y0;
+				c1 = c0;
+				y0 = y;
+				c0 = cnt;
+			}
+		}
+	}
+	s_dot[tid] = root_dot4(s_pi, y0);
+	s_cnt[tid] = c0;
+}
+
+// The list's transition tables (entry, side, category) in shared memory,
+// laid out as ptab4_kernel's, from the FP32 eigensystem in s_eig and the
+// scaled category rates in s_rate (same arithmetic as the transition
+// kernels).
+template <uint32_t kC>
+__device__ __forceinline__ void direct_tables(const ModelDev *m, const float *s_eig,
+					      const double *s_rate, const double *lengths,
+					      uint32_t n, float4 *s_tab)
+{
+	const uint32_t tid = threadIdx.x;
+	if (tid < n * 2 * kC) {
+		const uint32_t cc = tid % kC, es = tid / kC;
+		float P[16];
+		transition4f_eig(m, s_eig, lengths[es] * s_rate[cc], P);
+		float *out = reinterpret_cast<float *>(s_tab + tid * 5);
+		for (int k = 0; k < 4; k++)
+			for (int j = 0; j < 4; j++)
+				out[k * 4 + j] = P[j * 4 + k];
+		for (int j = 0; j < 4; j++)
+			out[16 + j] = 1.0f;
 	}
 }
 
@@ -635,29 +753,17 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	__shared__ double s_red[32];
 	__shared__ unsigned s_last;
 	const uint32_t tid = threadIdx.x;
-	const ModelDev *m = prm.model;
 	const uint32_t n = prm.n;
 	const uint32_t ntiles = prm.ldp / kTile;
-	// this thread's column
-	const uint32_t c = tid / kTile, pl = tid - c * kTile;
-	const Idx stride = (Idx)kC * prm.ldp;
-	const float4 *part = (const float4 *)prm.partials;
-	float4 *part_w = (float4 *)prm.partials;
+	float4 *part = (float4 *)prm.partials;
 
 	// clean inputs of the first entries of the first tile, in flight while
 	// the tables are built
 	float4 pv[kDirectAhead][2];
 	int32_t ps[kDirectAhead][2];
-	uint32_t t = blockIdx.x;
-	if (t < ntiles) {
-		const Idx col_off = (Idx)c * prm.ldp + t * kTile + pl;
-		const uint8_t *tips_p = prm.tips + t * kTile + pl;
-#pragma unroll
-		for (uint32_t u = 0; u < kDirectAhead; ++u)
-			if (u < n)
-				direct_fetch<Idx>(prm, u, part, prm.scales, tips_p, stride,
-						  col_off, pv[u], ps[u]);
-	}
+	if (blockIdx.x < ntiles)
+		direct_prefetch<Idx, kC>(prm.ops, prm.src, n, prm.ldp, prm.tips, part,
+					 prm.scales, blockIdx.x, pv, ps);
 	// from the parameters: no global-memory round trip before the tables
 	if (tid < 37)
 		s_eig[tid] = prm.eig[tid];
@@ -666,102 +772,24 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	else if (tid >= 64 && tid < 68)
 		s_pi[tid - 64] = (float)prm.pi[tid - 64];
 	__syncthreads();
-	if (tid < n * 2 * kC) {
-		// table (entry, side, category), laid out as ptab4_kernel's
-		const uint32_t cc = tid % kC, es = tid / kC;
-		float P[16];
-		transition4f_eig(m, s_eig, prm.lengths[es] * s_rate[cc], P);
-		float *out = reinterpret_cast<float *>(s_tab + tid * 5);
-		for (int k = 0; k < 4; k++)
-			for (int j = 0; j < 4; j++)
-				out[k * 4 + j] = P[j * 4 + k];
-		for (int j = 0; j < 4; j++)
-			out[16 + j] = 1.0f;
-	}
+	direct_tables<kC>(prm.model, s_eig, s_rate, prm.lengths, n, s_tab);
 	__syncthreads();
 
-	TileArgs a;
-	a.tips = prm.tips;
-	a.part = part_w;
-	a.scales = prm.scales;
-	a.ptab = s_tab;
+	TileArgs a{};
 	a.pi = prm.pi;
 	a.weights = prm.weights;
 	a.site_lnl = prm.site_lnl;
 	a.cat_lnl = nullptr;
-	a.ldp = prm.ldp;
 	a.C = kC;
-	a.L = prm.L;
 	a.tile = kTile;
-	a.n = n;
-	a.n_runs = 0;
-	a.tips_smem = 0;
 	a.log_inv_c = prm.log_inv_c;
 	double cta_sum = 0.0, cta_comp = 0.0; // thread 0: this block's tiles
-	for (; t < ntiles; t += gridDim.x) {
-		const Idx col_off = (Idx)c * prm.ldp + t * kTile + pl;
-		const uint8_t *tips_p = prm.tips + t * kTile + pl;
-		if (t != blockIdx.x) {
-#pragma unroll
-			for (uint32_t u = 0; u < kDirectAhead; ++u)
-				if (u < n)
-					direct_fetch<Idx>(prm, u, part, prm.scales, tips_p,
-							  stride, col_off, pv[u], ps[u]);
-		}
-		float4 y0 = make_float4(0.f, 0.f, 0.f, 0.f), y1 = y0;
-		int32_t c0 = 0, c1 = 0;
-		for (uint32_t i0 = 0; i0 < n; i0 += kDirectAhead) {
-#pragma unroll
-			for (uint32_t u = 0; u < kDirectAhead; ++u) {
-				const uint32_t i = i0 + u;
-				if (i < n) {
-					const NodeOp op = prm.ops[i];
-					const float4 *tl = s_tab + ((size_t)(2 * i) * kC + c) * 5;
-					const float4 *tr = tl + 5 * kC;
-					float4 in[2];
-					int32_t sc[2];
-					const uint32_t ids[2] = {op.left, op.right};
-#pragma unroll
-					for (int j = 0; j < 2; ++j) {
-						const float4 *tb = j ? tr : tl;
-						const uint32_t src = prm.src[i][j];
-						if (src == kSrcTip) {
-							in[j] = tb[ps[u][j]];
-							sc[j] = 0;
-						} else if (src == kSrcClean) {
-							in[j] = v4_apply(tb, pv[u][j]);
-							sc[j] = ps[u][j];
-						} else if (src == kSrcPrev) {
-							in[j] = v4_apply(tb, y0);
-							sc[j] = c0;
-						} else if (src == kSrcPrev2) {
-							in[j] = v4_apply(tb, y1);
-							sc[j] = c1;
-						} else {
-							const Idx ix = (Idx)ids[j] * stride + col_off;
-							in[j] = v4_apply(tb, part[ix]);
-							sc[j] = prm.scales[ix];
-						}
-					}
-					// the slot just consumed takes entry i + ahead
-					if (i + kDirectAhead < n)
-						direct_fetch<Idx>(prm, i + kDirectAhead, part,
-								  prm.scales, tips_p, stride, col_off,
-								  pv[u], ps[u]);
-					float4 y = v4_mul(in[0], in[1]);
-					const int32_t cnt = sc[0] + sc[1] + rescale_pow2(y);
-					const Idx ox = (Idx)op.out * stride + col_off;
-					part_w[ox] = y;
-					prm.scales[ox] = cnt;
-					y1 = y0;
-					c1 = c0;
-					y0 = y;
-					c0 = cnt;
-				}
-			}
-		}
-		s_dot[tid] = root_dot4(s_pi, y0);
-		s_cnt[tid] = c0;
+	for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		if (t != blockIdx.x)
+			direct_prefetch<Idx, kC>(prm.ops, prm.src, n, prm.ldp, prm.tips,
+						 part, prm.scales, t, pv, ps);
+		direct_walk<Idx, kC>(prm.ops, prm.src, n, prm.ldp, prm.tips, part,
+				     prm.scales, s_tab, s_pi, t, s_dot, s_cnt, pv, ps);
 		__syncthreads();
 		const double tsum = tile_root(a, t, s_dot, s_cnt, s_red);
 		if (tid == 0)
@@ -786,6 +814,164 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 	}
 }
 
+// Batched short lists: persistent blocks take (member, 128-pattern tile)
+// items of the members whose step is direct and has kC categories from
+// their own counter (work_next[1], [2], [3] for 4, 2, 1 categories;
+// costliest member first); a block that moves to another
+// member copies its list, classifies every child's source, converts the
+// member's eigensystem to FP32 and builds the list's tables (as the
+// single-calculator kernel does, so values match it), then walks the tile
+// serially with clean inputs loaded four entries ahead.  Each tile's
+// weighted sum goes to the member's tile slot; the block finishing a
+// member's last tile folds its sums (fixed order).
+template <typename Idx, uint32_t kC>
+__global__ void __launch_bounds__(128 * kC, 4 / kC)
+prune4_direct_batch_kernel(BatchParams bp)
+{
+	constexpr uint32_t kTile = 128, kCols = kTile * kC;
+	constexpr uint32_t kMaxMembers = 256;
+	__shared__ float4 s_tab[kDirectMax * 2 * kC * 5];
+	__shared__ NodeOp s_ops[kDirectMax];
+	__shared__ uint8_t s_src[kDirectMax][2];
+	__shared__ float s_eig[37];
+	__shared__ double s_rate[kC];
+	__shared__ float s_pi[4];
+	__shared__ float s_dot[kCols];
+	__shared__ int32_t s_cnt[kCols];
+	__shared__ double s_red[32];
+	__shared__ uint32_t s_prefix[kMaxMembers + 1];
+	__shared__ uint32_t s_work;
+	__shared__ unsigned s_last;
+	const uint32_t tid = threadIdx.x;
+	const uint32_t M = bp.num_members;
+	if (tid == 0) {
+		uint32_t acc = 0;
+		for (uint32_t m = 0; m < M; ++m) {
+			s_prefix[m] = acc;
+			const MemberStep &st = bp.steps[m];
+			if (st.n && st.direct && bp.members[m].C == kC)
+				acc += bp.members[m].ldp / kTile;
+		}
+		s_prefix[M] = acc;
+	}
+	__syncthreads();
+	const uint32_t total = s_prefix[M];
+	uint32_t cur = 0xFFFFFFFFu, n = 0;
+	const MemberDesc *md = nullptr;
+	TileArgs a{};
+	a.C = kC;
+	a.tile = kTile;
+	a.cat_lnl = nullptr;
+	float4 pv[kDirectAhead][2];
+	int32_t ps[kDirectAhead][2];
+	for (;;) {
+		if (tid == 0)
+			s_work = atomicAdd(bp.work_next + (kC == 4 ? 1 : kC == 2 ? 2 : 3), 1u);
+		__syncthreads();
+		const uint32_t w = s_work;
+		__syncthreads();
+		if (w >= total)
+			break;
+		uint32_t lo = 0, hi = M;
+		while (hi - lo > 1) {
+			const uint32_t mid = (lo + hi) >> 1;
+			if (s_prefix[mid] <= w)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		while (lo + 1 < M && s_prefix[lo + 1] <= w)
+			++lo;
+		const uint32_t m = lo, t = w - s_prefix[m];
+		md = &bp.members[m];
+		if (m != cur) {
+			const MemberStep st = bp.steps[m];
+			n = st.n;
+			const NodeOp *g_ops = (const NodeOp *)md->stage;
+			for (uint32_t k = tid; k < n; k += blockDim.x)
+				s_ops[k] = g_ops[k];
+			const ModelDev *mod = md->model;
+			if (tid < 16) {
+				s_eig[tid] = (float)mod->V[tid];
+				s_eig[16 + tid] = (float)mod->Vinv[tid];
+			} else if (tid < 20) {
+				s_eig[32 + tid - 16] = (float)mod->lambda[tid - 16];
+			} else if (tid == 20) {
+				s_eig[36] = mod->shortcuts ? 1.0f : 0.0f;
+			} else if (tid >= 32 && tid < 32 + kC) {
+				s_rate[tid - 32] = st.clock_rate * mod->cat_rates[tid - 32];
+			} else if (tid >= 64 && tid < 68) {
+				s_pi[tid - 64] =
+					(float)((const double *)(md->stage + md->off_pi))[tid - 64];
+			}
+			__syncthreads();
+			// where each child comes from (as the host classifies it for
+			// the single-calculator kernel)
+			if (tid < n) {
+				const NodeOp op = s_ops[tid];
+				const uint32_t ids[2] = {op.left, op.right};
+				for (int j = 0; j < 2; ++j) {
+					const uint32_t id = ids[j];
+					uint8_t sr = kSrcClean;
+					if (id & kTipBit) {
+						sr = kSrcTip;
+					} else if (tid >= 1 && id == s_ops[tid - 1].out) {
+						sr = kSrcPrev;
+					} else if (tid >= 2 && id == s_ops[tid - 2].out) {
+						sr = kSrcPrev2;
+					} else {
+						for (uint32_t k = 0; k + 2 < tid; ++k)
+							if (s_ops[k].out == id) {
+								sr = kSrcEarlier;
+								break;
+							}
+					}
+					s_src[tid][j] = sr;
+				}
+			}
+			__syncthreads();
+			a.pi = (const double *)(md->stage + md->off_pi);
+			a.weights = md->weights;
+			a.site_lnl = md->site_lnl;
+			a.ldp = md->ldp;
+			a.log_inv_c = md->log_inv_c;
+			direct_prefetch<Idx, kC>(s_ops, s_src, n, md->ldp, md->tips,
+						 (const float4 *)md->partials, md->scales, t, pv,
+						 ps);
+			direct_tables<kC>(mod, s_eig, s_rate,
+					  (const double *)(md->stage + md->off_in), n, s_tab);
+			cur = m;
+			__syncthreads();
+		} else {
+			direct_prefetch<Idx, kC>(s_ops, s_src, n, md->ldp, md->tips,
+						 (const float4 *)md->partials, md->scales, t, pv,
+						 ps);
+		}
+		direct_walk<Idx, kC>(s_ops, s_src, n, md->ldp, md->tips,
+				     (float4 *)md->partials, md->scales, s_tab, s_pi, t,
+				     s_dot, s_cnt, pv, ps);
+		__syncthreads();
+		const double tsum = tile_root(a, t, s_dot, s_cnt, s_red);
+		const uint32_t tiles = md->ldp / kTile;
+		if (tid == 0) {
+			md->tile_sums[t] = tsum;
+			__threadfence();
+			const unsigned tk = atomicAdd(md->ticket, 1u);
+			s_last = (tk == tiles - 1u);
+		}
+		__syncthreads();
+		if (s_last) {
+			__threadfence();
+			const double lnl = block_fold(md->tile_sums, tiles, s_red);
+			if (tid == 0) {
+				bp.lnl_out[m] = lnl;
+				*md->ticket = 0u;
+			}
+		}
+		__syncthreads();
+	}
+}
+
 // ---------------------------------------------------------------------------
 // Batched evaluation: many calculators (chains) in one launch.
 
@@ -793,7 +979,7 @@ __global__ void __launch_bounds__(32) ptab4_batch_kernel(BatchParams bp)
 {
 	const uint32_t m = blockIdx.y;
 	const MemberStep st = bp.steps[m];
-	if (st.n == 0)
+	if (st.n == 0 || st.direct)
 		return;
 	const MemberDesc &md = bp.members[m];
 	const uint32_t C = md.C;
@@ -840,7 +1026,7 @@ __global__ void __launch_bounds__(512, 2) prune4_batch_kernel(BatchParams bp)
 		uint32_t acc = 0;
 		for (uint32_t m = 0; m < M; ++m) {
 			s_prefix[m] = acc;
-			if (bp.steps[m].n)
+			if (bp.steps[m].n && !bp.steps[m].direct)
 				acc += bp.members[m].ldp / bp.steps[m].tile;
 		}
 		s_prefix[M] = acc;

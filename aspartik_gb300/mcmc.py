@@ -57,6 +57,27 @@ class McmcSettings:
     da_drift_limit: float = 0.0
     # relaxed clock: rate categories per edge (0: strict clock)
     clock_categories: int = 0
+    # "streams": one launch per chain on its own stream; "batch": every
+    # chain of a step in one graph-replayed batched launch (FP32)
+    launch: str = "streams"
+
+
+LAUNCH = {"streams": 0, "batch": 1}
+
+
+def _config(settings: McmcSettings) -> "nat.McmcConfig":
+    w = np.zeros(nat.OP_COUNT)
+    for name, val in settings.weights.items():
+        w[OPERATORS.index(name)] = val
+    return nat.McmcConfig(settings.num_chains, settings.num_categories,
+                          nat.PRECISION_F64 if settings.precision == "f64"
+                          else nat.PRECISION_F32,
+                          MODELS[settings.model], settings.seed, settings.heat,
+                          settings.swap_every, settings.sample_every, settings.tune_every,
+                          settings.device, (ct.c_double * nat.OP_COUNT)(*w),
+                          settings.da_pilot_steps, settings.da_epochs, settings.da_hidden,
+                          0, settings.da_drift_limit, settings.clock_categories,
+                          LAUNCH[settings.launch])
 
 
 class Mcmc:
@@ -64,17 +85,7 @@ class Mcmc:
                  heights: np.ndarray, settings: McmcSettings):
         leaves = nat.u8(leaves)
         L, P = leaves.shape
-        w = np.zeros(nat.OP_COUNT)
-        for name, val in settings.weights.items():
-            w[OPERATORS.index(name)] = val
-        cfg = nat.McmcConfig(settings.num_chains, settings.num_categories,
-                             nat.PRECISION_F64 if settings.precision == "f64"
-                             else nat.PRECISION_F32,
-                             MODELS[settings.model], settings.seed, settings.heat,
-                             settings.swap_every, settings.sample_every, settings.tune_every,
-                             settings.device, (ct.c_double * nat.OP_COUNT)(*w),
-                             settings.da_pilot_steps, settings.da_epochs, settings.da_hidden,
-                             0, settings.da_drift_limit, settings.clock_categories, 0)
+        cfg = _config(settings)
         self._wts = nat.u32(weights)
         self._par = nat.u32(parents)
         self._hei = nat.f64(heights)
@@ -86,6 +97,40 @@ class Mcmc:
         self._h = h
         self.settings = settings
         self.num_nodes = self._par.size
+        self.chain_nodes = [self.num_nodes] * settings.num_chains
+
+    @classmethod
+    def multi(cls, problems, settings: McmcSettings) -> "Mcmc":
+        """Chains over several alignments (b3g_mcmc_create_multi):
+        `problems` is a list of (leaves, weights, parents, heights);
+        settings.num_chains / len(problems) chains per problem form that
+        problem's temperature ladder (MC3 swaps within a problem only)."""
+        self = cls.__new__(cls)
+        self._keep = []
+        arr = (nat.McmcProblem * len(problems))()
+        for k, (leaves, weights, parents, heights) in enumerate(problems):
+            lv, wt = nat.u8(leaves), nat.u32(weights)
+            pa, he = nat.u32(parents), nat.f64(heights)
+            self._keep += [lv, wt, pa, he]
+            arr[k] = nat.McmcProblem(lv.shape[0], lv.shape[1], lv.ctypes.data,
+                                     wt.ctypes.data, pa.ctypes.data, he.ctypes.data)
+        h = ct.c_void_p()
+        check(lib.b3g_mcmc_create_multi(ct.byref(_config(settings)), len(problems), arr,
+                                        ct.byref(h)))
+        self._h = h
+        self.settings = settings
+        group = settings.num_chains // len(problems)
+        sizes = [nat.u32(p[2]).size for p in problems]
+        self.chain_nodes = [sizes[i // group] for i in range(settings.num_chains)]
+        self.num_nodes = sizes[0]
+        return self
+
+    def launch_stats(self) -> dict:
+        """{"batched": launch mode is the batched graph, "device_ms": device
+        time of its replays so far, "launches": their count}."""
+        b, ms, n = ct.c_uint32(), ct.c_double(), ct.c_uint64()
+        check(lib.b3g_mcmc_launch_stats(self._h, ct.byref(b), ct.byref(ms), ct.byref(n)))
+        return {"batched": bool(b.value), "device_ms": ms.value, "launches": n.value}
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -207,8 +252,8 @@ class Mcmc:
         return out.value
 
     def chain_state(self, chain: int):
-        parents = np.zeros(self.num_nodes, dtype=np.uint32)
-        heights = np.zeros(self.num_nodes)
+        parents = np.zeros(self.chain_nodes[chain], dtype=np.uint32)
+        heights = np.zeros(self.chain_nodes[chain])
         lnl, beta = ct.c_double(), ct.c_double()
         check(lib.b3g_mcmc_chain_state(self._h, chain, nat.as_ptr(parents, ct.c_uint32),
                                        nat.as_ptr(heights, ct.c_double), ct.byref(lnl),

@@ -377,8 +377,26 @@ typedef struct b3g_mcmc_config {
 	 * log-scale sd (prior Exponential, mean 1/3).  A category change
 	 * marks only its edge for recomputation, an sd change every edge. */
 	uint32_t clock_categories;
-	uint32_t clock_reserved; /* must be 0 */
+	/* B3G_MCMC_LAUNCH_STREAMS (0): each chain launches its own evaluations
+	 * on its own stream and a step's launches run concurrently;
+	 * B3G_MCMC_LAUNCH_BATCH (1, FP32 chosen form, several chains): every
+	 * chain's evaluation of a step in one replay of a captured CUDA graph
+	 * (b3g_batch_*: one staging copy, one persistent launch for the
+	 * members' short lists, one for the long ones, one read-back). */
+	uint32_t launch;
 } b3g_mcmc_config;
+
+enum { B3G_MCMC_LAUNCH_STREAMS = 0, B3G_MCMC_LAUNCH_BATCH = 1 };
+
+/* One alignment of a driver over several (b3g_mcmc_create_multi). */
+typedef struct b3g_mcmc_problem {
+	uint32_t num_leaves;
+	uint32_t num_patterns;
+	const uint8_t *samples;  /* [num_leaves][num_patterns] */
+	const uint32_t *weights; /* [num_patterns] */
+	const uint32_t *parents; /* [2 num_leaves - 1], root 0xFFFFFFFF */
+	const double *heights;   /* [2 num_leaves - 1] */
+} b3g_mcmc_problem;
 
 /* parents[2L-1] (root: 0xFFFFFFFF) and heights[2L-1] give the start tree of
  * every chain; samples/weights as for b3g_calculator_create/_set_weights. */
@@ -388,6 +406,20 @@ B3G_API b3g_status b3g_mcmc_create(const b3g_mcmc_config *config,
 				   const uint32_t *weights,
 				   const uint32_t *parents,
 				   const double *heights, b3g_mcmc **out);
+/* Chains over several alignments (no counterpart in the reference, whose
+ * Mcmc holds one likelihood): num_chains / num_problems chains per problem;
+ * chain i runs problem i / that count at temperature index i % that count,
+ * beta = 1 / (1 + heat * index), and MC3 swaps pair chains of one problem
+ * only.  Delayed acceptance needs a single problem; traces and samples of
+ * the cold chain are problem 0's, b3g_mcmc_chain_trace gives every chain. */
+B3G_API b3g_status b3g_mcmc_create_multi(const b3g_mcmc_config *config,
+					 uint32_t num_problems,
+					 const b3g_mcmc_problem *problems,
+					 b3g_mcmc **out);
+/* Launch mode in use (1: batched graph) and, when batched, the device time
+ * of all replays so far (ms) and their count. */
+B3G_API b3g_status b3g_mcmc_launch_stats(b3g_mcmc *mcmc, uint32_t *batched,
+					 double *device_ms, uint64_t *launches);
 B3G_API void b3g_mcmc_destroy(b3g_mcmc *mcmc);
 /* Start values (rates/frequencies may be NULL to keep the defaults). */
 B3G_API b3g_status b3g_mcmc_set_parameters(b3g_mcmc *mcmc, double kappa,
