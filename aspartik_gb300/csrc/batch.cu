@@ -59,6 +59,10 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 	try {
 		check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking),
 			   "stream");
+		check_cuda(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking),
+			   "stream");
+		check_cuda(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming), "event");
+		check_cuda(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming), "event");
 		check_cuda(cudaEventCreate(&ev0_), "event");
 		check_cuda(cudaEventCreate(&ev1_), "event");
 		check_cuda(cudaMalloc(&d_desc_, sizeof(MemberDesc) * M), "descriptors");
@@ -174,6 +178,10 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 			   "staging block copy");
 		check_cuda(cudaMemsetAsync(d_work_, 0, 4 * sizeof(unsigned), stream_),
 			   "work counters");
+		// two branches: the run walk of long lists on this stream, the
+		// short-list kernels on the second, joined before the read-back
+		check_cuda(cudaEventRecord(ev_fork_, stream_), "fork");
+		check_cuda(cudaStreamWaitEvent(stream2_, ev_fork_, 0), "fork");
 		check_cuda(launch_ptab4_batch(bp_, max_entries_, stream_),
 			   "batched transition kernel");
 		check_cuda(launch_prune4_batch(bp_, ctas_, stream_),
@@ -181,8 +189,10 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		for (uint32_t C : {4u, 2u, 1u})
 			if (direct_c_[C])
 				check_cuda(launch_prune4_direct_batch(
-						   bp_, C, (4u / C) * members_[0]->num_sms_, stream_),
+						   bp_, C, (4u / C) * members_[0]->num_sms_, stream2_),
 					   "batched short-list kernel");
+		check_cuda(cudaEventRecord(ev_join_, stream2_), "join");
+		check_cuda(cudaStreamWaitEvent(stream_, ev_join_, 0), "join");
 		check_cuda(cudaMemcpyAsync(h_lnl_, d_lnl_, sizeof(double) * M,
 					   cudaMemcpyDeviceToHost, stream_),
 			   "lnl copy");
@@ -245,8 +255,16 @@ void Batch::release()
 		cudaEventDestroy(ev0_);
 	if (ev1_)
 		cudaEventDestroy(ev1_);
+	if (ev_fork_)
+		cudaEventDestroy(ev_fork_);
+	if (ev_join_)
+		cudaEventDestroy(ev_join_);
 	if (stream_)
 		cudaStreamDestroy(stream_);
+	if (stream2_)
+		cudaStreamDestroy(stream2_);
+	ev_fork_ = ev_join_ = nullptr;
+	stream2_ = nullptr;
 	exec_ = nullptr;
 	graph_ = nullptr;
 	d_desc_ = nullptr;
@@ -272,7 +290,7 @@ void Batch::run()
 		evaluated_[order_[k]] = c->staged_ ? 1 : 0;
 		if (c->staged_) {
 			// the member's own last launch must not still read its tables
-			check_cuda(cudaEventSynchronize(c->ev_stage_free_), "member stage");
+			c->wait_stage();
 			s.n = c->staged_n_;
 			s.n_runs = c->n_runs_;
 			s.tile = c->staged_tile_;

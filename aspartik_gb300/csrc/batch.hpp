@@ -26,6 +26,8 @@ class Batch {
 	std::vector<uint32_t> order_; // members by cost, descending
 	int device_ = -1;
 	cudaStream_t stream_ = nullptr;
+	cudaStream_t stream2_ = nullptr; // the graph's short-list branch
+	cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
 	cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
 	MemberDesc *d_desc_ = nullptr;
 	MemberStep *d_steps_ = nullptr, *h_steps_ = nullptr;

@@ -864,14 +864,18 @@ prune4_direct_batch_kernel(BatchParams bp)
 	a.cat_lnl = nullptr;
 	float4 pv[kDirectAhead][2];
 	int32_t ps[kDirectAhead][2];
+	// items come in chunks of consecutive tiles (mostly of one member), so
+	// that a block rebuilds a member's tables less often
+	constexpr uint32_t kChunk = 4;
 	for (;;) {
 		if (tid == 0)
-			s_work = atomicAdd(bp.work_next + (kC == 4 ? 1 : kC == 2 ? 2 : 3), 1u);
+			s_work = atomicAdd(bp.work_next + (kC == 4 ? 1 : kC == 2 ? 2 : 3), kChunk);
 		__syncthreads();
-		const uint32_t w = s_work;
+		const uint32_t w0 = s_work;
 		__syncthreads();
-		if (w >= total)
+		if (w0 >= total)
 			break;
+	for (uint32_t w = w0; w < min(w0 + kChunk, total); ++w) {
 		uint32_t lo = 0, hi = M;
 		while (hi - lo > 1) {
 			const uint32_t mid = (lo + hi) >> 1;
@@ -969,6 +973,7 @@ prune4_direct_batch_kernel(BatchParams bp)
 			}
 		}
 		__syncthreads();
+	}
 	}
 }
 

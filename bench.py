@@ -612,6 +612,82 @@ def config_block(name: str, device: int, mcmc_steps: int, reps: int = 50) -> dic
     return out
 
 
+def c4_problems(seed: int = 4, problems: int = 4) -> list:
+    """The batched configuration's alignments: taxa uniform on 24..200, sites
+    log-uniform on 500..50,000, each simulated under GTR + Gamma4 as the
+    64-taxon configuration (exchangeabilities ~ Gamma(2, 1), frequencies ~
+    Dirichlet(5, 5, 5, 5), alpha 0.5) down a Yule tree of root height 1."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(problems):
+        L = int(rng.integers(24, 201))
+        N = int(np.exp(rng.uniform(np.log(500), np.log(50000))))
+        tree = sim.yule_tree(L, rng, root_height=1.0)
+        pi = sim.dirichlet([5.0] * 4, rng)
+        rates = rng.gamma(2.0, 1.0, size=6)
+        states = sim.simulate_alignment(tree, N, sim.reversible_q(rates, pi), pi, rng,
+                                        cat_rates=sim.gamma_rates(0.5, 4))
+        leaves, weights, _ = sim.deduplicate(sim.to_dna_codes(states))
+        out.append(dict(taxa=L, sites=N, patterns=int(leaves.shape[1]), leaves=leaves,
+                        weights=weights, tree=tree))
+    return out
+
+
+def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
+    """The batched configuration as an MCMC: 4 alignments (c4_problems) x 8
+    MC3 temperatures, beta_i = 1 / (1 + 0.1 i), = 32 FP32 chains of uneven
+    taxa and sites in one driver (b3g_mcmc_create_multi), swap attempts
+    every 10 steps within each alignment's ladder, the GTR moves of the MCMC
+    leg.  Run once per launch mode: every chain's evaluations of a step in
+    one graph replay of the batched kernels (one staging copy, the run walk
+    for long lists, the batched short-list kernel, one read-back), or one
+    launch per chain on its own stream.  Wall time per step and, batched,
+    the graph's device time per step (CUDA events); ESS of the cold chain of
+    the first alignment (lnL, root height, first exchangeability)."""
+    from aspartik_gb300.ess import min_ess
+    from aspartik_gb300.mcmc import GTR_WEIGHTS, Mcmc, McmcSettings
+
+    probs = c4_problems()
+    out = {"problems": [{k: p[k] for k in ("taxa", "sites", "patterns")} for p in probs],
+           "chains": temps * len(probs), "temperatures": temps, "steps": steps}
+    for launch in ("batch", "streams"):
+        s = McmcSettings(model="gtr", precision="f32", num_categories=4,
+                         num_chains=temps * len(probs), heat=0.1, swap_every=10, seed=4,
+                         sample_every=10, weights=dict(GTR_WEIGHTS), device=device,
+                         launch=launch)
+        m = Mcmc.multi([(p["leaves"], p["weights"], p["tree"].parents, p["tree"].heights)
+                        for p in probs], s)
+        m.set_parameters(rates=np.ones(6), frequencies=np.full(4, 0.25), alpha=0.5,
+                         birth_rate=1.0)
+        m.run(200)  # warm-up: operator tuning, first graph replays
+        st0 = m.launch_stats()
+        tried0, acc0 = m.swaps()
+        t0 = time.perf_counter()
+        m.run(steps)
+        dt = time.perf_counter() - t0
+        st = m.launch_stats()
+        tried, acc = m.swaps()
+        keep = (steps // 10) // 5
+        traces = {k: m.trace(k)[20 + keep:] for k in ESS_FIELDS}
+        e, per = min_ess(traces, burn_in=0.0)
+        arm = {"seconds": round(dt, 3), "wall_us_per_step": round(dt / steps * 1e6, 2),
+               "chain_steps_per_s": round(temps * len(probs) * steps / dt, 1),
+               "swap_rate": round((acc - acc0) / max(tried - tried0, 1), 3),
+               "cold_chain_ess_min": round(e, 2),
+               "cold_chain_ess": {k: round(v, 2) for k, v in per.items()},
+               "check_rel": m.check()}
+        if st["batched"]:
+            n = st["launches"] - st0["launches"]
+            dev_us = (st["device_ms"] - st0["device_ms"]) * 1e3 / max(n, 1)
+            arm["graph_replays"] = n
+            arm["device_us_per_step"] = round(dev_us, 2)
+            arm["wall_over_device"] = round(arm["wall_us_per_step"] / max(dev_us, 1e-9), 3)
+        out[launch] = arm
+        m.close()
+    out["faster"] = min(("batch", "streams"), key=lambda k: out[k]["wall_us_per_step"])
+    return out
+
+
 def dedup_leg(device: int, seed: int = 4) -> dict:
     """Site-pattern compression of the largest batched configuration's
     alignment size (200 taxa x 50,000 sites, simulated under GTR) on the
@@ -756,6 +832,9 @@ def run_ours(args):
     mc3_out = mc3(wl, 5000, device) if long_legs else None
     if long_legs:
         progress("MC3")
+    c4 = c4_mcmc(device, 20_000) if long_legs else None
+    if long_legs:
+        progress("32-chain MCMC (4 alignments x 8 temperatures)")
     configs = None
     if long_legs and args.workload == DEFAULT_WORKLOAD:
         configs = {"dna16x1000_hky": config_block("dna16x1000_hky", device, 10_000)}
@@ -839,6 +918,7 @@ def run_ours(args):
                        "kernel_us": round(dprune * 1e3 / max(dn, 1), 3)},
         "mcmc": mcmc,
         "mc3": mc3_out,
+        "c4_mcmc": c4,
         "configs": configs,
         "dedup": dedup,
         "batched": batch,
