@@ -75,9 +75,11 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 					 cudaHostAllocDefault),
 			   "pinned lnl");
 		check_cuda(cudaMalloc(&d_work_, 4 * sizeof(unsigned)), "work counters");
+		// one sum per tile of a member, for tiles as small as 16 patterns
+		// (whatever tile the member's autotuner picks later)
 		size_t total_tiles = 0;
 		for (Calculator *c : members_)
-			total_tiles += c->ldp_ / c->runs_tile_;
+			total_tiles += c->ldp_ / 16;
 		check_cuda(cudaMalloc(&d_tile_sums_, sizeof(double) * total_tiles),
 			   "tile sums");
 		check_cuda(cudaMalloc(&d_tickets_, sizeof(unsigned) * M), "tickets");
@@ -108,7 +110,7 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 			d.L = c->L_;
 			d.tile = c->runs_tile_;
 			d.log_inv_c = std::log(1.0 / static_cast<double>(c->C_));
-			tile_off += c->ldp_ / c->runs_tile_;
+			tile_off += c->ldp_ / 16;
 			max_ops = std::max<uint32_t>(
 				max_ops, c->I_ * sizeof(NodeOp) +
 						 ((c->I_ + 4) & ~3u) * sizeof(uint32_t));

@@ -112,7 +112,7 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		runs_tile_ >>= 1;
 	if (const char *env = std::getenv("B3G_RUNS_TILE")) {
 		const uint32_t t = static_cast<uint32_t>(std::atoi(env));
-		if (t == 32 || t == 64 || t == 128)
+		if (t == 16 || t == 32 || t == 64 || t == 128)
 			runs_tile_ = t;
 	}
 	if (const char *env = std::getenv("B3G_RUNS_BLOCK")) {
@@ -169,9 +169,10 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 
 	const size_t slots = 2ull * I_;
 	const size_t rsz = f32_ ? sizeof(float) : sizeof(double);
-	// one block sum per thread block of either walk: at most one block
-	// per 32 patterns
-	const size_t nblocks = ldp_ / 32;
+	// one block sum per thread block of any walk: at most one block per
+	// 16 patterns (the smallest run-walk tile)
+	const size_t nblocks = ldp_ / 16;
+	block_sums_cap_ = static_cast<uint32_t>(nblocks);
 
 	try {
 		check_cuda(cudaStreamCreateWithFlags(&stream_,
@@ -648,6 +649,8 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 		pp.slots = reinterpret_cast<const uint32_t *>(d_stage_ + off_slots_);
 		const uint32_t tiles = ldp_ / pp.tile;
 		const uint32_t ctas = std::min(tiles, num_sms_ * (1024 / block));
+		if (ctas > block_sums_cap_)
+			throw Error(B3G_ERR_STATE, "run walk grid exceeds the block sums");
 		// the result also goes straight to the mapped host word
 		pp.lnl_host = d_lnl_host_;
 		arm_poll();
@@ -1201,10 +1204,14 @@ uint32_t Calculator::autotune(const uint32_t *internals,
 	// tuned tile
 	if (!use_runs_ || (use_direct_ && n <= kDirectMax))
 		return runs_tile_;
-	// (patterns per tile, threads per block)
+	// (patterns per tile, threads per block).  Two pattern columns of one
+	// category per thread: a warp spans 32 / (tile / 2) categories, so
+	// tiles of 16 and 32 patterns put four and two categories in a warp
+	// (and give small alignments more blocks), 64 and 128 one.
 	uint32_t best_tile = runs_tile_, best_block = runs_block_;
 	float best_ms = INFINITY;
-	const uint32_t cand[][2] = {{32, 512}, {64, 512}, {128, 512}, {32, 1024}, {64, 1024}};
+	const uint32_t cand[][2] = {{16, 512},  {32, 512},  {64, 512},
+				    {128, 512}, {32, 1024}, {64, 1024}};
 	for (const auto &tb : cand) {
 		const uint32_t t = tb[0], b = tb[1];
 		if (t * C_ > 512 || (b == 1024 && t * C_ >= 512))

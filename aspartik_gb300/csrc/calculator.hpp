@@ -77,7 +77,7 @@ class Calculator {
 	uint32_t runs_block() const { return runs_block_; }
 	void set_runs_shape(uint32_t tile, uint32_t block)
 	{
-		if ((tile != 32 && tile != 64 && tile != 128) ||
+		if ((tile != 16 && tile != 32 && tile != 64 && tile != 128) ||
 		    (block != 512 && block != 1024) || tile * C_ > 512 ||
 		    (block == 1024 && tile * C_ >= 512))
 			throw Error(B3G_ERR_INVALID_ARGUMENT, "no such run-walk shape");
@@ -235,6 +235,7 @@ class Calculator {
 	// synchronised with it (model uploads, eigen kernel, own proposals)
 	bool stream_dirty_ = false;
 	uint32_t num_sms_ = 1;
+	uint32_t block_sums_cap_ = 0; // d_block_sums_ entries
 	uint32_t runs_tile_ = 64;
 	bool use_runs_ = false;
 	bool use_direct_ = false;

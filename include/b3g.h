@@ -210,8 +210,11 @@ B3G_API b3g_status b3g_calculator_span_end(b3g_calculator *calc, float *ms);
 /* Autotuner (no counterpart in the reference).  Times a representative list
  * (normally the whole tree) with each launch configuration of this
  * calculator's form and keeps the fastest: patterns per tile of the
- * run-synchronous walk (32, 64 or 128; four-state FP32), or tensor cores
- * (one or two thread groups per CTA) against CUDA cores (20-state FP32).
+ * run-synchronous walk (16, 32, 64 or 128, with 512- or 1,024-thread
+ * blocks; a thread owns two pattern columns of one category, so a warp
+ * spans four, two, one or one categories; four-state FP32), or tensor
+ * cores (one or two thread groups per CTA) against CUDA cores (20-state
+ * FP32).
  * Every trial proposal is rejected, so
  * call it between steps; the accepted state is unchanged.  `choice`
  * receives the tile, or 1 (tensor cores) / 0 (CUDA cores); the FP64 form

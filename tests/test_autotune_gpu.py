@@ -30,7 +30,7 @@ def test_dna_tile_choice_keeps_state(rng):
         g.accept()
     tree.accept()
     choice = tuned.autotune(*full, 1.0)
-    assert choice in (32, 64, 128)
+    assert choice in (16, 32, 64, 128)
     for _ in range(4):
         random_move(tree, rng)
         inc = lists_and_lengths(tree)

@@ -22,6 +22,7 @@ pytestmark = pytest.mark.gpu
 SHAPES = [  # (tile, block, slots, inline)
     (64, 512, 0, 0), (64, 512, 1, 0), (64, 512, 0, 1), (64, 512, 1, 1),
     (32, 512, 1, 1), (32, 1024, 1, 1), (64, 1024, 1, 1), (64, 1024, 0, 0),
+    (16, 512, 1, 1), (16, 512, 0, 0), (16, 1024, 1, 1),
 ]
 
 
