@@ -233,6 +233,7 @@ struct Tc20Params {
 	uint32_t ops_smem;   // stage the list in shared memory
 	uint32_t tips_smem;  // stage the tile's tip codes in shared memory
 	uint32_t groups;     // 128-thread groups per CTA (1 or 2)
+	uint32_t cluster;    // CTAs per (tile, category) work item, 1..8
 	double log_inv_c;
 };
 // Dynamic shared memory of one tensor-core pruning CTA.

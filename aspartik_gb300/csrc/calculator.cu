@@ -129,6 +129,13 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 		use_tc20_ = use_tc20_ && std::atoi(env) != 0;
 	// groups of 128 threads per tensor-core CTA (B3G_TC20_GROUPS = 1 or 2;
 	// default: chosen per launch from the grid size)
+	if (const char *env = std::getenv("B3G_TC20_CLUSTER")) {
+		const int k = std::atoi(env);
+		if (k >= 1 && k <= 8) {
+			tc20_cluster_ = static_cast<uint32_t>(k);
+			tc20_cluster_fixed_ = true;
+		}
+	}
 	if (const char *env = std::getenv("B3G_TC20_GROUPS")) {
 		const int gr = std::atoi(env);
 		if (gr == 1 || gr == 2) {
@@ -726,6 +733,15 @@ void Calculator::launch20(uint32_t n, bool matrices_mode, double clock_rate,
 			tc20_groups_ ? tc20_groups_
 				     : ((ldp_ / 128u) * C_ < 6u * num_sms_ ? 2u : 1u);
 		tp.groups = groups;
+		// a work item (tile, category) spread over a cluster of CTAs
+		// while the grid has fewer items than CTA slots (4 / groups per
+		// SM), so that every SM holds groups on independent entries
+		const uint32_t items = (ldp_ / 128u) * C_;
+		uint32_t cluster = std::max(1u, std::min(8u, (4u / groups) * num_sms_ /
+								      std::max(items, 1u)));
+		if (tc20_cluster_fixed_)
+			cluster = tc20_cluster_;
+		tp.cluster = cluster;
 		const size_t budget = smem_budget(256u * groups);
 		const size_t ops_bytes = (size_t)n * sizeof(NodeOp);
 		size_t used = prune20tc_smem(groups, false, n, false, L_);

@@ -242,6 +242,8 @@ class Calculator {
 	bool use_tc20_ = false;
 	uint32_t tc20_groups_ = 0; // 0: per launch from the grid size
 	bool tc20_groups_fixed_ = false; // set by B3G_TC20_GROUPS
+	uint32_t tc20_cluster_ = 1;      // CTAs per work item when fixed
+	bool tc20_cluster_fixed_ = false; // set by B3G_TC20_CLUSTER
 	float *d_tc_tab_ = nullptr;     // 20-state MMA operand blocks
 	double *d_root_val_ = nullptr;  // [C][ldp] root pi . x per category
 	int32_t *d_root_exp_ = nullptr; // [C][ldp] its exponent

@@ -26,12 +26,16 @@
 #include "b3g_device.cuh"
 #include "tc_ptx.cuh"
 
+#include <cooperative_groups.h>
+
 #include <math.h>
 
 #include <atomic>
 
 namespace b3g {
 namespace {
+
+namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------------
 // 4-vectors: double4_32a (one 256-bit access) and float4 (one 128-bit access)
@@ -920,14 +924,29 @@ static cudaError_t launch_prune20tc_g(const Tc20Params &p, bool narrow, int smem
 		kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 	if (e != cudaSuccess)
 		return e;
-	kern<<<dim3(p.ldp / kTcRows, p.C), 128 * kG, smem, s>>>(p);
+	// grid (K, tiles, C), clusters of the K CTAs of one work item
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(p.cluster, p.ldp / kTcRows, p.C);
+	cfg.blockDim = dim3(128 * kG);
+	cfg.dynamicSmemBytes = (size_t)smem;
+	cfg.stream = s;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = p.cluster;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	e = cudaLaunchKernelEx(&cfg, kern, p);
+	if (e != cudaSuccess)
+		return e;
 	return cudaGetLastError();
 }
 
 cudaError_t launch_prune20tc(const Tc20Params &p, cudaStream_t s)
 {
 	if (p.C == 0 || p.C > 8 || p.ldp % kTcRows || p.n == 0 ||
-	    (p.groups != 1 && p.groups != 2))
+	    (p.groups != 1 && p.groups != 2) || p.cluster < 1 || p.cluster > 8)
 		return cudaErrorInvalidValue;
 	const bool narrow = (uint64_t)p.L * 2 * p.C * p.ldp < (1ull << 31);
 	const int smem = (int)prune20tc_smem(p.groups, p.ops_smem != 0, p.n,

@@ -14,11 +14,15 @@
 // 2 S^2 per internal child and (pattern, category); the tensor core
 // executes 3 x (32/20) x (24/20) times that.
 //
-// Work: one CTA per (pattern tile, category) with kG groups of 128 threads;
-// thread t of a group owns pattern t of the tile (tensor-memory lane t).
-// The list is walked run by run (NodeOp::pad = entries left in the run, so
-// the entries of a run are mutually independent): group g takes entries
-// g, g + kG, ... of each run, and the whole CTA synchronises between runs.
+// Work: one cluster of K CTAs per (pattern tile, category), each CTA with kG
+// groups of 128 threads; thread t of a group owns pattern t of the tile
+// (tensor-memory lane t).  The list is walked run by run (NodeOp::pad =
+// entries left in the run, so the entries of a run are mutually
+// independent): group gg = rank kG + g of the cluster takes entries gg,
+// gg + K kG, ... of each run, and the cluster synchronises between runs
+// (partials written by one CTA are read by another's bulk copies in the
+// next run).  K > 1 spreads a work item over several SMs when the grid has
+// fewer items than CTA slots (K = 1: one CTA, a barrier of its own).
 // Per entry a group stages its internal children's partials (split) and the
 // two tables' operand blocks in its own shared memory, thread 0 of the group
 // issues the MMAs into the group's tensor-memory columns and commits them to
@@ -135,14 +139,20 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 	__shared__ __align__(8) uint64_t mbar[kG]; // MMA completion, per group
 	__shared__ __align__(8) uint64_t lbar[kG]; // input copies, per group
 	__shared__ uint32_t holder;
+	// cluster-wide stop flags (rank 0's are read), one per run parity
+	__shared__ uint32_t s_stop[2];
 	const uint32_t g = threadIdx.x >> 7, t = threadIdx.x & 127u;
 	const uint32_t warp = threadIdx.x >> 5;
 	float *sA = sBase + g * kTcGroup; // [side][hi, lo][2,560]
 	float *sB = sA + 4 * kTcA;         // [side][hi, lo][768]
-	const uint32_t c = blockIdx.y, C = prm.C;
-	const uint32_t p = blockIdx.x * kTcRows + t;
+	// grid (K, tiles, C): the cluster's CTAs share blockIdx.y / z
+	const uint32_t K = gridDim.x, rank = blockIdx.x;
+	const uint32_t gg = rank * kG + g, G = K * kG; // group in the cluster
+	const uint32_t tile = blockIdx.y;
+	const uint32_t c = blockIdx.z, C = prm.C;
+	const uint32_t p = tile * kTcRows + t;
 	const Idx stride = (Idx)C * prm.ldp;
-	const Idx col0 = (Idx)c * prm.ldp + blockIdx.x * kTcRows;
+	const Idx col0 = (Idx)c * prm.ldp + tile * kTcRows;
 	const Idx col = col0 + t;
 	const uint32_t mb = tc::smem_u32(&mbar[g]);
 	const uint32_t lb = tc::smem_u32(&lbar[g]);
@@ -160,15 +170,17 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 		for (uint32_t k = threadIdx.x; k < prm.L * 32u; k += blockDim.x) {
 			const uint32_t leaf = k >> 5, w4 = k & 31u;
 			s32[k] = *reinterpret_cast<const uint32_t *>(
-				prm.tips + (size_t)leaf * prm.ldp + blockIdx.x * kTcRows + 4 * w4);
+				prm.tips + (size_t)leaf * prm.ldp + tile * kTcRows + 4 * w4);
 		}
 	}
 	const NodeOp *ops = prm.ops_smem ? sOps : prm.ops;
-	if (threadIdx.x == 0)
+	if (threadIdx.x == 0) {
 		for (uint32_t k = 0; k < kG; k++) {
 			tc::mbar_init(tc::smem_u32(&mbar[k]), 1);
 			tc::mbar_init(tc::smem_u32(&lbar[k]), 1);
 		}
+		s_stop[0] = s_stop[1] = 0u;
+	}
 	if (warp == 0)
 		tc::tmem_alloc(tc::smem_u32(&holder), 128 * kG);
 	tc::fence_proxy_async_smem(); // the zeroed areas before the first copies
@@ -231,13 +243,16 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 	uint32_t lphase = 0, mphase = 0;
 	bool failed = false, pending = false;
 	uint32_t e0 = 0, r = run_len(0);
-	if (g < r) {
+	if (K > 1)
+		cg::this_cluster().sync(); // every CTA started, its flags zeroed
+	if (gg < r) {
 		if (t == 0)
-			issue(g);
+			issue(gg);
 		pending = true;
 	}
+	uint32_t run = 0;
 	for (;;) {
-		for (uint32_t e = e0 + g; e < e0 + r; e += kG) {
+		for (uint32_t e = e0 + gg; e < e0 + r; e += G) {
 			const NodeOp op = ops[e];
 			const uint32_t ids[2] = {op.left, op.right};
 			const bool any = !(ids[0] & kTipBit) || !(ids[1] & kTipBit);
@@ -277,11 +292,11 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 			}
 			// every copied row read, the previous entry's output stored
 			group_sync(g);
-			const bool next = e + kG < e0 + r;
+			const bool next = e + G < e0 + r;
 			if (!any) {
 				if (next) {
 					if (t == 0)
-						issue(e + kG);
+						issue(e + G);
 					pending = true;
 				}
 			} else {
@@ -331,7 +346,7 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 				// travel during this epilogue
 				if (next) {
 					if (t == 0)
-						issue(e + kG);
+						issue(e + G);
 					pending = true;
 				}
 				tc::fence_after_sync();
@@ -379,23 +394,38 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 			for (uint32_t q = 0; q < 5; q++)
 				d4[t + 128 * q] = s4[t + 128 * q];
 		}
-		// the run's outputs are visible to every group, and to the bulk
-		// copies of the next run, before those read them
+		// the run's outputs are visible to every group of the cluster,
+		// and to the bulk copies of the next run, before those read them
 		tc::fence_proxy_async_global();
 		tc::fence_before_sync();
-		const int stop = __syncthreads_or(failed);
+		int stop = __syncthreads_or(failed);
+		if (K > 1) {
+			// a stop anywhere stops every CTA at this run: the flag of
+			// this run's parity in rank 0 (the other parity's may
+			// already be written by a CTA ahead, never this one)
+			cg::cluster_group cl = cg::this_cluster();
+			uint32_t *flag = cl.map_shared_rank(&s_stop[run & 1u], 0);
+			if (threadIdx.x == 0 && stop)
+				atomicOr(flag, 1u);
+			cl.sync();
+			stop = *(volatile uint32_t *)flag != 0u;
+		}
 		tc::fence_after_sync();
 		if (stop) {
 			failed = true;
 			break;
 		}
+		++run;
 		e0 += r;
 		if (e0 >= prm.n)
 			break;
 		r = run_len(e0);
-		if (g < r) {
-			if (t == 0)
-				issue(e0 + g);
+		if (gg < r) {
+			if (t == 0) {
+				// other CTAs' stores before this CTA's bulk copies
+				tc::fence_proxy_async_global();
+				issue(e0 + gg);
+			}
 			pending = true;
 		}
 	}
@@ -411,6 +441,9 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 	tc::fence_after_sync();
 	if (warp == 0)
 		tc::tmem_dealloc(holder, 128 * kG);
+	// no CTA leaves while another may still read rank 0's flags
+	if (K > 1)
+		cg::this_cluster().sync();
 }
 
 // Category mixing of the root (FP32 form: values with power-of-two

@@ -263,3 +263,47 @@ def test_tensor_core_single_entry_lists_and_eight_categories(groups):
             assert tc.log_likelihood() == pytest.approx(g64.log_likelihood(), rel=F32_TOL)
         tc.close()
         g64.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2])
+def test_tensor_core_clusters_agree(rng, groups):
+    """A work item (pattern tile, category) spread over a thread-block
+    cluster of 2, 3 or 8 CTAs walks every run's independent entries on more
+    groups (a cluster barrier between runs, partials passed through global
+    memory) with the same per-entry arithmetic: the likelihoods equal one
+    CTA per item bit for bit, whole tree and dirty paths, and meet the FP32
+    bar against the FP64 form."""
+    c = protein_case(48, 600, seed=71, alpha=0.6, num_categories=4, gaps=0.02)
+    tree = O.DatedTree(c.tree.parents, c.tree.heights)
+    calcs = {k: make20_env(c, 4, B3G_TC20_GROUPS=groups, B3G_TC20_CLUSTER=k)
+             for k in (1, 2, 3, 8)}
+    g64 = make20(c, "f64", 4)
+    every = list(calcs.values()) + [g64]
+    for g in every:
+        g.set_reversible(c.rates, c.pi)
+        g.set_gamma(0.6)
+        g.propose_lengths(*whole(tree), 1.0)
+    ref = g64.log_likelihood()
+    base = calcs[1].log_likelihood()
+    assert base == pytest.approx(ref, rel=F32_TOL)
+    for k, g in calcs.items():
+        assert g.log_likelihood() == base, k
+        np.testing.assert_array_equal(g.site_log_likelihoods(),
+                                      calcs[1].site_log_likelihoods())
+    for g in every:
+        g.accept()
+    tree.accept()
+    for step in range(5):
+        random_move(tree, rng)
+        inc = lists_and_lengths(tree)
+        for g in every:
+            g.propose_lengths(*inc, 1.0)
+        base = calcs[1].log_likelihood()
+        assert base == pytest.approx(g64.log_likelihood(), rel=F32_TOL), step
+        for k, g in calcs.items():
+            assert g.log_likelihood() == base, (step, k)
+        tree.accept()
+        for g in every:
+            g.accept()
+    for g in every:
+        g.close()
