@@ -191,7 +191,7 @@ Batch::Batch(Calculator *const *members, uint32_t count)
 		for (uint32_t C : {4u, 2u, 1u})
 			if (direct_c_[C])
 				check_cuda(launch_prune4_direct_batch(
-						   bp_, C, (4u / C) * members_[0]->num_sms_, stream2_),
+						   bp_, C, (8u / C) * members_[0]->num_sms_, stream2_),
 					   "batched short-list kernel");
 		check_cuda(cudaEventRecord(ev_join_, stream2_), "join");
 		check_cuda(cudaStreamWaitEvent(stream_, ev_join_, 0), "join");

@@ -868,9 +868,8 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 		harvest(slot);
 	slot.direct = true;
 	record(slot.k0);
-	// 128-pattern tiles, 128 * C threads per block, 512 threads per SM (the
-	// walk's loads ahead take up to 128 registers a thread)
-	const uint32_t ctas = std::min(ldp_ / 128u, (4u / C_) * num_sms_);
+	// 128-pattern tiles, 128 * C threads per block, 1024 threads per SM
+	const uint32_t ctas = std::min(ldp_ / 128u, (8u / C_) * num_sms_);
 	arm_poll();
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
 	++in_flight_;

@@ -595,10 +595,13 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 // code.  Every clean input and tip code is known before the walk starts
 // (the host marks each child's source in DirectParams::src), so they are
 // loaded kDirectAhead entries ahead of their use, the first ones before the
-// tables are built: one DRAM round trip for the whole list instead of one
-// per entry.  The two previous outputs stay in registers; an older output
-// is read back when needed (written by the same thread earlier).
-constexpr uint32_t kDirectAhead = 4;
+// tables are built.  The two previous outputs stay in registers; an older
+// output is read back when needed (written by the same thread earlier).
+// Two entries ahead fit 64 registers, so two blocks share an SM and
+// several chains' launches can overlap on the same SMs.  (One, two and four
+// entries ahead measured within 2 % of each other on one chain and on
+// eight: the walk is not bound by these loads.)
+constexpr uint32_t kDirectAhead = 2;
 
 template <typename Idx>
 __device__ __forceinline__ void direct_fetch(const NodeOp *ops, const uint8_t (*src)[2],
@@ -740,7 +743,7 @@ __device__ __forceinline__ void direct_tables(const ModelDev *m, const float *s_
 }
 
 template <typename Idx, uint32_t kC>
-__global__ void __launch_bounds__(128 * kC, 4 / kC)
+__global__ void __launch_bounds__(128 * kC, 8 / kC)
 prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 {
 	constexpr uint32_t kTile = 128, kCols = kTile * kC;
@@ -825,7 +828,7 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 // weighted sum goes to the member's tile slot; the block finishing a
 // member's last tile folds its sums (fixed order).
 template <typename Idx, uint32_t kC>
-__global__ void __launch_bounds__(128 * kC, 4 / kC)
+__global__ void __launch_bounds__(128 * kC, 8 / kC)
 prune4_direct_batch_kernel(BatchParams bp)
 {
 	constexpr uint32_t kTile = 128, kCols = kTile * kC;
