@@ -104,6 +104,7 @@ class McmcConfig(ct.Structure):
         ("da_drift_limit", ct.c_double),
         ("clock_categories", ct.c_uint32),
         ("launch", ct.c_uint32),
+        ("host_threads", ct.c_uint32),
     ]
 
 
@@ -185,6 +186,7 @@ SIGNATURES = {
     "b3g_surrogate_train": (ct.c_int, [_vp, _f32p, _f32p, _f32p, ct.c_uint32, ct.c_uint32,
                                        ct.c_uint32, ct.c_float, ct.c_uint64, _f32p]),
     "b3g_surrogate_delta": (ct.c_int, [_vp, _f32p, _f32p, _f32p]),
+    "b3g_surrogate_deltas": (ct.c_int, [_vp, _f32p, _f32p, ct.c_uint32, _f32p]),
     "b3g_batch_create": (ct.c_int, [ct.POINTER(_vp), ct.c_uint32, ct.POINTER(_vp)]),
     "b3g_batch_destroy": (None, [_vp]),
     "b3g_calculator_stage_lengths": (

@@ -169,6 +169,24 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 		batch_ = std::make_unique<Batch>(calcs.data(), (uint32_t)calcs.size());
 		batch_lnl_.assign(calcs.size(), 0.0);
 	}
+	uint32_t threads = cfg.host_threads;
+	if (const char *env = std::getenv("B3G_MCMC_THREADS"))
+		threads = (uint32_t)std::max(0, std::atoi(env));
+	if (threads == 0) // a thread for every four chains, at most 8
+		threads = std::min<uint32_t>(
+			{((uint32_t)chains_.size() + 3) / 4, 8u,
+			 std::max(1u, std::thread::hardware_concurrency())});
+	threads = std::min<uint32_t>(threads, (uint32_t)chains_.size());
+	// a batched step's host work per chain is a few copies: the pool's
+	// hand-offs cost more than they save
+	if (batch_)
+		threads = 1;
+	if (threads > 1) {
+		const int dev = cfg.device;
+		pool_ = std::make_unique<HostPool>(threads, [dev] {
+			check_cuda(cudaSetDevice(dev), "cudaSetDevice");
+		});
+	}
 }
 
 double Mcmc::send_model(Chain &ch, bool mark_all)
@@ -626,21 +644,41 @@ void Mcmc::features(const Chain &ch, float *out) const
 // Carlo using an approximation", J. Comput. Graph. Stat. 14(4), 2005): the
 // proposal passes with probability min(1, r*), r* its MH ratio with the
 // surrogate difference in place of the exact log-likelihood difference.
-void Mcmc::screen(Chain &ch)
+// Every pending screenable proposal of the step goes through one surrogate
+// launch, before any chain's evaluation is queued (a launch behind them
+// would wait for their blocks).
+void Mcmc::screen_all()
 {
-	float xn[kDaInputs], xo[kDaInputs];
-	for (uint32_t k = 0; k < kDaInputs; ++k) {
-		xn[k] = (ch.feat_new[k] - in_mean_[k]) * in_scale_[k];
-		xo[k] = (ch.feat_old[k] - in_mean_[k]) * in_scale_[k];
+	screen_idx_.clear();
+	for (auto &ch : chains_)
+		if (ch->status == 0 && ch->screenable)
+			screen_idx_.push_back(ch->index);
+	const uint32_t n = (uint32_t)screen_idx_.size();
+	if (n == 0)
+		return;
+	screen_xn_.resize((size_t)n * kDaInputs);
+	screen_xo_.resize((size_t)n * kDaInputs);
+	screen_out_.resize(n);
+	for (uint32_t j = 0; j < n; ++j) {
+		const Chain &ch = *chains_[screen_idx_[j]];
+		for (uint32_t k = 0; k < kDaInputs; ++k) {
+			screen_xn_[j * kDaInputs + k] =
+				(ch.feat_new[k] - in_mean_[k]) * in_scale_[k];
+			screen_xo_[j * kDaInputs + k] =
+				(ch.feat_old[k] - in_mean_[k]) * in_scale_[k];
+		}
 	}
-	ch.da_delta = out_scale_ * (double)surrogate_->delta(xn, xo);
-	const double log_r1 =
-		ch.beta * (ch.da_delta + ch.prior_new - ch.prior_cache) + ch.hastings;
-	if (log_r1 > std::log(ch.rng.uniform())) {
-		ch.screened = true;
-	} else {
-		ch.status = 3;
-		++da_.stage1_rejects;
+	surrogate_->deltas(screen_xn_.data(), screen_xo_.data(), n, screen_out_.data());
+	for (uint32_t j = 0; j < n; ++j) {
+		Chain &ch = *chains_[screen_idx_[j]];
+		ch.da_delta = out_scale_ * (double)screen_out_[j];
+		const double log_r1 = ch.beta * (ch.da_delta + ch.prior_new -
+						 ch.prior_cache) +
+				      ch.hastings;
+		if (log_r1 > std::log(ch.rng.uniform()))
+			ch.screened = true;
+		else
+			ch.status = 3;
 	}
 }
 
@@ -691,38 +729,35 @@ void Mcmc::train_surrogate()
 	drift_pos_ = 0;
 }
 
-// Metropolis-Hastings and finalize_step (mcmc.rs:337-393); for a screened
-// proposal, stage two of delayed acceptance: min(1, r / r*).
-void Mcmc::finish(Chain &ch)
+void Mcmc::prepare(Chain &ch)
 {
-	OpStats &st = ops_[ch.op];
+	propose(ch);
+	if (ch.status != 0)
+		return;
+	ch.prior_new = prior(ch);
+	if (ch.prior_new == kNegInf)
+		ch.status = 2; // mcmc.rs:331-335
+}
+
+// Metropolis-Hastings and finalize_step (mcmc.rs:337-393); for a screened
+// proposal, stage two of delayed acceptance: min(1, r / r*).  Touches the
+// chain alone; tally() gathers the statistics.
+void Mcmc::settle(Chain &ch)
+{
 	bool accept = false;
+	ch.evaluated = ch.finite = false;
 	if (ch.status == 0) {
 		const double lnl = !ch.launched ? ch.lnl_cache
 				   : batch_    ? batch_lnl_[ch.index]
 					       : ch.calc->log_likelihood();
 		ch.lnl_new = lnl;
-		if (ch.launched)
-			++da_.exact_evaluations;
+		ch.evaluated = ch.launched;
 		if (lnl != kNegInf && !std::isnan(lnl)) {
-			const double dlnl = lnl - ch.lnl_cache;
+			ch.finite = true;
+			ch.dlnl = lnl - ch.lnl_cache;
 			if (ch.screened) {
-				const double err = dlnl - ch.da_delta;
+				const double err = ch.dlnl - ch.da_delta;
 				accept = ch.beta * err > std::log(ch.rng.uniform());
-				++(accept ? da_.stage2_accepts : da_.stage2_rejects);
-				// drift of the screen: RMS of the last window of errors
-				drift_[drift_pos_++ % drift_.size()] = err * err;
-				if (drift_pos_ >= drift_.size()) {
-					double s = 0.0;
-					for (const double e2 : drift_)
-						s += e2;
-					da_.drift_rms = std::sqrt(s / drift_.size());
-					if (cfg_.da_drift_limit > 0.0 &&
-					    da_.drift_rms > cfg_.da_drift_limit) {
-						da_active_ = false; // back to the exact chain
-						da_.fallback = 1;
-					}
-				}
 			} else {
 				const double new_post = lnl + ch.prior_new;
 				const double old_post = ch.lnl_cache + ch.prior_cache;
@@ -730,25 +765,10 @@ void Mcmc::finish(Chain &ch)
 					ch.beta * (new_post - old_post) + ch.hastings;
 				accept = ratio > std::log(ch.rng.uniform());
 			}
-			// pilot pairs for the surrogate
-			if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
-			    da_.fallback == 0 && std::isfinite(dlnl)) {
-				pilot_old_.insert(pilot_old_.end(), ch.feat_old,
-						  ch.feat_old + kDaInputs);
-				pilot_new_.insert(pilot_new_.end(), ch.feat_new,
-						  ch.feat_new + kDaInputs);
-				pilot_delta_.push_back((float)dlnl);
-				++da_.pilot_pairs;
-			}
 		}
 	}
-	if (ch.status == 1)
-		++st.aborts;
-	else if (ch.status == 2)
-		++st.prior_rejects;
+	ch.accepted = accept;
 	if (accept) {
-		++st.accepts;
-		++st.window_accepts;
 		ch.tree->accept();
 		ch.kappa.accept();
 		ch.alpha.accept();
@@ -762,10 +782,6 @@ void Mcmc::finish(Chain &ch)
 		ch.lnl_cache = ch.lnl_new;
 		ch.prior_cache = ch.prior_new;
 	} else {
-		if (ch.status == 0 || ch.status == 3) {
-			++st.rejects;
-			++st.window_rejects;
-		}
 		const bool restore_model = ch.model_sent;
 		const bool restore_alpha = ch.alpha_sent;
 		ch.tree->reject();
@@ -792,6 +808,57 @@ void Mcmc::finish(Chain &ch)
 	ch.launched = false;
 	ch.model_sent = false;
 	ch.alpha_sent = false;
+}
+
+// In chain order, so the counters, the drift window and the surrogate's
+// pilot pairs do not depend on the host threads.
+void Mcmc::tally(const Chain &ch)
+{
+	OpStats &st = ops_[ch.op];
+	if (ch.evaluated)
+		++da_.exact_evaluations;
+	if (ch.status == 3)
+		++da_.stage1_rejects;
+	if (ch.status == 0 && ch.finite) {
+		if (ch.screened) {
+			++(ch.accepted ? da_.stage2_accepts : da_.stage2_rejects);
+			// drift of the screen: RMS of the last window of errors
+			const double err = ch.dlnl - ch.da_delta;
+			drift_[drift_pos_++ % drift_.size()] = err * err;
+			if (drift_pos_ >= drift_.size()) {
+				double s = 0.0;
+				for (const double e2 : drift_)
+					s += e2;
+				da_.drift_rms = std::sqrt(s / drift_.size());
+				if (cfg_.da_drift_limit > 0.0 &&
+				    da_.drift_rms > cfg_.da_drift_limit) {
+					da_active_ = false; // back to the exact chain
+					da_.fallback = 1;
+				}
+			}
+		}
+		// pilot pairs for the surrogate
+		if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
+		    da_.fallback == 0 && std::isfinite(ch.dlnl)) {
+			pilot_old_.insert(pilot_old_.end(), ch.feat_old,
+					  ch.feat_old + kDaInputs);
+			pilot_new_.insert(pilot_new_.end(), ch.feat_new,
+					  ch.feat_new + kDaInputs);
+			pilot_delta_.push_back((float)ch.dlnl);
+			++da_.pilot_pairs;
+		}
+	}
+	if (ch.status == 1)
+		++st.aborts;
+	else if (ch.status == 2)
+		++st.prior_rejects;
+	if (ch.accepted) {
+		++st.accepts;
+		++st.window_accepts;
+	} else if (ch.status == 0 || ch.status == 3) {
+		++st.rejects;
+		++st.window_rejects;
+	}
 }
 
 // Metropolis coupling: adjacent temperatures exchange with probability
@@ -916,33 +983,69 @@ void Mcmc::record()
 
 void Mcmc::run(uint64_t steps)
 {
+	const uint32_t n = (uint32_t)chains_.size();
+	// chain i on host thread i % T, each thread's chains in order
+	auto each = [&](auto &&fn) {
+		if (!pool_) {
+			for (auto &ch : chains_)
+				fn(*ch);
+			return;
+		}
+		const uint32_t T = pool_->size();
+		pool_->run([&](uint32_t w) {
+			for (uint32_t i = w; i < n; i += T)
+				fn(*chains_[i]);
+		});
+	};
+	auto launch_pending = [&](Chain &ch) {
+		if (ch.status == 0)
+			launch(ch);
+	};
 	for (uint64_t s = 0; s < steps; ++s) {
-		for (auto &ch : chains_)
-			propose(*ch);
-		for (auto &ch : chains_) {
-			if (ch->status != 0)
-				continue;
-			ch->prior_new = prior(*ch);
-			if (ch->prior_new == kNegInf)
-				ch->status = 2; // mcmc.rs:331-335
-			else if (da_active_ && ch->screenable)
-				screen(*ch);
+		// the surrogate screens the step's proposals between their
+		// preparation and the first launch; without it each thread goes
+		// straight from a chain's proposal to its launch
+		const bool screening = da_active_;
+		if (screening) {
+			each([&](Chain &ch) { prepare(ch); });
+			screen_all();
 		}
-		// every chain's device work is queued before any result is read
-		bool any = false;
-		for (auto &ch : chains_)
-			if (ch->status == 0) {
-				launch(*ch);
+		if (batch_) {
+			each([&](Chain &ch) {
+				if (!screening)
+					prepare(ch);
+				launch_pending(ch);
+			});
+			bool any = false;
+			for (auto &ch : chains_)
 				any = any || ch->launched;
+			if (any) {
+				batch_->run();
+				batch_->log_likelihoods(batch_lnl_.data());
+				batch_ms_ += batch_->last_ms();
+				++batch_runs_;
 			}
-		if (batch_ && any) {
-			batch_->run();
-			batch_->log_likelihoods(batch_lnl_.data());
-			batch_ms_ += batch_->last_ms();
-			++batch_runs_;
+			each([&](Chain &ch) { settle(ch); });
+		} else {
+			// every chain's device work is queued before any result is
+			// read: by each thread for its own chains
+			const uint32_t T = pool_ ? pool_->size() : 1;
+			auto job = [&](uint32_t w) {
+				for (uint32_t i = w; i < n; i += T) {
+					if (!screening)
+						prepare(*chains_[i]);
+					launch_pending(*chains_[i]);
+				}
+				for (uint32_t i = w; i < n; i += T)
+					settle(*chains_[i]);
+			};
+			if (pool_)
+				pool_->run(job);
+			else
+				job(0);
 		}
 		for (auto &ch : chains_)
-			finish(*ch);
+			tally(*ch);
 		++step_;
 		if (cfg_.da_pilot_steps && step_ == cfg_.da_pilot_steps && !surrogate_)
 			train_surrogate();

@@ -15,6 +15,7 @@
 
 #include "batch.hpp"
 #include "calculator.hpp"
+#include "host_pool.hpp"
 #include "mlp.hpp"
 #include "tree.hpp"
 
@@ -143,6 +144,11 @@ struct McmcConfig {
 	double da_drift_limit;
 	uint32_t clock_categories; // 0: strict clock
 	uint32_t launch;           // kLaunch*
+	// host threads that step the chains (0: one for every four chains, at
+	// most 8 and at most the hardware threads; 1: the calling thread
+	// alone; the batched launch mode uses the calling thread); the results
+	// do not depend on it
+	uint32_t host_threads;
 };
 
 // Inputs of the surrogate, for the moves that re-evaluate the whole tree
@@ -191,6 +197,11 @@ struct Chain {
 	bool screened = false; // passed stage one of delayed acceptance
 	double da_delta = 0.0; // surrogate f(x_new) - f(x_old)
 	float feat_old[kDaInputs], feat_new[kDaInputs];
+	// the step's outcome, for the statistics gathered in chain order
+	bool accepted = false;
+	bool evaluated = false; // an exact evaluation was read
+	bool finite = false;    // ... and gave a finite log-likelihood
+	double dlnl = 0.0;      // its difference to the current state's
 	std::vector<uint32_t> internals, children;
 	std::vector<double> lengths;
 	explicit Chain(uint64_t seed) : rng(seed) {}
@@ -269,18 +280,29 @@ class Mcmc {
 	double prior(const Chain &ch) const;
 	void sync_model(Chain &ch);
 	void launch(Chain &ch);
-	void finish(Chain &ch);
+	// propose and prior (any host thread)
+	void prepare(Chain &ch);
+	// read the result, Metropolis-Hastings, accept or reject the chain's
+	// state (any host thread)
+	void settle(Chain &ch);
+	// the step's statistics of one chain (calling thread, chain order)
+	void tally(const Chain &ch);
 	void swap_temperatures();
 	void tune();
 	void record();
 	double send_model(Chain &ch, bool mark_all);
 	void features(const Chain &ch, float *out) const;
-	void screen(Chain &ch);
+	void screen_all();
 	void train_surrogate();
 
 	McmcConfig cfg_;
 	uint32_t num_problems_ = 1;
 	std::vector<std::unique_ptr<Chain>> chains_;
+	// host threads of the step (none: the calling thread alone)
+	std::unique_ptr<HostPool> pool_;
+	// the step's screened chains and the surrogate's inputs and outputs
+	std::vector<uint32_t> screen_idx_;
+	std::vector<float> screen_xn_, screen_xo_, screen_out_;
 	double batch_ms_ = 0.0;
 	uint64_t batch_runs_ = 0;
 	// FP32 chosen form: every chain's proposal of a step is evaluated by

@@ -80,6 +80,9 @@ b3g::McmcConfig config_of(const b3g_mcmc_config *config)
 	if (config->launch > B3G_MCMC_LAUNCH_BATCH)
 		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
 	c.launch = config->launch;
+	if (config->host_threads > 256)
+		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "at most 256 host threads");
+	c.host_threads = config->host_threads;
 	return c;
 }
 

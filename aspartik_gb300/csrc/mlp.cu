@@ -190,13 +190,17 @@ __device__ __forceinline__ float dot4(float4 w, float4 x)
 	return fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, w.w * x.w)));
 }
 
+// One cluster per pair: pair k = pairs[k * stride ...], result out[k].
 __global__ void __cluster_dims__(kDeltaCluster, 1, 1) __launch_bounds__(256)
-	mlp_delta_kernel(const float *__restrict__ params, const float *pair, float *out,
-			 uint32_t in, uint32_t hidden)
+	mlp_delta_kernel(const float *__restrict__ params, const float *pairs, float *out,
+			 uint32_t in, uint32_t hidden, uint32_t stride)
 {
 	extern __shared__ __align__(16) float sh[];
 	cg::cluster_group cluster = cg::this_cluster();
 	const uint32_t rank = cluster.block_rank();
+	const uint32_t item = blockIdx.x / kDeltaCluster;
+	const float *pair = pairs + (size_t)item * stride;
+	out += item;
 	const uint32_t width_max = max(in, hidden);
 	float *a = sh;                 // [2][width] current layer (inputs first)
 	float *b = sh + 2 * width_max; // [2][hidden] next layer
@@ -339,11 +343,13 @@ Mlp::Mlp(uint32_t in_dim, uint32_t hidden, uint64_t seed, int device)
 	check_cuda(cudaMemcpy(d_params_, p.data(), bytes, cudaMemcpyHostToDevice), "params");
 	check_cuda(cudaMemset(d_m_, 0, bytes), "adam m");
 	check_cuda(cudaMemset(d_v_, 0, bytes), "adam v");
-	// inference pair and result in host-mapped memory: no copies, no
-	// stream synchronisation per screened proposal
-	check_cuda(cudaHostAlloc((void **)&h_pair_, sizeof(float) * (2 * in_ + 4),
+	// inference pairs and results in host-mapped memory: no copies, no
+	// stream synchronisation per screening; results [kDeltaMax] first,
+	// then the pairs [kDeltaMax][2 in]
+	check_cuda(cudaHostAlloc((void **)&h_pair_,
+				 sizeof(float) * kDeltaMax * (1 + 2 * in_),
 				 cudaHostAllocMapped),
-		   "mapped pair");
+		   "mapped pairs");
 	check_cuda(cudaHostGetDevicePointer((void **)&d_pair_, h_pair_, 0), "mapped pair");
 }
 
@@ -580,34 +586,53 @@ constexpr uint32_t kDeltaSentinel = 0x7fb3a5e1u;
 
 float Mlp::delta(const float *x_new, const float *x_old)
 {
-	volatile uint32_t *word = reinterpret_cast<volatile uint32_t *>(h_pair_ + 2 * in_);
-	std::memcpy(h_pair_, x_new, sizeof(float) * in_);
-	std::memcpy(h_pair_ + in_, x_old, sizeof(float) * in_);
-	*word = kDeltaSentinel;
+	float out;
+	deltas(x_new, x_old, 1, &out);
+	return out;
+}
+
+void Mlp::deltas(const float *x_new, const float *x_old, uint32_t count, float *out)
+{
+	if (count == 0)
+		return;
+	if (count > kDeltaMax)
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "too many surrogate pairs at once");
+	volatile uint32_t *words = reinterpret_cast<volatile uint32_t *>(h_pair_);
+	float *pairs = h_pair_ + kDeltaMax;
+	const uint32_t stride = 2 * in_;
+	for (uint32_t k = 0; k < count; ++k) {
+		std::memcpy(pairs + (size_t)k * stride, x_new + (size_t)k * in_,
+			    sizeof(float) * in_);
+		std::memcpy(pairs + (size_t)k * stride + in_, x_old + (size_t)k * in_,
+			    sizeof(float) * in_);
+		words[k] = kDeltaSentinel;
+	}
 	std::atomic_thread_fence(std::memory_order_seq_cst);
 	const size_t smem = sizeof(float) * 2 * (std::max(hidden_, in_) + hidden_);
-	mlp_delta_kernel<<<kDeltaCluster, 256, smem, stream_>>>(d_params_, d_pair_,
-								 d_pair_ + 2 * in_, in_, hidden_);
+	mlp_delta_kernel<<<kDeltaCluster * count, 256, smem, stream_>>>(
+		d_params_, d_pair_ + kDeltaMax, d_pair_, in_, hidden_, stride);
 	check_cuda(cudaGetLastError(), "surrogate inference");
-	// poll the mapped word; every 64 polls ask the stream, so that an error
-	// surfaces and a finished kernel that wrote nothing ends the wait
-	for (uint32_t k = 1;; ++k) {
-		uint32_t bits = *word;
+	// poll the mapped words; every 64 polls ask the stream, so that an
+	// error surfaces and a finished kernel that wrote nothing ends the wait
+	uint32_t k = 0;
+	for (uint32_t poll = 1; k < count; ++poll) {
+		uint32_t bits = words[k];
 		if (bits != kDeltaSentinel) {
-			float v;
-			std::memcpy(&v, &bits, sizeof(v));
-			return v;
+			std::memcpy(out + k, &bits, sizeof(float));
+			++k;
+			continue;
 		}
-		if ((k & 63u) == 0) {
+		if ((poll & 63u) == 0) {
 			const cudaError_t e = cudaStreamQuery(stream_);
 			if (e == cudaSuccess) {
-				bits = *word;
-				if (bits == kDeltaSentinel)
-					throw Error(B3G_ERR_CUDA,
-						    "surrogate inference finished without a result");
-				float v;
-				std::memcpy(&v, &bits, sizeof(v));
-				return v;
+				for (; k < count; ++k) {
+					bits = words[k];
+					if (bits == kDeltaSentinel)
+						throw Error(B3G_ERR_CUDA,
+							    "surrogate inference finished without a result");
+					std::memcpy(out + k, &bits, sizeof(float));
+				}
+				return;
 			}
 			if (e != cudaErrorNotReady)
 				check_cuda(e, "surrogate inference");

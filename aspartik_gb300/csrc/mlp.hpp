@@ -40,8 +40,13 @@ class Mlp {
 	float train(const float *x_new, const float *x_old, const float *delta,
 		    uint32_t n, uint32_t epochs, uint32_t batch, float lr,
 		    uint64_t seed);
-	// f(x_new) - f(x_old) for one pair (fused single-block kernel)
+	// pairs evaluated by one launch at most
+	static constexpr uint32_t kDeltaMax = 256;
+	// f(x_new) - f(x_old) for one pair (one fused cluster launch)
 	float delta(const float *x_new, const float *x_old);
+	// the same for `count` pairs, x_new and x_old [count][in], in one
+	// launch (a cluster per pair)
+	void deltas(const float *x_new, const float *x_old, uint32_t count, float *out);
 
       private:
 	void ensure_batch(uint32_t rows);

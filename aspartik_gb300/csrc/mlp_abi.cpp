@@ -143,4 +143,19 @@ B3G_API b3g_status b3g_surrogate_delta(b3g_surrogate *s, const float *x_new,
 	});
 }
 
+B3G_API b3g_status b3g_surrogate_deltas(b3g_surrogate *s, const float *x_new,
+					const float *x_old, uint32_t n,
+					float *out)
+{
+	return guarded([&] {
+		need(x_new);
+		need(x_old);
+		need(out);
+		if (n < 1 || n > b3g::Mlp::kDeltaMax)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "1..256 pairs per call");
+		mlp_of(s)->deltas(x_new, x_old, n, out);
+	});
+}
+
 } // extern "C"

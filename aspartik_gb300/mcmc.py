@@ -60,6 +60,10 @@ class McmcSettings:
     # "streams": one launch per chain on its own stream; "batch": every
     # chain of a step in one graph-replayed batched launch (FP32)
     launch: str = "streams"
+    # host threads stepping the chains (0: one for every four chains, at
+    # most 8; 1: the calling thread); the results are the same for every
+    # value
+    host_threads: int = 0
 
 
 LAUNCH = {"streams": 0, "batch": 1}
@@ -77,7 +81,7 @@ def _config(settings: McmcSettings) -> "nat.McmcConfig":
                           settings.device, (ct.c_double * nat.OP_COUNT)(*w),
                           settings.da_pilot_steps, settings.da_epochs, settings.da_hidden,
                           0, settings.da_drift_limit, settings.clock_categories,
-                          LAUNCH[settings.launch])
+                          LAUNCH[settings.launch], settings.host_threads)
 
 
 class Mcmc:

@@ -86,3 +86,12 @@ class Surrogate:
         check(lib.b3g_surrogate_delta(self._h, nat.as_ptr(xn, ct.c_float),
                                       nat.as_ptr(xo, ct.c_float), ct.byref(out)))
         return out.value
+
+    def deltas(self, x_new, x_old) -> np.ndarray:
+        """f(x_new[k]) - f(x_old[k]) for every row, one launch."""
+        xn, xo = _f32(x_new), _f32(x_old)
+        out = np.empty(xn.shape[0], np.float32)
+        check(lib.b3g_surrogate_deltas(self._h, nat.as_ptr(xn, ct.c_float),
+                                       nat.as_ptr(xo, ct.c_float), xn.shape[0],
+                                       nat.as_ptr(out, ct.c_float)))
+        return out

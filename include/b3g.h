@@ -387,6 +387,14 @@ typedef struct b3g_mcmc_config {
 	 * (b3g_batch_*: one staging copy, one persistent launch for the
 	 * members' short lists, one for the long ones, one read-back). */
 	uint32_t launch;
+	/* Host threads that step the chains, chain i on thread i % threads:
+	 * each proposes and launches its chains' evaluations, then reads
+	 * their results; statistics are gathered in chain order, so the
+	 * results are the same for every value.  0 = one for every four
+	 * chains, at most 8 and at most the hardware threads; 1 = the calling
+	 * thread alone (the environment variable B3G_MCMC_THREADS overrides
+	 * it).  The batched launch mode steps on the calling thread. */
+	uint32_t host_threads;
 } b3g_mcmc_config;
 
 enum { B3G_MCMC_LAUNCH_STREAMS = 0, B3G_MCMC_LAUNCH_BATCH = 1 };
@@ -521,9 +529,16 @@ B3G_API b3g_status b3g_surrogate_train(b3g_surrogate *s, const float *x_new,
 				       uint32_t n, uint32_t epochs,
 				       uint32_t batch, float lr, uint64_t seed,
 				       float *final_loss);
-/* f(x_new) - f(x_old) for one pair (fused single-block kernel). */
+/* f(x_new) - f(x_old) for one pair (one fused launch: a cluster of 8
+ * blocks holds the hidden layers in distributed shared memory). */
 B3G_API b3g_status b3g_surrogate_delta(b3g_surrogate *s, const float *x_new,
 				       const float *x_old, float *out);
+/* The same for n pairs (1..256) in one launch, a cluster per pair; x_new
+ * and x_old [n][inputs], out[n].  The MCMC driver screens every chain's
+ * proposal of a step with one call. */
+B3G_API b3g_status b3g_surrogate_deltas(b3g_surrogate *s, const float *x_new,
+					const float *x_old, uint32_t n,
+					float *out);
 
 /* ---- allocation-free pruning --------------------------------------------
  * This entry point has no counterpart in the reference.

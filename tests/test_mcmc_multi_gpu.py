@@ -70,3 +70,40 @@ def test_problems_must_divide_the_chains():
     s = McmcSettings(model="gtr", precision="f32", num_categories=4, num_chains=5)
     with pytest.raises(B3GError):
         Mcmc.multi(problems(), s)
+
+
+@pytest.mark.parametrize("launch,da", [("streams", 0), ("streams", 300), ("batch", 0)])
+def test_host_threads_leave_the_results_unchanged(launch, da):
+    """The same run on the calling thread alone and on three or eight host
+    threads (chain i on thread i % threads): every chain's trace, the cold
+    chain's samples, the operator, swap and delayed-acceptance statistics
+    are identical."""
+    from aspartik_gb300.mcmc import Mcmc, McmcSettings
+
+    c = dna_case(20, 400, seed=41, model="gtr", alpha=0.5, num_categories=4,
+                 root_height=0.7)
+    runs = []
+    for threads in (1, 3, 8):
+        s = McmcSettings(model="gtr", precision="f32", num_categories=4, num_chains=8,
+                         heat=0.05, swap_every=7, seed=13, sample_every=5, tune_every=200,
+                         launch=launch, host_threads=threads, da_pilot_steps=da,
+                         da_epochs=5, da_hidden=64)
+        m = Mcmc(c.leaves, c.weights, c.tree.parents, c.tree.heights, s)
+        m.set_parameters(rates=np.ones(6), frequencies=np.full(4, 0.25), alpha=0.5,
+                         birth_rate=1.0)
+        m.run(1500)
+        assert m.check() < 1e-12
+        runs.append(dict(traces=[m.trace("lnl", chain=i) for i in range(8)],
+                         heights=m.samples()["heights"], ops=m.operator_stats(),
+                         swaps=m.swaps(), da=m.da_stats()))
+        m.close()
+    base = runs[0]
+    if da:
+        assert base["da"]["pilot_pairs"] > 0
+    for other in runs[1:]:
+        for a, b in zip(base["traces"], other["traces"]):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(base["heights"], other["heights"])
+        assert base["ops"] == other["ops"]
+        assert base["swaps"] == other["swaps"]
+        assert base["da"] == other["da"]

@@ -58,6 +58,23 @@ def test_fused_pair_kernel_matches_forward(rng, hidden):
         assert d == pytest.approx(ref[0] - ref[1], rel=1e-4, abs=1e-5)
 
 
+@pytest.mark.parametrize("count", [1, 5, 256])
+def test_batched_pairs_match_single_pairs(rng, count):
+    """One launch over `count` pairs (a cluster per pair) gives, pair by
+    pair, the single-pair launch's bits; more than 256 pairs are refused."""
+    from aspartik_gb300._native import B3GError
+
+    s = net(seed=5, hidden=256)
+    xn = rng.normal(size=(count, INPUTS)).astype(np.float32)
+    xo = rng.normal(size=(count, INPUTS)).astype(np.float32)
+    d = s.deltas(xn, xo)
+    assert d.shape == (count,)
+    for k in range(0, count, max(1, count // 9)):
+        assert d[k] == s.delta(xn[k], xo[k])
+    with pytest.raises(B3GError):
+        s.deltas(np.zeros((257, INPUTS), np.float32), np.zeros((257, INPUTS), np.float32))
+
+
 def test_training_learns_a_difference_function(rng):
     """delta = g(x_new) - g(x_old) for a smooth g: the trained network's
     differences explain most of the variance."""
