@@ -425,31 +425,24 @@ __device__ double tile_root(const TileArgs &a, uint32_t t, const float *s_dot,
 	return tsum;
 }
 
-// Sum `count` doubles at `sums` in a fixed order: strided per thread,
-// then a warp-shuffle tree and the warps' sums in a second tree.  The
-// result is returned in thread 0; s_red holds blockDim.x / 32 doubles.
-// Pairwise FP64 over a few hundred block sums loses nothing at the FP32
-// form's accuracy, and keeps the serial tail of the launch to ~14
-// dependent FP64 adds (the pipe runs at 1/64 of the FP32 rate here).
+// Sum `count` doubles at `sums` in a fixed order: lane l of warp 0 adds
+// entries l, l + 32, ... in order, then a warp-shuffle tree.  The result is
+// returned in thread 0; no barrier, so only warp 0 needs to call it (s_red
+// is unused).  Pairwise FP64 over a few hundred block sums loses nothing at
+// the FP32 form's accuracy, and keeps the serial tail of the launch to a
+// few dependent FP64 adds (the pipe runs at 1/64 of the FP32 rate here).
 __device__ double block_fold(const double *sums, uint32_t count, double *s_red)
 {
-	const uint32_t tid = threadIdx.x, nwarps = blockDim.x >> 5;
+	(void)s_red;
+	const uint32_t tid = threadIdx.x;
+	if (tid >= 32)
+		return 0.0;
 	double sum = 0.0;
-	for (uint32_t k = tid; k < count; k += blockDim.x)
+	for (uint32_t k = tid; k < count; k += 32)
 		sum += __ldcg(sums + k);
 	for (int off = 16; off > 0; off >>= 1)
 		sum += __shfl_down_sync(0xffffffffu, sum, off);
-	if ((tid & 31u) == 0)
-		s_red[tid >> 5] = sum;
-	__syncthreads();
-	double total = 0.0;
-	if (tid < 32) {
-		total = tid < nwarps ? s_red[tid] : 0.0;
-		for (int off = 16; off > 0; off >>= 1)
-			total += __shfl_down_sync(0xffffffffu, total, off);
-	}
-	__syncthreads();
-	return total;
+	return sum;
 }
 
 // shared memory (byte offsets as prune4_runs_smem computes them):

@@ -522,10 +522,15 @@ def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
                                (trained on the GPU) screens the moves that
                                re-evaluate the whole tree
       chosen_f32_da_replicates the chosen form in full: 8 independent
-                               replicates stepping together (all chains'
-                               evaluations of a step queued before any
-                               result is read) with delayed acceptance,
-                               chosen_steps / 7.5 steps, multi-chain ESS
+                               replicates stepping together (the step's
+                               screened proposals through one surrogate
+                               launch, then all chains' evaluations queued
+                               before any result is read) with delayed
+                               acceptance (pilot: the first 1/16 of the
+                               steps), chosen_steps / 3.75 steps (each
+                               chain long enough that the multi-chain ESS,
+                               which counts the chains' disagreement, is
+                               not dominated by it), multi-chain ESS
     Moves: the driver's GTR mix (tree scale 3, subtree slide 30, narrow
     exchange 30, wide exchange 3, root slide 3, node slide 30, up-down 3,
     alpha scale 1, birth-rate scale 3, delta exchange of rates 1 and of
@@ -542,9 +547,9 @@ def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
     out["chosen_f32_da"] = mcmc_arm(wl, start, tunings, "f32", chosen_steps, device,
                                     da_pilot=min(100_000, chosen_steps // 5))
     progress("MCMC delayed-acceptance arm")
-    rep = int(chosen_steps / 7.5)
+    rep = int(chosen_steps / 3.75)
     out["chosen_f32_da_replicates"] = mcmc_arm(wl, start, tunings, "f32", rep, device,
-                                               chains=8, da_pilot=rep // 8)
+                                               chains=8, da_pilot=rep // 16)
     progress("MCMC replicates arm")
     base = max(out["plain_f64"]["ess_per_s"], 1e-12)
     for arm in ("chosen_f32", "chosen_f32_da", "chosen_f32_da_replicates"):
@@ -641,7 +646,8 @@ def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
     leg.  Run once per launch mode: every chain's evaluations of a step in
     one graph replay of the batched kernels (one staging copy, the run walk
     for long lists, the batched short-list kernel, one read-back), or one
-    launch per chain on its own stream.  Wall time per step and, batched,
+    launch per chain on its own stream, the chains spread over host threads
+    (one for every four chains, at most 8).  Wall time per step and, batched,
     the graph's device time per step (CUDA events); ESS of the cold chain of
     the first alignment (lnL, root height, first exchangeability)."""
     from aspartik_gb300.ess import min_ess
@@ -649,7 +655,8 @@ def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
 
     probs = c4_problems()
     out = {"problems": [{k: p[k] for k in ("taxa", "sites", "patterns")} for p in probs],
-           "chains": temps * len(probs), "temperatures": temps, "steps": steps}
+           "chains": temps * len(probs), "temperatures": temps, "steps": steps,
+           "host_threads_streams": min((temps * len(probs) + 3) // 4, 8, os.cpu_count() or 1)}
     for launch in ("batch", "streams"):
         s = McmcSettings(model="gtr", precision="f32", num_categories=4,
                          num_chains=temps * len(probs), heat=0.1, swap_every=10, seed=4,
@@ -1060,7 +1067,7 @@ def main():
     ap.add_argument("--no-protein", action="store_true", help="skip the 20-state leg")
     ap.add_argument("--mcmc-steps", type=int, default=1_500_000,
                     help="steps of the chosen-form MCMC arms of the ESS/s comparison; the "
-                         "plain arm runs 0.4x, burn-in and replicates 1/7.5x (0 = skip the "
+                         "plain arm runs 0.4x, burn-in 1/7.5x and replicates 1/3.75x (0 = skip the "
                          "MCMC legs and the smaller configurations)")
     args = ap.parse_args()
     if args.warmup < 3:
