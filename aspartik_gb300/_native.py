@@ -213,6 +213,11 @@ SIGNATURES = {
     "b3g_mcmc_swaps": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_dump": (ct.c_int, [_vp, _u8p, ct.c_uint64, ct.POINTER(ct.c_uint64)]),
     "b3g_mcmc_load": (ct.c_int, [_vp, _u8p, ct.c_uint64]),
+    "b3g_mcmc_dump_verbatim": (ct.c_int, [_vp, ct.c_uint32, _u32p, ct.c_uint32, _u32p,
+                                          ct.c_uint32, _u8p, ct.c_uint64,
+                                          ct.POINTER(ct.c_uint64)]),
+    "b3g_mcmc_load_verbatim": (ct.c_int, [_vp, ct.c_uint32, _u32p, ct.c_uint32, _u32p,
+                                          ct.c_uint32, _u8p, ct.c_uint64]),
     "b3g_mcmc_check": (ct.c_int, [_vp, _f64p]),
     "b3g_mcmc_da_stats": (ct.c_int, [_vp, ct.POINTER(ct.c_uint64), _f64p]),
     "b3g_mcmc_chain_state": (ct.c_int, [_vp, ct.c_uint32, _u32p, _f64p, _f64p, _f64p]),

@@ -125,6 +125,28 @@ enum : uint32_t {
 	kLaunchBatch = 1,   // every chain of a step in one graph-replayed batch
 };
 
+// Parameters of a state file in the reference's layout (Mcmc::dump,
+// crates/b3/src/mcmc.rs:251-268), in the order its Mcmc lists them.
+enum VerbatimParam : uint32_t {
+	kVpTree = 0,         // DatedTree: parents, heights (tree.rs:1012-1016)
+	kVpBirthRate,        // Real: f64 (real.rs:59-62)
+	kVpKappa,            // Real
+	kVpAlpha,            // Real
+	kVpRates,            // RealVector: 6 f64 (real_vector.rs:77-82)
+	kVpFreqs,            // RealVector: 4 f64
+	kVpClockSd,          // Real
+	kVpClockCategories,  // ClassVector: u32 per node (class_vector.rs:82-87)
+	kVpCount
+};
+
+// One operator of the reference's scheduler: which of this driver's
+// operator kinds it is, and whether it has a tuning parameter (its dump then
+// carries one, operators/mod.rs:208-219).
+struct VerbatimOp {
+	uint32_t op;
+	uint32_t has_tuning;
+};
+
 struct McmcConfig {
 	uint32_t num_chains;
 	uint32_t num_categories;
@@ -270,6 +292,17 @@ class Mcmc {
 	// data and continues bit for bit as the dumped run would have.
 	std::vector<uint8_t> dump() const;
 	void load(const uint8_t *state, size_t size);
+	// A state in the reference's own layout (mcmc_verbatim.cpp) for one
+	// chain: its parameters in the order `params` gives, the operators'
+	// statistics and tunings in the order `ops` gives, the step and the
+	// chain's posterior; load takes such a state (written by either) into
+	// the chain and the driver's step and operators, and re-evaluates.
+	std::vector<uint8_t> dump_verbatim(uint32_t chain, const uint32_t *params,
+					   uint32_t num_params, const VerbatimOp *ops,
+					   uint32_t num_ops) const;
+	void load_verbatim(uint32_t chain, const uint32_t *params,
+			   uint32_t num_params, const VerbatimOp *ops,
+			   uint32_t num_ops, const uint8_t *state, size_t size);
 
       private:
 	void propose(Chain &ch);

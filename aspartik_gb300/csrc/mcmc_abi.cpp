@@ -308,6 +308,56 @@ B3G_API b3g_status b3g_mcmc_load(b3g_mcmc *mcmc, const uint8_t *state,
 	return guarded([&] { mcmc_of(mcmc)->load(state, (size_t)size); });
 }
 
+static_assert(sizeof(b3g_state_operator) == sizeof(b3g::VerbatimOp),
+	      "b3g_state_operator mirrors VerbatimOp");
+static_assert(B3G_STATE_TREE == b3g::kVpTree &&
+		      B3G_STATE_BIRTH_RATE == b3g::kVpBirthRate &&
+		      B3G_STATE_KAPPA == b3g::kVpKappa &&
+		      B3G_STATE_ALPHA == b3g::kVpAlpha &&
+		      B3G_STATE_RATES == b3g::kVpRates &&
+		      B3G_STATE_FREQUENCIES == b3g::kVpFreqs &&
+		      B3G_STATE_CLOCK_SD == b3g::kVpClockSd &&
+		      B3G_STATE_CLOCK_CATEGORIES == b3g::kVpClockCategories,
+	      "state parameter ids");
+
+B3G_API b3g_status b3g_mcmc_dump_verbatim(b3g_mcmc *mcmc, uint32_t chain,
+					  const uint32_t *params,
+					  uint32_t num_params,
+					  const b3g_state_operator *ops,
+					  uint32_t num_ops, uint8_t *out,
+					  uint64_t capacity, uint64_t *size)
+{
+	return guarded([&] {
+		if (!size)
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "null size");
+		const std::vector<uint8_t> state = mcmc_of(mcmc)->dump_verbatim(
+			chain, params, num_params,
+			reinterpret_cast<const b3g::VerbatimOp *>(ops), num_ops);
+		*size = state.size();
+		if (!out)
+			return;
+		if (capacity < state.size())
+			throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
+					 "buffer smaller than the state");
+		std::memcpy(out, state.data(), state.size());
+	});
+}
+
+B3G_API b3g_status b3g_mcmc_load_verbatim(b3g_mcmc *mcmc, uint32_t chain,
+					  const uint32_t *params,
+					  uint32_t num_params,
+					  const b3g_state_operator *ops,
+					  uint32_t num_ops, const uint8_t *state,
+					  uint64_t size)
+{
+	return guarded([&] {
+		mcmc_of(mcmc)->load_verbatim(
+			chain, params, num_params,
+			reinterpret_cast<const b3g::VerbatimOp *>(ops), num_ops, state,
+			(size_t)size);
+	});
+}
+
 B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff)
 {
 	return guarded([&] {

@@ -5,7 +5,9 @@
 // tag, a protocol version, the current step, the posterior, every
 // parameter, the scheduler and the RNG.  This driver's state differs from
 // the reference's (its own operators, xoshiro256** RNGs, several chains), so
-// the layout is its own; it holds everything later steps depend on:
+// this exact checkpoint has its own layout (mcmc_verbatim.cpp writes and
+// reads one chain in the reference's); it holds everything later steps
+// depend on:
 //
 //   "B3GMCST1", u32 version = 2, u32 chains, leaves, model, categories,
 //   clock categories, precision, reserved

@@ -20,6 +20,9 @@ OPERATORS = ["tree_scale", "subtree_slide", "narrow_exchange", "scale_kappa",
              "scale_alpha", "scale_birth_rate", "delta_rates", "delta_frequencies",
              "relaxed_category", "scale_clock_sd", "node_slide", "root_slide", "up_down",
              "wide_exchange"]
+# parameters of a state file in the reference's layout (B3G_STATE_*)
+STATE_PARAMETERS = ["tree", "birth_rate", "kappa", "alpha", "rates", "frequencies",
+                    "clock_sd", "clock_categories"]
 TRACE_FIELDS = ["lnl", "prior", "posterior", "root_height", "kappa_or_rate0", "alpha",
                 "tree_length", "clock_sd"]
 
@@ -249,6 +252,39 @@ class Mcmc:
         buf = np.frombuffer(state, dtype=np.uint8)
         check(lib.b3g_mcmc_load(self._h, nat.as_ptr(np.ascontiguousarray(buf), ct.c_uint8),
                                 buf.size))
+
+    @staticmethod
+    def _state_layout(parameters, operators):
+        params = nat.u32([STATE_PARAMETERS.index(p) for p in parameters])
+        ops = nat.u32([[OPERATORS.index(name), int(bool(tuned))]
+                       for name, tuned in operators]).reshape(-1)
+        return params, ops
+
+    def dump_verbatim(self, parameters, operators, chain: int = 0) -> bytes:
+        """One chain's state in the reference's state-file layout
+        (b3g_mcmc_dump_verbatim): `parameters` in the reference Mcmc's
+        order (names of STATE_PARAMETERS), `operators` in its scheduler's
+        order as (OPERATORS name, has a tuning) pairs."""
+        params, ops = self._state_layout(parameters, operators)
+        size = ct.c_uint64()
+        args = (self._h, chain, nat.as_ptr(params, ct.c_uint32), params.size,
+                nat.as_ptr(ops, ct.c_uint32), ops.size // 2)
+        check(lib.b3g_mcmc_dump_verbatim(*args, None, 0, ct.byref(size)))
+        buf = np.empty(size.value, dtype=np.uint8)
+        check(lib.b3g_mcmc_dump_verbatim(*args, nat.as_ptr(buf, ct.c_uint8), size.value,
+                                         ct.byref(size)))
+        return buf.tobytes()
+
+    def load_verbatim(self, state: bytes, parameters, operators, chain: int = 0) -> None:
+        """Take a state in the reference's layout into one chain (and the
+        driver's step and operator statistics), re-evaluating it
+        (b3g_mcmc_load_verbatim)."""
+        params, ops = self._state_layout(parameters, operators)
+        buf = np.ascontiguousarray(np.frombuffer(state, dtype=np.uint8))
+        check(lib.b3g_mcmc_load_verbatim(self._h, chain, nat.as_ptr(params, ct.c_uint32),
+                                         params.size, nat.as_ptr(ops, ct.c_uint32),
+                                         ops.size // 2, nat.as_ptr(buf, ct.c_uint8),
+                                         buf.size))
 
     def check(self) -> float:
         out = ct.c_double()

@@ -493,6 +493,49 @@ B3G_API b3g_status b3g_mcmc_dump(b3g_mcmc *mcmc, uint8_t *out,
 				 uint64_t capacity, uint64_t *size);
 B3G_API b3g_status b3g_mcmc_load(b3g_mcmc *mcmc, const uint8_t *state,
 				 uint64_t size);
+
+/* State files in the reference's own layout (Mcmc::dump_state /
+ * load_state, crates/b3/src/mcmc.rs:175-219, 251-268, written through
+ * crates/verbatim: little-endian values padded to their size, slices with a
+ * u32 length): tag 62 33 b3 44, u32 version 19, u64 step, f64 posterior,
+ * the parameters in the reference Mcmc's order, each operator's u32
+ * accepts and rejects since its last tuning and its f64 tuning if it has
+ * one, the RNG as two u128 values.  The caller gives the reference
+ * configuration's parameter order (B3G_STATE_*) and operator order (this
+ * driver's B3G_OP_* kind of each, and whether it is tuned).  One chain's
+ * parameters; the step and the operators' statistics and tunings are the
+ * driver's.  The RNG section carries this driver's xoshiro256** words on
+ * dump and reseeds the chain's generator on load (the reference's PCG64
+ * stream is not reproduced); b3g_mcmc_dump is the exact checkpoint.  Load
+ * re-evaluates the chain (likelihood and priors) and accepts, as
+ * load_state does; a state of another version, tag, tree size or with
+ * bytes left after its RNG is refused with nothing changed. */
+enum {
+	B3G_STATE_TREE = 0,             /* u32 parents slice, f64 heights slice */
+	B3G_STATE_BIRTH_RATE = 1,       /* f64 */
+	B3G_STATE_KAPPA = 2,            /* f64 (HKY) */
+	B3G_STATE_ALPHA = 3,            /* f64 (Gamma categories) */
+	B3G_STATE_RATES = 4,            /* 6 f64 (GTR) */
+	B3G_STATE_FREQUENCIES = 5,      /* 4 f64 */
+	B3G_STATE_CLOCK_SD = 6,         /* f64 (relaxed clock) */
+	B3G_STATE_CLOCK_CATEGORIES = 7  /* u32 per node (relaxed clock) */
+};
+typedef struct b3g_state_operator {
+	uint32_t op;         /* B3G_OP_* */
+	uint32_t has_tuning; /* 0 or 1 */
+} b3g_state_operator;
+B3G_API b3g_status b3g_mcmc_dump_verbatim(b3g_mcmc *mcmc, uint32_t chain,
+					  const uint32_t *params,
+					  uint32_t num_params,
+					  const b3g_state_operator *ops,
+					  uint32_t num_ops, uint8_t *out,
+					  uint64_t capacity, uint64_t *size);
+B3G_API b3g_status b3g_mcmc_load_verbatim(b3g_mcmc *mcmc, uint32_t chain,
+					  const uint32_t *params,
+					  uint32_t num_params,
+					  const b3g_state_operator *ops,
+					  uint32_t num_ops, const uint8_t *state,
+					  uint64_t size);
 /* Re-evaluates every chain from scratch and returns the largest relative
  * difference to its incrementally maintained log-likelihood. */
 B3G_API b3g_status b3g_mcmc_check(b3g_mcmc *mcmc, double *max_rel_diff);

@@ -85,3 +85,128 @@ def test_bad_checkpoints_are_refused():
     assert e.value.status == B3G_ERR_STATE
     for m in (a, b, other, da):
         m.close()
+
+
+# A reference configuration's order: GTR + Gamma with a Yule tree
+# (parameters as python/aspartik/b3/config lists them for such a run) and
+# its scheduler's operators with their tuning flags.
+GTR_PARAMS = ["birth_rate", "rates", "frequencies", "alpha", "tree"]
+CLOCK_PARAMS = ["birth_rate", "rates", "frequencies", "alpha", "clock_sd",
+                "clock_categories", "tree"]
+OPS = [("tree_scale", True), ("subtree_slide", True), ("narrow_exchange", False),
+       ("wide_exchange", False), ("node_slide", False), ("root_slide", True),
+       ("up_down", True), ("scale_alpha", True), ("scale_birth_rate", True),
+       ("delta_rates", True), ("delta_frequencies", True)]
+
+
+def parse_state(state: bytes, params, ops, nodes):
+    from tests.verbatim_ref import STATE_TAG, STATE_VERSION, Reader
+
+    r = Reader(state)
+    assert r.tag(4) == STATE_TAG
+    assert r.prim("u32") == STATE_VERSION
+    out = {"step": r.prim("u64"), "posterior": r.prim("f64")}
+    sizes = {"rates": 6, "frequencies": 4, "clock_categories": nodes}
+    for p in params:
+        if p == "tree":
+            out["parents"] = r.slice("u32")
+            out["heights"] = r.slice("f64")
+        elif p == "clock_categories":
+            out[p] = [r.prim("u32") for _ in range(nodes)]
+        elif p in sizes:
+            out[p] = [r.prim("f64") for _ in range(sizes[p])]
+        else:
+            out[p] = r.prim("f64")
+    out["ops"] = []
+    for _, tuned in ops:
+        a, rj = r.prim("u32"), r.prim("u32")
+        out["ops"].append((a, rj, r.prim("f64") if tuned else None))
+    out["rng"] = (r.u128(), r.u128())
+    assert r.left() == 0
+    return out
+
+
+@pytest.mark.parametrize("clock", [0, 4])
+def test_reference_layout_state_round_trip(clock):
+    """A chain's state in the reference's state-file layout: the bytes parse
+    under the restated reference reader with the chain's tree, parameters,
+    step, posterior and operator tunings; a fresh driver that loads them
+    holds the same tree and parameters, re-evaluates the same likelihood,
+    and keeps stepping with its incremental likelihood exact."""
+    from aspartik_gb300.mcmc import OPERATORS
+
+    c = dna_case(18, 500, seed=35, model="gtr", alpha=0.5, num_categories=4)
+    params = CLOCK_PARAMS if clock else GTR_PARAMS
+    ops = OPS + ([("relaxed_category", False), ("scale_clock_sd", True)] if clock else [])
+    a = fresh(c, clock, precision="f32")
+    a.run(600)  # a multiple of sample_every: the last sample is the state
+    state = a.dump_verbatim(params, ops)
+    nodes = c.tree.parents.size
+    st = parse_state(state, params, ops, nodes)
+    par, hei, lnl, _ = a.chain_state(0)
+    smp = a.samples()
+    assert st["step"] == 600
+    assert st["parents"] == list(par) and st["heights"] == list(hei)
+    assert st["posterior"] == pytest.approx(a.trace("posterior")[-1], rel=0, abs=0)
+    assert st["rates"] == list(smp["rates"][-1])
+    assert st["frequencies"] == list(smp["frequencies"][-1])
+    assert st["alpha"] == smp["alpha"][-1] and st["birth_rate"] == smp["birth_rate"][-1]
+    if clock:
+        assert st["clock_sd"] == smp["clock_sd"][-1]
+        assert max(v for i, v in enumerate(st["clock_categories"])
+                   if par[i] != 0xFFFFFFFF) < clock
+    stats = a.operator_stats()
+    for (name, tuned), (acc, rej, tuning) in zip(ops, st["ops"]):
+        assert acc + rej <= stats[name]["accepts"] + stats[name]["rejects"]
+        if tuned:
+            assert tuning == stats[name]["tuning"]
+
+    b = fresh(c, clock, precision="f32")
+    b.load_verbatim(state, params, ops)
+    pb, hb, lb, _ = b.chain_state(0)
+    assert np.array_equal(pb, par) and np.array_equal(hb, hei)
+    assert lb == pytest.approx(lnl, rel=1e-12)  # a whole-tree evaluation
+    again = b.dump_verbatim(params, ops)
+    # all but the posterior (re-evaluated) and the RNG words (reseeded)
+    assert again[:16] == state[:16] and again[24:-32] == state[24:-32]
+    for name, tuned in ops:
+        if tuned:
+            assert b.operator_stats()[name]["tuning"] == stats[name]["tuning"]
+    b.run(300)
+    assert b.check() < 1e-12
+    assert b.dump_verbatim(params, ops)[8:16] == (900).to_bytes(8, "little")
+    assert OPERATORS  # the names used above are the driver's
+    a.close()
+    b.close()
+
+
+def test_reference_layout_states_that_do_not_fit_are_refused():
+    """Version 7 in byte 4 (the reference's own version test), a foreign
+    tag, a parameter list longer or shorter than the writer's, a tree of
+    another size and a short state are refused, and the driver is unchanged."""
+    c = dna_case(14, 300, seed=36, model="gtr", alpha=0.5, num_categories=4)
+    a = fresh(c, precision="f32")
+    a.run(100)
+    state = a.dump_verbatim(GTR_PARAMS, OPS)
+    b = fresh(c, precision="f32")
+    before = b.chain_state(0)
+    v7 = state[:4] + b"\x07" + state[5:]
+    with pytest.raises(B3GError, match="protocol version v7 is incompatible"):
+        b.load_verbatim(v7, GTR_PARAMS, OPS)
+    for bad, params in ((b"XXXX" + state[4:], GTR_PARAMS), (state, GTR_PARAMS[:-1]),
+                        (state, GTR_PARAMS + ["birth_rate"]), (state[:-40], GTR_PARAMS),
+                        (state + b"\0" * 8, GTR_PARAMS)):
+        with pytest.raises(B3GError) as e:
+            b.load_verbatim(bad, params, OPS)
+        assert e.value.status == B3G_ERR_INVALID_ARGUMENT
+    small = dna_case(10, 300, seed=37, model="gtr", alpha=0.5, num_categories=4)
+    s = fresh(small, precision="f32")
+    with pytest.raises(B3GError) as e:
+        s.load_verbatim(state, GTR_PARAMS, OPS)
+    assert e.value.status == B3G_ERR_INVALID_ARGUMENT
+    after = b.chain_state(0)
+    assert np.array_equal(before[0], after[0]) and before[2] == after[2]
+    with pytest.raises(B3GError):
+        a.dump_verbatim(["kappa"], [])  # kappa belongs to HKY chains
+    for m in (a, b, s):
+        m.close()
