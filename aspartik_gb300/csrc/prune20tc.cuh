@@ -209,15 +209,26 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 
 	// Inputs of entry e, copied by thread 0 of the group: an internal
 	// side's 128 partial rows (contiguous) into its A-lo block, where they
-	// wait to be split, and its operand blocks into its B blocks; a tip
-	// side's table into its B blocks.
+	// wait to be split, its 128 scale exponents and its operand blocks into
+	// its B blocks; a tip side's table into its B blocks and, unless the
+	// tile's codes sit in shared memory, its 128 tip codes.  Exponents and
+	// codes land in the right A-hi block (scales at bytes [512 + 512 j,
+	// 1024 + 512 j), codes at [1536 + 128 j, 1664 + 128 j)): it is free
+	// from the MMAs' end, when the next entry's copies are issued, to the
+	// split, which reads them into registers first (the output rows pass
+	// through the left A-hi block meanwhile).  Its first 128 bytes stay
+	// clear: the left A-lo block's padded K chunk reads them, and exponent
+	// bits could be NaNs.  So no global load waits on the entry's path.
+	uint8_t *sSide = reinterpret_cast<uint8_t *>(sA + 2 * kTcA);
 	auto issue = [&](uint32_t e) {
 		const NodeOp op = ops[e];
 		const uint32_t ids[2] = {op.left, op.right};
 		uint32_t bytes = 0;
 #pragma unroll
 		for (uint32_t j = 0; j < 2; j++)
-			bytes += (ids[j] & kTipBit) ? kTipBytes : kRowBytes + kOpBytes;
+			bytes += (ids[j] & kTipBit)
+					 ? kTipBytes + (prm.tips_smem ? 0u : kTcRows)
+					 : kRowBytes + kOpBytes + kTcRows * 4u;
 		tc::mbar_expect_tx(lb, bytes);
 #pragma unroll
 		for (uint32_t j = 0; j < 2; j++) {
@@ -225,11 +236,18 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 			const uint32_t bdst = tc::smem_u32(sB + j * 2 * kTcB);
 			if (ids[j] & kTipBit) {
 				tc::bulk_g2s(bdst, prm.tab + tid_tab * (S + 1) * S, kTipBytes, lb);
+				if (!prm.tips_smem)
+					tc::bulk_g2s(tc::smem_u32(sSide + 1536 + 128 * j),
+						     prm.tips + (size_t)(ids[j] & ~kTipBit) * prm.ldp +
+							     tile * kTcRows,
+						     kTcRows, lb);
 			} else {
 				const Idx ix0 = (Idx)ids[j] * stride + col0;
 				tc::bulk_g2s(tc::smem_u32(sA + (2 * j + 1) * kTcA),
 					     prm.partials + (size_t)ix0 * S, kRowBytes, lb);
 				tc::bulk_g2s(bdst, prm.tc_tab + tid_tab * 2 * kTcB, kOpBytes, lb);
+				tc::bulk_g2s(tc::smem_u32(sSide + 512 + 512 * j), prm.scales + ix0,
+					     kTcRows * 4u, lb);
 			}
 		}
 	};
@@ -273,12 +291,12 @@ __global__ void __launch_bounds__(128 * kG, 4 / kG) prune20tc_kernel(Tc20Params 
 					const uint32_t leaf = ids[j] & ~kTipBit;
 					const uint32_t code =
 						prm.tips_smem ? sTips[leaf * kTcRows + t]
-							      : prm.tips[(size_t)leaf * prm.ldp + p];
+							      : sSide[1536 + 128 * j + t];
 					row = sB + j * 2 * kTcB + min(code, (uint32_t)S) * S;
 					sc[j] = 0;
 				} else {
 					row = sA + (2 * j + 1) * kTcA + t * S;
-					sc[j] = prm.scales[(Idx)ids[j] * stride + col];
+					sc[j] = reinterpret_cast<const int32_t *>(sSide + 512 + 512 * j)[t];
 				}
 				const float4 *r4 = reinterpret_cast<const float4 *>(row);
 #pragma unroll
