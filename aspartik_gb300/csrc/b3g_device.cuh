@@ -74,6 +74,9 @@ struct PruneParams {
 	unsigned *ticket;   // zero between launches
 	double *lnl_out;    // [1]
 	double *lnl_host;   // host-mapped word that also receives it, or null
+	// host-mapped [gridDim.x], or null: each block writes its sum there and
+	// the host folds them (no ticket, no last-block fold, no lnl_out)
+	double *sums_host;
 	uint32_t n;
 	uint32_t ldp;
 	uint32_t C;
@@ -178,6 +181,9 @@ struct DirectParams {
 	unsigned *ticket;   // zero between launches
 	double *lnl_out;    // device copy of the result
 	double *lnl_host;   // host-mapped pinned word, written by the last block
+	// host-mapped [gridDim.x], or null: each block writes its sum there and
+	// the host folds them (then lnl_out and lnl_host are not written)
+	double *sums_host;
 	uint32_t n, ldp, L, C; // C: 1, 2 or 4 categories
 	double clock_rate;
 	double log_inv_c;

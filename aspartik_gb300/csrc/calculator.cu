@@ -242,6 +242,14 @@ Calculator::Calculator(const b3g_config &cfg, const uint8_t *samples)
 			   "pinned lnl");
 		check_cuda(cudaHostGetDevicePointer((void **)&d_lnl_host_, h_lnl_, 0),
 			   "mapped lnl");
+		if (f32_ && S_ == 4) {
+			check_cuda(cudaHostAlloc((void **)&h_bsums_,
+						 block_sums_cap_ * sizeof(double),
+						 cudaHostAllocMapped),
+				   "pinned block sums");
+			check_cuda(cudaHostGetDevicePointer((void **)&d_bsums_, h_bsums_, 0),
+				   "mapped block sums");
+		}
 
 		// DNA: single bases -> 0..3, everything else -> unknown (4)
 		// (cpu4.rs:117-124).  Protein: states 0..19 as given, anything
@@ -325,6 +333,8 @@ void Calculator::release()
 	own_h_stage_ = nullptr;
 	cudaFreeHost(h_model_);
 	cudaFreeHost(h_lnl_);
+	cudaFreeHost(h_bsums_);
+	h_bsums_ = d_bsums_ = nullptr;
 	d_tips_ = nullptr;
 	d_partials_ = nullptr;
 	d_scales_ = nullptr;
@@ -527,6 +537,7 @@ uint32_t Calculator::assign_slots(uint32_t n, uint32_t capacity)
 void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 			bool want_cat)
 {
+	host_fold_blocks_ = 0;
 	if (use_direct_ && !matrices_mode && !want_cat && n > 0 &&
 	    n <= kDirectMax) {
 		launch_direct(n, clock_rate);
@@ -658,9 +669,14 @@ void Calculator::launch(uint32_t n, bool matrices_mode, double clock_rate,
 		const uint32_t ctas = std::min(tiles, num_sms_ * (1024 / block));
 		if (ctas > block_sums_cap_)
 			throw Error(B3G_ERR_STATE, "run walk grid exceeds the block sums");
-		// the result also goes straight to the mapped host word
-		pp.lnl_host = d_lnl_host_;
-		arm_poll();
+		// the blocks' sums go straight to mapped host memory
+		if (d_bsums_) {
+			pp.sums_host = d_bsums_;
+			arm_host_fold(ctas);
+		} else {
+			pp.lnl_host = d_lnl_host_;
+			arm_poll();
+		}
 		check_cuda(launch_prune4_runs(pp, ctas, block, stream_), "pruning kernel");
 	} else {
 		poll_result_ = false;
@@ -819,6 +835,7 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	dp.ticket = d_ticket_;
 	dp.lnl_out = d_lnl_;
 	dp.lnl_host = d_lnl_host_;
+	dp.sums_host = d_bsums_;
 	dp.n = n;
 	dp.ldp = ldp_;
 	dp.L = L_;
@@ -870,7 +887,12 @@ void Calculator::launch_direct(uint32_t n, double clock_rate)
 	record(slot.k0);
 	// 128-pattern tiles, 128 * C threads per block, 1024 threads per SM
 	const uint32_t ctas = std::min(ldp_ / 128u, (8u / C_) * num_sms_);
-	arm_poll();
+	if (ctas > block_sums_cap_)
+		throw Error(B3G_ERR_STATE, "short-list grid exceeds the block sums");
+	if (d_bsums_)
+		arm_host_fold(ctas);
+	else
+		arm_poll();
 	check_cuda(launch_prune4_direct(dp, ctas, stream_), "fused pruning kernel");
 	++in_flight_;
 	last_launches_ = 1;
@@ -1004,6 +1026,60 @@ void Calculator::arm_poll()
 		std::memcpy(h_lnl_, &kLnlSentinel, sizeof(double));
 }
 
+void Calculator::arm_host_fold(uint32_t blocks)
+{
+	host_fold_blocks_ = blocks;
+	poll_result_ = in_flight_ == 0;
+	if (poll_result_)
+		for (uint32_t k = 0; k < blocks; ++k)
+			std::memcpy(h_bsums_ + k, &kLnlSentinel, sizeof(double));
+}
+
+// Waits for every block's mapped sum to leave the sentinel (the same
+// stream queries as wait_mapped); false: the stream finished with a sum
+// missing, or polling was not armed.
+bool Calculator::wait_host_sums()
+{
+	const volatile uint64_t *w = reinterpret_cast<const volatile uint64_t *>(h_bsums_);
+	uint32_t k = 0;
+	for (uint32_t poll = 1; k < host_fold_blocks_; ++poll) {
+		if (w[k] != kLnlSentinel) {
+			++k;
+			continue;
+		}
+		if ((poll & 63u) == 0) {
+			const cudaError_t e = cudaStreamQuery(stream_);
+			if (e == cudaSuccess) {
+				for (; k < host_fold_blocks_; ++k)
+					if (w[k] == kLnlSentinel)
+						return false;
+				return true;
+			}
+			if (e != cudaErrorNotReady)
+				check_cuda(e, "evaluation");
+		}
+	}
+	return true;
+}
+
+// The device fold's order (block_fold): lane l of a warp adds sums l, l +
+// 32, ... in order, then a shuffle-down tree of halving offsets into lane
+// 0, so the result is the one a last block would have computed.
+double Calculator::fold_host_sums() const
+{
+	double lane[32];
+	for (uint32_t l = 0; l < 32; ++l) {
+		double sum = 0.0;
+		for (uint32_t k = l; k < host_fold_blocks_; k += 32)
+			sum += h_bsums_[k];
+		lane[l] = sum;
+	}
+	for (uint32_t off = 16; off > 0; off >>= 1)
+		for (uint32_t l = 0; l + off < 32; ++l)
+			lane[l] += lane[l + off];
+	return lane[0];
+}
+
 // Waits for the mapped result word to leave the sentinel; every 64 polls
 // the stream is queried, so a launch error surfaces and a stream that
 // finished without writing the word ends the wait (false: synchronise).
@@ -1037,6 +1113,25 @@ double Calculator::log_likelihood()
 	if (!have_result_)
 		throw Error(B3G_ERR_STATE, "no proposal evaluated yet");
 	double value;
+	if (host_fold_blocks_) {
+		if (!(poll_result_ && wait_host_sums()))
+			check_cuda(cudaStreamSynchronize(stream_), "sync");
+		upload_pending_ = false;
+		in_flight_ = 0;
+		for (uint32_t k = 0; k < host_fold_blocks_; ++k) {
+			uint64_t bits;
+			std::memcpy(&bits, h_bsums_ + k, sizeof(bits));
+			if (poll_result_ && bits == kLnlSentinel)
+				throw Error(B3G_ERR_CUDA,
+					    "the evaluation finished without writing its result");
+		}
+		value = fold_host_sums();
+		// later reads return the folded value
+		*h_lnl_ = value;
+		host_fold_blocks_ = 0;
+		poll_result_ = false;
+		return value;
+	}
 	if (poll_result_ && wait_mapped(value)) {
 		// the kernel ran, so the upload before it did too
 		upload_pending_ = false;

@@ -113,6 +113,16 @@ class Calculator {
 	bool poll_result_ = false;
 	void arm_poll();
 	bool wait_mapped(double &value);
+	// FP32 four-state walks (run walk, fused short list): every block writes
+	// its sum into the mapped array h_bsums_ and the host folds them in the
+	// device fold's order, so no block waits for a ticket and no last block
+	// folds.  host_fold_blocks_: the last launch's block count (0: its
+	// result is a single word).
+	double *h_bsums_ = nullptr, *d_bsums_ = nullptr;
+	uint32_t host_fold_blocks_ = 0;
+	void arm_host_fold(uint32_t blocks);
+	bool wait_host_sums();
+	double fold_host_sums() const;
 	struct TimingSlot;
 	void launch20(uint32_t n, bool matrices_mode, double clock_rate,
 		      bool want_cat, TimingSlot &slot);

@@ -553,6 +553,12 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
 	}
+	if (prm.sums_host) { // the host folds the blocks' sums
+		if (tid == 0)
+			prm.sums_host[blockIdx.x] =
+				isfinite(cta_sum) ? cta_sum + cta_comp : cta_sum;
+		return;
+	}
 	if (tid == 0) {
 		prm.block_sums[blockIdx.x] =
 			isfinite(cta_sum) ? cta_sum + cta_comp : cta_sum;
@@ -790,6 +796,12 @@ prune4_direct_kernel(const __grid_constant__ DirectParams prm)
 		const double tsum = tile_root(a, t, s_dot, s_cnt, s_red);
 		if (tid == 0)
 			neumaier_add(cta_sum, cta_comp, tsum);
+	}
+	if (prm.sums_host) { // the host folds the blocks' sums
+		if (tid == 0)
+			prm.sums_host[blockIdx.x] =
+				isfinite(cta_sum) ? cta_sum + cta_comp : cta_sum;
+		return;
 	}
 	if (tid == 0) {
 		prm.block_sums[blockIdx.x] =
