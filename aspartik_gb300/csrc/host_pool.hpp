@@ -6,6 +6,7 @@
 #pragma once
 
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdint>
 #include <exception>
@@ -93,17 +94,22 @@ class HostPool {
 				t.join();
 	}
 
-	// A worker spins on the job counter for a while after each job (the
-	// next step follows within microseconds), then sleeps.
+	// A worker spins on the job counter for up to a millisecond after each
+	// job (the next step follows within tens of microseconds, and a wake-up
+	// from sleep costs about as much as a step), then sleeps.
 	void work(uint32_t w)
 	{
-		constexpr uint32_t kSpin = 1u << 16;
+		using clock = std::chrono::steady_clock;
+		constexpr auto kSpin = std::chrono::microseconds(1000);
 		uint64_t seen = 0;
 		for (;;) {
 			uint64_t g = gen_.load(std::memory_order_acquire);
-			for (uint32_t k = 0; g == seen && k < kSpin; ++k) {
+			const auto t0 = clock::now();
+			for (uint32_t k = 1; g == seen; ++k) {
 				if (stop_.load(std::memory_order_acquire))
 					return;
+				if ((k & 1023u) == 0 && clock::now() - t0 > kSpin)
+					break;
 				g = gen_.load(std::memory_order_acquire);
 			}
 			if (g == seen) {

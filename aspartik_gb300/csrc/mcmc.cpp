@@ -172,15 +172,15 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 	uint32_t threads = cfg.host_threads;
 	if (const char *env = std::getenv("B3G_MCMC_THREADS"))
 		threads = (uint32_t)std::max(0, std::atoi(env));
-	if (threads == 0) // a thread for every four chains, at most 8
-		threads = std::min<uint32_t>(
-			{((uint32_t)chains_.size() + 3) / 4, 8u,
-			 std::max(1u, std::thread::hardware_concurrency())});
+	// automatic: a thread for every four chains, at most 8; the batched
+	// mode's host work per chain is a few copies, so it keeps to the
+	// calling thread unless asked otherwise
+	if (threads == 0)
+		threads = batch_ ? 1u
+				 : std::min<uint32_t>(
+					   {((uint32_t)chains_.size() + 3) / 4, 8u,
+					    std::max(1u, std::thread::hardware_concurrency())});
 	threads = std::min<uint32_t>(threads, (uint32_t)chains_.size());
-	// a batched step's host work per chain is a few copies: the pool's
-	// hand-offs cost more than they save
-	if (batch_)
-		threads = 1;
 	if (threads > 1) {
 		const int dev = cfg.device;
 		pool_ = std::make_unique<HostPool>(threads, [dev] {

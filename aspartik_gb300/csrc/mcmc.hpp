@@ -167,8 +167,8 @@ struct McmcConfig {
 	uint32_t clock_categories; // 0: strict clock
 	uint32_t launch;           // kLaunch*
 	// host threads that step the chains (0: one for every four chains, at
-	// most 8 and at most the hardware threads; 1: the calling thread
-	// alone; the batched launch mode uses the calling thread); the results
+	// most 8 and at most the hardware threads, and the calling thread alone
+	// in the batched launch mode; 1: the calling thread alone); the results
 	// do not depend on it
 	uint32_t host_threads;
 };

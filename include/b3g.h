@@ -391,9 +391,10 @@ typedef struct b3g_mcmc_config {
 	 * each proposes and launches its chains' evaluations, then reads
 	 * their results; statistics are gathered in chain order, so the
 	 * results are the same for every value.  0 = one for every four
-	 * chains, at most 8 and at most the hardware threads; 1 = the calling
-	 * thread alone (the environment variable B3G_MCMC_THREADS overrides
-	 * it).  The batched launch mode steps on the calling thread. */
+	 * chains, at most 8 and at most the hardware threads (the calling
+	 * thread alone in the batched launch mode, whose per-chain host work
+	 * is a few copies); 1 = the calling thread alone (the environment
+	 * variable B3G_MCMC_THREADS overrides it). */
 	uint32_t host_threads;
 } b3g_mcmc_config;
 
