@@ -181,6 +181,7 @@ struct DirectParams {
 	unsigned *ticket;   // zero between launches
 	double *lnl_out;    // device copy of the result
 	double *lnl_host;   // host-mapped pinned word, written by the last block
+			    // (without a host fold)
 	// host-mapped [gridDim.x], or null: each block writes its sum there and
 	// the host folds them (then lnl_out and lnl_host are not written)
 	double *sums_host;

@@ -104,9 +104,10 @@ class Calculator {
 	void launch_direct(uint32_t n, double clock_rate);
 	void wait_stage();
 	bool upload_pending_ = false; // an upload from h_stage_ may be in flight
-	// The fused short-list kernel and the run walk write the result into
-	// the mapped host word h_lnl_.  Before such a launch with no earlier
-	// evaluation in flight, the host stores a sentinel there and
+	// The fused short-list kernel and the run walk write their results
+	// into mapped host memory (the blocks' sums, h_bsums_ below; without
+	// it the word h_lnl_).  Before such a launch with no earlier
+	// evaluation in flight, the host stores sentinels there and
 	// log_likelihood polls for the result instead of synchronising the
 	// stream; otherwise (or on any other path) it synchronises.
 	uint32_t in_flight_ = 0; // evaluations launched since the last wait

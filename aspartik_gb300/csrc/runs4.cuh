@@ -569,7 +569,8 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 	__syncthreads();
 	if (!s_last)
 		return;
-	// the last block folds the block sums in a fixed-shape tree
+	// without a host fold the last block folds the block sums in a
+	// fixed-shape tree
 	__threadfence();
 	const double total = block_fold(prm.block_sums, gridDim.x, s_red);
 	if (tid == 0) {
@@ -586,8 +587,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 // walk).  Every block converts the device eigensystem to FP32, builds the
 // list's transition tables in shared memory with the same arithmetic as the
 // transition kernels (so results match a two-kernel evaluation bit for
-// bit), walks its tiles, and the last block writes the root lnL to the
-// device and to the host-mapped word.
+// bit), walks its tiles, and writes its sum to host-mapped memory, which
+// the host folds (with sums_host null: the last block folds the sums and
+// writes the root lnL to the device and to the host-mapped word).
 //
 // The walk is a chain: each entry needs the previous one's output, and its
 // other child is a clean partial written long ago (mostly in DRAM) or a tip
