@@ -100,8 +100,11 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 			    "per alignment)");
 	if (cfg.model > 1)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "model must be 0 (HKY) or 1 (GTR)");
-	if (cfg.launch > kLaunchBatch)
+	if (cfg.launch > kLaunchIndependent)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
+	if (cfg.launch == kLaunchIndependent && cfg.heat != 0.0 && cfg.swap_every != 0)
+		throw Error(B3G_ERR_INVALID_ARGUMENT,
+			    "independent stepping needs uncoupled chains (heat 0 or no swaps)");
 	for (uint32_t k = 0; k < kOpCount; ++k) {
 		if (!(cfg.weights[k] >= 0.0) || !std::isfinite(cfg.weights[k]))
 			throw Error(B3G_ERR_INVALID_ARGUMENT, "bad operator weight");
@@ -159,7 +162,8 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 	// stream, the launches of a step running concurrently
 	bool use_batch = cfg.launch == kLaunchBatch;
 	if (const char *env = std::getenv("B3G_MCMC_BATCH"))
-		use_batch = std::atoi(env) != 0;
+		if (cfg.launch != kLaunchIndependent)
+			use_batch = std::atoi(env) != 0;
 	if (use_batch && (cfg.precision != B3G_PRECISION_F32 || chains_.size() < 2))
 		use_batch = false;
 	if (use_batch) {
@@ -175,11 +179,14 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 	// automatic: a thread for every four chains, at most 8; the batched
 	// mode's host work per chain is a few copies, so it keeps to the
 	// calling thread unless asked otherwise
+	// (independent stepping: a thread per chain, at most 8)
 	if (threads == 0)
 		threads = batch_ ? 1u
-				 : std::min<uint32_t>(
-					   {((uint32_t)chains_.size() + 3) / 4, 8u,
-					    std::max(1u, std::thread::hardware_concurrency())});
+			  : std::min<uint32_t>(
+				    {cfg.launch == kLaunchIndependent
+					     ? (uint32_t)chains_.size()
+					     : ((uint32_t)chains_.size() + 3) / 4,
+				     8u, std::max(1u, std::thread::hardware_concurrency())});
 	threads = std::min<uint32_t>(threads, (uint32_t)chains_.size());
 	if (threads > 1) {
 		const int dev = cfg.device;
@@ -682,8 +689,49 @@ void Mcmc::screen_all()
 	}
 }
 
+void Mcmc::screen_chains(const std::vector<uint32_t> &idx, uint32_t ctx,
+			 std::vector<float> &xn, std::vector<float> &xo,
+			 std::vector<float> &out)
+{
+	const uint32_t n = (uint32_t)idx.size();
+	if (n == 0)
+		return;
+	xn.resize((size_t)n * kDaInputs);
+	xo.resize((size_t)n * kDaInputs);
+	out.resize(n);
+	for (uint32_t j = 0; j < n; ++j) {
+		const Chain &ch = *chains_[idx[j]];
+		for (uint32_t k = 0; k < kDaInputs; ++k) {
+			xn[j * kDaInputs + k] = (ch.feat_new[k] - in_mean_[k]) * in_scale_[k];
+			xo[j * kDaInputs + k] = (ch.feat_old[k] - in_mean_[k]) * in_scale_[k];
+		}
+	}
+	surrogate_->deltas(ctx, xn.data(), xo.data(), n, out.data());
+	for (uint32_t j = 0; j < n; ++j) {
+		Chain &ch = *chains_[idx[j]];
+		ch.da_delta = out_scale_ * (double)out[j];
+		const double log_r1 =
+			ch.beta * (ch.da_delta + ch.prior_new - ch.prior_cache) + ch.hastings;
+		if (log_r1 > std::log(ch.rng.uniform()))
+			ch.screened = true;
+		else
+			ch.status = 3;
+	}
+}
+
 void Mcmc::train_surrogate()
 {
+	// independent stepping: the chains' pilot pairs, in chain order
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		pilot_old_.insert(pilot_old_.end(), ch.pilot_old.begin(), ch.pilot_old.end());
+		pilot_new_.insert(pilot_new_.end(), ch.pilot_new.begin(), ch.pilot_new.end());
+		pilot_delta_.insert(pilot_delta_.end(), ch.pilot_delta.begin(),
+				    ch.pilot_delta.end());
+		ch.pilot_old.clear();
+		ch.pilot_new.clear();
+		ch.pilot_delta.clear();
+	}
 	const size_t n = pilot_delta_.size();
 	if (n < 64) { // too few pairs: stay with the exact chain
 		da_.fallback = 1;
@@ -727,6 +775,13 @@ void Mcmc::train_surrogate()
 	da_active_ = true;
 	drift_.assign(200, 0.0);
 	drift_pos_ = 0;
+	for (auto &chp : chains_) {
+		chp->da_on = true;
+		chp->drift.assign(200, 0.0);
+		chp->drift_pos = 0;
+	}
+	if (pool_ && cfg_.launch == kLaunchIndependent)
+		surrogate_->ensure_contexts(pool_->size());
 }
 
 void Mcmc::prepare(Chain &ch)
@@ -933,56 +988,66 @@ void Mcmc::set_tuning(uint32_t op, double tuning)
 	ops_[op].tuning = tuning;
 }
 
-void Mcmc::record()
+// The chain with the largest beta (the first of equals).
+size_t Mcmc::cold_chain() const
 {
-	// the trace fields of one chain
-	auto fields = [&](const Chain &ch, double f[8]) {
-		const DatedTree &tr = *ch.tree;
-		double length = 0.0;
-		for (uint32_t v = 0; v < tr.num_nodes(); ++v)
-			if (v != tr.root())
-				length += tr.edge_length(v);
-		f[0] = ch.lnl_cache;
-		f[1] = ch.prior_cache;
-		f[2] = ch.lnl_cache + ch.prior_cache;
-		f[3] = tr.root_height();
-		f[4] = cfg_.model == 0 ? ch.kappa.v : ch.rates.v[0];
-		f[5] = ch.alpha.v;
-		f[6] = length;
-		f[7] = cfg_.clock_categories ? ch.clock_sd.v : 0.0;
-	};
-	const Chain *cold = chains_[0].get();
-	for (const auto &c : chains_)
-		if (c->beta > cold->beta)
-			cold = c.get();
-	const DatedTree &t = *cold->tree;
-	double f[8];
-	fields(*cold, f);
+	size_t cold = 0;
+	for (size_t i = 1; i < chains_.size(); ++i)
+		if (chains_[i]->beta > chains_[cold]->beta)
+			cold = i;
+	return cold;
+}
+
+void Mcmc::record_chain(size_t i, bool cold, uint64_t step)
+{
+	const Chain &ch = *chains_[i];
+	const DatedTree &t = *ch.tree;
+	double length = 0.0;
+	for (uint32_t v = 0; v < t.num_nodes(); ++v)
+		if (v != t.root())
+			length += t.edge_length(v);
+	const double f[8] = {ch.lnl_cache,
+			     ch.prior_cache,
+			     ch.lnl_cache + ch.prior_cache,
+			     t.root_height(),
+			     cfg_.model == 0 ? ch.kappa.v : ch.rates.v[0],
+			     ch.alpha.v,
+			     length,
+			     cfg_.clock_categories ? ch.clock_sd.v : 0.0};
+	for (uint32_t k = 0; k < 8; ++k)
+		chain_trace_[i * 8 + k].push_back(f[k]);
+	if (!cold)
+		return;
 	for (uint32_t k = 0; k < 8; ++k)
 		trace_[k].push_back(f[k]);
-	chain_trace_.resize(chains_.size() * 8);
-	for (size_t i = 0; i < chains_.size(); ++i) {
-		fields(*chains_[i], f);
-		for (uint32_t k = 0; k < 8; ++k)
-			chain_trace_[i * 8 + k].push_back(f[k]);
-	}
 	// the whole sample for trace files: tree and parameters
-	sample_steps_.push_back(step_);
+	sample_steps_.push_back(step);
 	for (uint32_t v = 0; v < t.num_nodes(); ++v) {
 		sample_parents_.push_back(t.parent_of(v));
 		sample_heights_.push_back(t.height(v));
 	}
 	const double p[kSampleParams] = {
-		cold->kappa.v, cold->alpha.v, cold->birth_rate.v,
-		cold->rates.v[0], cold->rates.v[1], cold->rates.v[2],
-		cold->rates.v[3], cold->rates.v[4], cold->rates.v[5],
-		cold->freqs.v[0], cold->freqs.v[1], cold->freqs.v[2],
-		cold->freqs.v[3], cfg_.clock_categories ? cold->clock_sd.v : 0.0};
+		ch.kappa.v,    ch.alpha.v,    ch.birth_rate.v, ch.rates.v[0],
+		ch.rates.v[1], ch.rates.v[2], ch.rates.v[3],   ch.rates.v[4],
+		ch.rates.v[5], ch.freqs.v[0], ch.freqs.v[1],   ch.freqs.v[2],
+		ch.freqs.v[3], cfg_.clock_categories ? ch.clock_sd.v : 0.0};
 	sample_params_.insert(sample_params_.end(), p, p + kSampleParams);
+}
+
+void Mcmc::record()
+{
+	chain_trace_.resize(chains_.size() * 8);
+	const size_t cold = cold_chain();
+	for (size_t i = 0; i < chains_.size(); ++i)
+		record_chain(i, i == cold, step_);
 }
 
 void Mcmc::run(uint64_t steps)
 {
+	if (cfg_.launch == kLaunchIndependent) {
+		run_independent(steps);
+		return;
+	}
 	const uint32_t n = (uint32_t)chains_.size();
 	// chain i on host thread i % T, each thread's chains in order
 	auto each = [&](auto &&fn) {
@@ -1055,6 +1120,153 @@ void Mcmc::run(uint64_t steps)
 			tune();
 		if (cfg_.sample_every && step_ % cfg_.sample_every == 0)
 			record();
+	}
+}
+
+// Independent stepping.  Between two synchronisation points (an operator
+// tuning, the end of the delayed-acceptance pilot, the end of the call)
+// every host thread advances its own chains on their own, reading only
+// what stays fixed there (operator tunings, the surrogate, the
+// configuration) and counting into the chains' own accumulators; at the
+// point the counts are merged (integers: their order does not matter) and
+// the driver tunes or trains.  Pilot pairs are concatenated in chain order
+// when the surrogate is trained, and each chain keeps its own drift window.
+// So the results depend neither on the thread count nor on how the steps
+// are split into calls.
+void Mcmc::run_independent(uint64_t steps)
+{
+	const uint32_t T = pool_ ? pool_->size() : 1;
+	chain_trace_.resize(chains_.size() * 8);
+	uint64_t left = steps;
+	while (left > 0) {
+		uint64_t k = left;
+		if (cfg_.tune_every)
+			k = std::min<uint64_t>(k, cfg_.tune_every - step_ % cfg_.tune_every);
+		if (cfg_.da_pilot_steps && !surrogate_ && step_ < cfg_.da_pilot_steps)
+			k = std::min<uint64_t>(k, cfg_.da_pilot_steps - step_);
+		const uint64_t at = step_;
+		auto job = [&](uint32_t w) { window(w, T, at, k); };
+		if (pool_)
+			pool_->run(job);
+		else
+			job(0);
+		merge_own();
+		step_ += k;
+		left -= k;
+		if (cfg_.da_pilot_steps && step_ == cfg_.da_pilot_steps && !surrogate_)
+			train_surrogate();
+		if (cfg_.tune_every && step_ % cfg_.tune_every == 0)
+			tune();
+	}
+}
+
+void Mcmc::window(uint32_t w, uint32_t threads, uint64_t first_step, uint64_t count)
+{
+	const uint32_t n = (uint32_t)chains_.size();
+	const size_t cold = cold_chain();
+	std::vector<uint32_t> mine, idx;
+	for (uint32_t i = w; i < n; i += threads)
+		mine.push_back(i);
+	std::vector<float> xn, xo, out;
+	const bool screening = da_active_ && surrogate_;
+	for (uint64_t s = 0; s < count; ++s) {
+		const uint64_t step = first_step + s + 1;
+		for (const uint32_t i : mine)
+			prepare(*chains_[i]);
+		if (screening) {
+			idx.clear();
+			for (const uint32_t i : mine) {
+				const Chain &ch = *chains_[i];
+				if (ch.da_on && ch.status == 0 && ch.screenable)
+					idx.push_back(i);
+			}
+			screen_chains(idx, w, xn, xo, out);
+		}
+		for (const uint32_t i : mine)
+			if (chains_[i]->status == 0)
+				launch(*chains_[i]);
+		for (const uint32_t i : mine) {
+			settle(*chains_[i]);
+			tally_own(*chains_[i]);
+		}
+		if (cfg_.sample_every && step % cfg_.sample_every == 0)
+			for (const uint32_t i : mine)
+				record_chain(i, i == cold, step);
+	}
+}
+
+// tally() into the chain's own accumulators, with its own drift window.
+void Mcmc::tally_own(Chain &ch)
+{
+	OpStats &st = ch.acc_ops[ch.op];
+	DaStats &da = ch.acc_da;
+	if (ch.evaluated)
+		++da.exact_evaluations;
+	if (ch.status == 3)
+		++da.stage1_rejects;
+	if (ch.status == 0 && ch.finite) {
+		if (ch.screened) {
+			++(ch.accepted ? da.stage2_accepts : da.stage2_rejects);
+			const double err = ch.dlnl - ch.da_delta;
+			ch.drift[ch.drift_pos++ % ch.drift.size()] = err * err;
+			if (ch.drift_pos >= ch.drift.size()) {
+				double sum = 0.0;
+				for (const double e2 : ch.drift)
+					sum += e2;
+				da.drift_rms = std::sqrt(sum / ch.drift.size());
+				if (cfg_.da_drift_limit > 0.0 && da.drift_rms > cfg_.da_drift_limit) {
+					ch.da_on = false; // this chain back to the exact chain
+					da.fallback = 1;
+				}
+			}
+		}
+		if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
+		    da_.fallback == 0 && std::isfinite(ch.dlnl)) {
+			ch.pilot_old.insert(ch.pilot_old.end(), ch.feat_old, ch.feat_old + kDaInputs);
+			ch.pilot_new.insert(ch.pilot_new.end(), ch.feat_new, ch.feat_new + kDaInputs);
+			ch.pilot_delta.push_back((float)ch.dlnl);
+			++da.pilot_pairs;
+		}
+	}
+	if (ch.status == 1)
+		++st.aborts;
+	else if (ch.status == 2)
+		++st.prior_rejects;
+	if (ch.accepted) {
+		++st.accepts;
+		++st.window_accepts;
+	} else if (ch.status == 0 || ch.status == 3) {
+		++st.rejects;
+		++st.window_rejects;
+	}
+}
+
+void Mcmc::merge_own()
+{
+	for (auto &chp : chains_) {
+		Chain &ch = *chp;
+		for (uint32_t k = 0; k < kOpCount; ++k) {
+			OpStats &o = ops_[k];
+			const OpStats &a = ch.acc_ops[k];
+			o.accepts += a.accepts;
+			o.rejects += a.rejects;
+			o.aborts += a.aborts;
+			o.prior_rejects += a.prior_rejects;
+			o.window_accepts += a.window_accepts;
+			o.window_rejects += a.window_rejects;
+			ch.acc_ops[k] = OpStats{};
+		}
+		const DaStats &a = ch.acc_da;
+		da_.pilot_pairs += a.pilot_pairs;
+		da_.stage1_rejects += a.stage1_rejects;
+		da_.stage2_accepts += a.stage2_accepts;
+		da_.stage2_rejects += a.stage2_rejects;
+		da_.exact_evaluations += a.exact_evaluations;
+		da_.fallback |= a.fallback;
+		da_.drift_rms = std::max(da_.drift_rms, a.drift_rms);
+		ch.acc_da.pilot_pairs = ch.acc_da.stage1_rejects = 0;
+		ch.acc_da.stage2_accepts = ch.acc_da.stage2_rejects = 0;
+		ch.acc_da.exact_evaluations = 0;
 	}
 }
 

@@ -123,6 +123,11 @@ struct Problem {
 enum : uint32_t {
 	kLaunchStreams = 0, // one launch per chain, each chain on its own stream
 	kLaunchBatch = 1,   // every chain of a step in one graph-replayed batch
+	// each chain on its own stream, and the chains (no MC3 coupling: heat
+	// 0 or no swaps) advance independently between the driver's
+	// synchronisation points (operator tuning, the end of the
+	// delayed-acceptance pilot, the end of a run)
+	kLaunchIndependent = 2,
 };
 
 // Parameters of a state file in the reference's layout (Mcmc::dump,
@@ -166,10 +171,10 @@ struct McmcConfig {
 	double da_drift_limit;
 	uint32_t clock_categories; // 0: strict clock
 	uint32_t launch;           // kLaunch*
-	// host threads that step the chains (0: one for every four chains, at
-	// most 8 and at most the hardware threads, and the calling thread alone
-	// in the batched launch mode; 1: the calling thread alone); the results
-	// do not depend on it
+	// host threads that step the chains (0: one for every four chains, one
+	// per chain with independent stepping, at most 8 and at most the
+	// hardware threads, and the calling thread alone in the batched launch
+	// mode; 1: the calling thread alone); the results do not depend on it
 	uint32_t host_threads;
 };
 
@@ -226,6 +231,16 @@ struct Chain {
 	double dlnl = 0.0;      // its difference to the current state's
 	std::vector<uint32_t> internals, children;
 	std::vector<double> lengths;
+	// independent stepping: the chain's own statistics since the last
+	// synchronisation point (merged into the driver's there), its pilot
+	// pairs (concatenated in chain order for training), and its own
+	// delayed-acceptance drift window and screening switch
+	OpStats acc_ops[kOpCount];
+	DaStats acc_da;
+	std::vector<float> pilot_old, pilot_new, pilot_delta;
+	std::vector<double> drift;
+	size_t drift_pos = 0;
+	bool da_on = false;
 	explicit Chain(uint64_t seed) : rng(seed) {}
 };
 
@@ -320,6 +335,23 @@ class Mcmc {
 	void settle(Chain &ch);
 	// the step's statistics of one chain (calling thread, chain order)
 	void tally(const Chain &ch);
+	// independent stepping (kLaunchIndependent): `steps` steps in windows
+	// between synchronisation points; a window's steps of the chains of
+	// host thread w; the same statistics as tally() into the chain's own
+	// accumulators; their merge at a synchronisation point
+	void run_independent(uint64_t steps);
+	void window(uint32_t w, uint32_t threads, uint64_t first_step, uint64_t count);
+	void tally_own(Chain &ch);
+	void merge_own();
+	// screening of the listed chains' pending proposals through surrogate
+	// inference context ctx (one launch)
+	void screen_chains(const std::vector<uint32_t> &idx, uint32_t ctx,
+			   std::vector<float> &xn, std::vector<float> &xo,
+			   std::vector<float> &out);
+	// chain i's trace fields (and, for the cold chain, its sample) at
+	// step `step`
+	void record_chain(size_t i, bool cold, uint64_t step);
+	size_t cold_chain() const;
 	void swap_temperatures();
 	void tune();
 	void record();

@@ -77,7 +77,7 @@ b3g::McmcConfig config_of(const b3g_mcmc_config *config)
 		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT,
 				 "at most 64 relaxed-clock categories");
 	c.clock_categories = config->clock_categories;
-	if (config->launch > B3G_MCMC_LAUNCH_BATCH)
+	if (config->launch > B3G_MCMC_LAUNCH_INDEPENDENT)
 		throw b3g::Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
 	c.launch = config->launch;
 	if (config->host_threads > 256)

@@ -372,6 +372,11 @@ Mlp::~Mlp()
 	cudaFree(d_delta_);
 	cudaFree(d_loss_);
 	cudaFreeHost(h_pair_);
+	for (InferCtx &c : extra_) {
+		cudaStreamSynchronize(c.stream);
+		cudaStreamDestroy(c.stream);
+		cudaFreeHost(c.h);
+	}
 	if (stream_)
 		cudaStreamDestroy(stream_);
 }
@@ -591,14 +596,43 @@ float Mlp::delta(const float *x_new, const float *x_old)
 	return out;
 }
 
+void Mlp::ensure_contexts(uint32_t n)
+{
+	check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+	int least = 0, greatest = 0;
+	check_cuda(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+	while (extra_.size() + 1 < n) {
+		InferCtx c{};
+		check_cuda(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking,
+							 greatest),
+			   "surrogate stream");
+		check_cuda(cudaHostAlloc((void **)&c.h, sizeof(float) * kDeltaMax * (1 + 2 * in_),
+					 cudaHostAllocMapped),
+			   "mapped pairs");
+		check_cuda(cudaHostGetDevicePointer((void **)&c.d, c.h, 0), "mapped pairs");
+		extra_.push_back(c);
+	}
+}
+
 void Mlp::deltas(const float *x_new, const float *x_old, uint32_t count, float *out)
+{
+	deltas(0, x_new, x_old, count, out);
+}
+
+void Mlp::deltas(uint32_t ctx, const float *x_new, const float *x_old, uint32_t count,
+		 float *out)
 {
 	if (count == 0)
 		return;
 	if (count > kDeltaMax)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "too many surrogate pairs at once");
-	volatile uint32_t *words = reinterpret_cast<volatile uint32_t *>(h_pair_);
-	float *pairs = h_pair_ + kDeltaMax;
+	if (ctx > extra_.size())
+		throw Error(B3G_ERR_INVALID_ARGUMENT, "no such surrogate context");
+	float *const h_pair = ctx ? extra_[ctx - 1].h : h_pair_;
+	float *const d_pair = ctx ? extra_[ctx - 1].d : d_pair_;
+	const cudaStream_t stream = ctx ? extra_[ctx - 1].stream : stream_;
+	volatile uint32_t *words = reinterpret_cast<volatile uint32_t *>(h_pair);
+	float *pairs = h_pair + kDeltaMax;
 	const uint32_t stride = 2 * in_;
 	for (uint32_t k = 0; k < count; ++k) {
 		std::memcpy(pairs + (size_t)k * stride, x_new + (size_t)k * in_,
@@ -609,8 +643,8 @@ void Mlp::deltas(const float *x_new, const float *x_old, uint32_t count, float *
 	}
 	std::atomic_thread_fence(std::memory_order_seq_cst);
 	const size_t smem = sizeof(float) * 2 * (std::max(hidden_, in_) + hidden_);
-	mlp_delta_kernel<<<kDeltaCluster * count, 256, smem, stream_>>>(
-		d_params_, d_pair_ + kDeltaMax, d_pair_, in_, hidden_, stride);
+	mlp_delta_kernel<<<kDeltaCluster * count, 256, smem, stream>>>(
+		d_params_, d_pair + kDeltaMax, d_pair, in_, hidden_, stride);
 	check_cuda(cudaGetLastError(), "surrogate inference");
 	// poll the mapped words; every 64 polls ask the stream, so that an
 	// error surfaces and a finished kernel that wrote nothing ends the wait
@@ -623,7 +657,7 @@ void Mlp::deltas(const float *x_new, const float *x_old, uint32_t count, float *
 			continue;
 		}
 		if ((poll & 63u) == 0) {
-			const cudaError_t e = cudaStreamQuery(stream_);
+			const cudaError_t e = cudaStreamQuery(stream);
 			if (e == cudaSuccess) {
 				for (; k < count; ++k) {
 					bits = words[k];

@@ -47,6 +47,13 @@ class Mlp {
 	// the same for `count` pairs, x_new and x_old [count][in], in one
 	// launch (a cluster per pair)
 	void deltas(const float *x_new, const float *x_old, uint32_t count, float *out);
+	// Inference contexts: context 0 is the network's own stream and mapped
+	// staging; contexts 1..n-1 have their own highest-priority stream and
+	// staging, so that host threads screen concurrently (their launches go
+	// ahead of queued evaluation blocks).
+	void ensure_contexts(uint32_t n);
+	void deltas(uint32_t ctx, const float *x_new, const float *x_old, uint32_t count,
+		    float *out);
 
       private:
 	void ensure_batch(uint32_t rows);
@@ -70,6 +77,11 @@ class Mlp {
 	float *d_y_ = nullptr, *d_dy_ = nullptr, *d_delta_ = nullptr,
 	      *d_loss_ = nullptr;
 	float *d_pair_ = nullptr, *h_pair_ = nullptr; // inference staging
+	struct InferCtx {
+		cudaStream_t stream;
+		float *h, *d;
+	};
+	std::vector<InferCtx> extra_; // contexts 1.. (context 0: the above)
 };
 
 } // namespace b3g

@@ -61,7 +61,9 @@ class McmcSettings:
     # relaxed clock: rate categories per edge (0: strict clock)
     clock_categories: int = 0
     # "streams": one launch per chain on its own stream; "batch": every
-    # chain of a step in one graph-replayed batched launch (FP32)
+    # chain of a step in one graph-replayed batched launch (FP32);
+    # "independent": streams, uncoupled chains (heat 0 or no swaps)
+    # advancing on their own between tuning points
     launch: str = "streams"
     # host threads stepping the chains (0: one for every four chains, at
     # most 8; 1: the calling thread); the results are the same for every
@@ -69,7 +71,7 @@ class McmcSettings:
     host_threads: int = 0
 
 
-LAUNCH = {"streams": 0, "batch": 1}
+LAUNCH = {"streams": 0, "batch": 1, "independent": 2}
 
 
 def _config(settings: McmcSettings) -> "nat.McmcConfig":

@@ -463,7 +463,8 @@ def burn_in(wl, steps: int, device: int) -> tuple[dict, dict, float]:
 
 
 def mcmc_arm(wl, start, tunings, precision: str, steps: int, device: int, chains: int = 1,
-             da_pilot: int = 0, burn_frac: float = 0.05, seed: int = 4) -> dict:
+             da_pilot: int = 0, burn_frac: float = 0.05, seed: int = 4,
+             launch: str = "streams") -> dict:
     """One arm of the ESS/s comparison: `chains` chains (independent
     replicates stepping together) from `start`, `steps` steps, wall time of
     the whole run (pilot and surrogate training included).  ESS of lnL, root
@@ -474,7 +475,8 @@ def mcmc_arm(wl, start, tunings, precision: str, steps: int, device: int, chains
     from aspartik_gb300.ess import min_ess, multi_chain_ess
     from aspartik_gb300.mcmc import Mcmc
 
-    kw = dict(seed=seed, device=device, num_chains=chains, heat=0.0, swap_every=0)
+    kw = dict(seed=seed, device=device, num_chains=chains, heat=0.0, swap_every=0,
+              launch=launch)
     if da_pilot:
         kw.update(da_pilot_steps=da_pilot, da_epochs=100, da_hidden=256, da_drift_limit=20.0)
     m = Mcmc(wl["leaves"], wl["weights"], start["parents"], start["heights"],
@@ -497,7 +499,7 @@ def mcmc_arm(wl, start, tunings, precision: str, steps: int, device: int, chains
         e = min(per.values())
         traces = {"lnl": np.concatenate([m.trace("lnl", chain=c)[keep:]
                                          for c in range(chains)])}
-    out = {"chains": chains, "steps": steps, "seconds": round(dt, 3),
+    out = {"chains": chains, "launch": launch, "steps": steps, "seconds": round(dt, 3),
            "us_per_step": round(dt / steps * 1e6, 2),
            "chain_steps_per_s": round(chains * steps / dt, 1),
            "ess_min": round(e, 1), "ess": {k: round(v, 1) for k, v in per.items()},
@@ -522,10 +524,10 @@ def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
                                (trained on the GPU) screens the moves that
                                re-evaluate the whole tree
       chosen_f32_da_replicates the chosen form in full: 8 independent
-                               replicates stepping together (the step's
-                               screened proposals through one surrogate
-                               launch, then all chains' evaluations queued
-                               before any result is read) with delayed
+                               replicates, each on its own host thread and
+                               stream, advancing on their own between the
+                               driver's synchronisation points (operator
+                               tuning, the pilot's end), with delayed
                                acceptance (pilot: the first 1/16 of the
                                steps), chosen_steps / 3.75 steps (each
                                chain long enough that the multi-chain ESS,
@@ -549,7 +551,8 @@ def mcmc_ess(wl, chosen_steps: int, device: int) -> dict:
     progress("MCMC delayed-acceptance arm")
     rep = int(chosen_steps / 3.75)
     out["chosen_f32_da_replicates"] = mcmc_arm(wl, start, tunings, "f32", rep, device,
-                                               chains=8, da_pilot=rep // 16)
+                                               chains=8, da_pilot=rep // 16,
+                                               launch="independent")
     progress("MCMC replicates arm")
     base = max(out["plain_f64"]["ess_per_s"], 1e-12)
     for arm in ("chosen_f32", "chosen_f32_da", "chosen_f32_da_replicates"):
@@ -749,7 +752,7 @@ def mc3(wl, steps: int, device: int, chains: int = 8) -> dict:
     keep = (steps // 10) // 5
     traces = {k: m.trace(k)[keep:] for k in ESS_FIELDS}
     e, _ = min_ess(traces, burn_in=0.0)
-    out = {"chains": chains, "steps": steps, "seconds": round(dt, 3),
+    out = {"chains": chains, "launch": launch, "steps": steps, "seconds": round(dt, 3),
            "us_per_step": round(dt / steps * 1e6, 2),
            "chain_steps_per_s": round(chains * steps / dt, 1),
            "swaps_tried": tried, "swaps_accepted": accepted,

@@ -385,9 +385,20 @@ typedef struct b3g_mcmc_config {
 	 * B3G_MCMC_LAUNCH_BATCH (1, FP32 chosen form, several chains): every
 	 * chain's evaluation of a step in one replay of a captured CUDA graph
 	 * (b3g_batch_*: one staging copy, one persistent launch for the
-	 * members' short lists, one for the long ones, one read-back). */
+	 * members' short lists, one for the long ones, one read-back);
+	 * B3G_MCMC_LAUNCH_INDEPENDENT (2, chains not coupled by MC3: heat 0
+	 * or swap_every 0): as streams, but each host thread advances its
+	 * chains on their own between the driver's synchronisation points
+	 * (operator tuning, the end of the delayed-acceptance pilot, the end
+	 * of b3g_mcmc_run), so no chain waits for another's evaluation; the
+	 * chains' statistics are merged at those points, each chain keeps its
+	 * own delayed-acceptance drift window, and the results depend neither
+	 * on the thread count nor on how the steps are split into runs (they
+	 * differ from the other modes' in the statistics and drift decisions
+	 * only). */
 	uint32_t launch;
-	/* Host threads that step the chains, chain i on thread i % threads:
+	/* Host threads that step the chains, chain i on thread i % threads
+	 * (independent stepping: automatically one per chain, at most 8):
 	 * each proposes and launches its chains' evaluations, then reads
 	 * their results; statistics are gathered in chain order, so the
 	 * results are the same for every value.  0 = one for every four
@@ -398,7 +409,11 @@ typedef struct b3g_mcmc_config {
 	uint32_t host_threads;
 } b3g_mcmc_config;
 
-enum { B3G_MCMC_LAUNCH_STREAMS = 0, B3G_MCMC_LAUNCH_BATCH = 1 };
+enum {
+	B3G_MCMC_LAUNCH_STREAMS = 0,
+	B3G_MCMC_LAUNCH_BATCH = 1,
+	B3G_MCMC_LAUNCH_INDEPENDENT = 2
+};
 
 /* One alignment of a driver over several (b3g_mcmc_create_multi). */
 typedef struct b3g_mcmc_problem {
