@@ -102,9 +102,6 @@ Mcmc::Mcmc(const McmcConfig &cfg, const std::vector<Problem> &problems)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "model must be 0 (HKY) or 1 (GTR)");
 	if (cfg.launch > kLaunchIndependent)
 		throw Error(B3G_ERR_INVALID_ARGUMENT, "unknown launch mode");
-	if (cfg.launch == kLaunchIndependent && cfg.heat != 0.0 && cfg.swap_every != 0)
-		throw Error(B3G_ERR_INVALID_ARGUMENT,
-			    "independent stepping needs uncoupled chains (heat 0 or no swaps)");
 	for (uint32_t k = 0; k < kOpCount; ++k) {
 		if (!(cfg.weights[k] >= 0.0) || !std::isfinite(cfg.weights[k]))
 			throw Error(B3G_ERR_INVALID_ARGUMENT, "bad operator weight");
@@ -1123,13 +1120,14 @@ void Mcmc::run(uint64_t steps)
 	}
 }
 
-// Independent stepping.  Between two synchronisation points (an operator
-// tuning, the end of the delayed-acceptance pilot, the end of the call)
+// Independent stepping.  Between two synchronisation points (an MC3 swap
+// attempt, an operator tuning, the end of the delayed-acceptance pilot,
+// the end of the call)
 // every host thread advances its own chains on their own, reading only
 // what stays fixed there (operator tunings, the surrogate, the
-// configuration) and counting into the chains' own accumulators; at the
-// point the counts are merged (integers: their order does not matter) and
-// the driver tunes or trains.  Pilot pairs are concatenated in chain order
+// configuration, the temperatures) and counting into the chains' own
+// accumulators; at the point the counts are merged (integers: their order
+// does not matter) and the driver swaps, tunes or trains.  Pilot pairs are concatenated in chain order
 // when the surrogate is trained, and each chain keeps its own drift window.
 // So the results depend neither on the thread count nor on how the steps
 // are split into calls.
@@ -1144,6 +1142,8 @@ void Mcmc::run_independent(uint64_t steps)
 			k = std::min<uint64_t>(k, cfg_.tune_every - step_ % cfg_.tune_every);
 		if (cfg_.da_pilot_steps && !surrogate_ && step_ < cfg_.da_pilot_steps)
 			k = std::min<uint64_t>(k, cfg_.da_pilot_steps - step_);
+		if (cfg_.swap_every)
+			k = std::min<uint64_t>(k, cfg_.swap_every - step_ % cfg_.swap_every);
 		const uint64_t at = step_;
 		auto job = [&](uint32_t w) { window(w, T, at, k); };
 		if (pool_)
@@ -1155,6 +1155,8 @@ void Mcmc::run_independent(uint64_t steps)
 		left -= k;
 		if (cfg_.da_pilot_steps && step_ == cfg_.da_pilot_steps && !surrogate_)
 			train_surrogate();
+		if (cfg_.swap_every && step_ % cfg_.swap_every == 0)
+			swap_temperatures();
 		if (cfg_.tune_every && step_ % cfg_.tune_every == 0)
 			tune();
 	}

@@ -123,10 +123,10 @@ struct Problem {
 enum : uint32_t {
 	kLaunchStreams = 0, // one launch per chain, each chain on its own stream
 	kLaunchBatch = 1,   // every chain of a step in one graph-replayed batch
-	// each chain on its own stream, and the chains (no MC3 coupling: heat
-	// 0 or no swaps) advance independently between the driver's
-	// synchronisation points (operator tuning, the end of the
-	// delayed-acceptance pilot, the end of a run)
+	// each chain on its own stream, and the chains advance independently
+	// between the driver's synchronisation points (MC3 swap attempts,
+	// operator tuning, the end of the delayed-acceptance pilot, the end of
+	// a run)
 	kLaunchIndependent = 2,
 };
 

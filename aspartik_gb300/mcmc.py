@@ -62,8 +62,8 @@ class McmcSettings:
     clock_categories: int = 0
     # "streams": one launch per chain on its own stream; "batch": every
     # chain of a step in one graph-replayed batched launch (FP32);
-    # "independent": streams, uncoupled chains (heat 0 or no swaps)
-    # advancing on their own between tuning points
+    # "independent": streams, chains advancing on their own between swap
+    # attempts and tuning points
     launch: str = "streams"
     # host threads stepping the chains (0: one for every four chains, at
     # most 8; 1: the calling thread); the results are the same for every

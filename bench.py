@@ -650,7 +650,9 @@ def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
     one graph replay of the batched kernels (one staging copy, the run walk
     for long lists, the batched short-list kernel, one read-back), or one
     launch per chain on its own stream, the chains spread over host threads
-    (one for every four chains, at most 8).  Wall time per step and, batched,
+    (one for every four chains, at most 8), or the same with each thread
+    advancing its chains on their own between swap attempts (independent
+    stepping, 8 threads).  Wall time per step and, batched,
     the graph's device time per step (CUDA events); ESS of the cold chain of
     the first alignment (lnL, root height, first exchangeability)."""
     from aspartik_gb300.ess import min_ess
@@ -660,7 +662,7 @@ def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
     out = {"problems": [{k: p[k] for k in ("taxa", "sites", "patterns")} for p in probs],
            "chains": temps * len(probs), "temperatures": temps, "steps": steps,
            "host_threads_streams": min((temps * len(probs) + 3) // 4, 8, os.cpu_count() or 1)}
-    for launch in ("batch", "streams"):
+    for launch in ("batch", "streams", "independent"):
         s = McmcSettings(model="gtr", precision="f32", num_categories=4,
                          num_chains=temps * len(probs), heat=0.1, swap_every=10, seed=4,
                          sample_every=10, weights=dict(GTR_WEIGHTS), device=device,
@@ -694,7 +696,8 @@ def c4_mcmc(device: int, steps: int, temps: int = 8) -> dict:
             arm["wall_over_device"] = round(arm["wall_us_per_step"] / max(dev_us, 1e-9), 3)
         out[launch] = arm
         m.close()
-    out["faster"] = min(("batch", "streams"), key=lambda k: out[k]["wall_us_per_step"])
+    out["faster"] = min(("batch", "streams", "independent"),
+                        key=lambda k: out[k]["wall_us_per_step"])
     return out
 
 
@@ -729,18 +732,18 @@ def dedup_leg(device: int, seed: int = 4) -> dict:
             "cpu_baseline_ms": round(t_cpu * 1e3, 3), "identical_to_cpu": same}
 
 
-def mc3(wl, steps: int, device: int, chains: int = 8) -> dict:
+def mc3(wl, steps: int, device: int, chains: int = 8, launch: str = "independent") -> dict:
     """Metropolis-coupled MCMC on the workload: `chains` FP32 chains at
     beta_i = 1 / (1 + 0.1 i), swap attempts every 10 steps, the moves of
-    mcmc_ess.  Every chain launches its own evaluations on its own stream and
-    all chains' evaluations of a step are queued before any result is read
-    (the driver's default; the batched CUDA-graph launch is opt-in,
-    B3G_MCMC_BATCH=1)."""
+    mcmc_ess.  Every chain launches its own evaluations on its own stream;
+    with independent stepping (the default here) each host thread advances
+    its chains on their own between swap attempts, otherwise all chains'
+    evaluations of a step are queued before any result is read."""
     from aspartik_gb300.ess import min_ess
     from aspartik_gb300.mcmc import Mcmc
 
     s = mcmc_settings(wl, "f32", num_chains=chains, heat=0.1, swap_every=10, seed=4,
-                      device=device)
+                      device=device, launch=launch)
     m = Mcmc(wl["leaves"], wl["weights"], wl["tree"].parents, wl["tree"].heights, s)
     m.set_parameters(rates=wl["rates"], frequencies=wl["pi"],
                      alpha=wl["spec"]["alpha"] or 1.0, birth_rate=1.0)

@@ -386,11 +386,11 @@ typedef struct b3g_mcmc_config {
 	 * chain's evaluation of a step in one replay of a captured CUDA graph
 	 * (b3g_batch_*: one staging copy, one persistent launch for the
 	 * members' short lists, one for the long ones, one read-back);
-	 * B3G_MCMC_LAUNCH_INDEPENDENT (2, chains not coupled by MC3: heat 0
-	 * or swap_every 0): as streams, but each host thread advances its
-	 * chains on their own between the driver's synchronisation points
-	 * (operator tuning, the end of the delayed-acceptance pilot, the end
-	 * of b3g_mcmc_run), so no chain waits for another's evaluation; the
+	 * B3G_MCMC_LAUNCH_INDEPENDENT (2): as streams, but each host thread
+	 * advances its chains on their own between the driver's
+	 * synchronisation points (MC3 swap attempts, operator tuning, the end
+	 * of the delayed-acceptance pilot, the end of b3g_mcmc_run), so no
+	 * chain waits for another's evaluation in between; the
 	 * chains' statistics are merged at those points, each chain keeps its
 	 * own delayed-acceptance drift window, and the results depend neither
 	 * on the thread count nor on how the steps are split into runs (they

@@ -148,12 +148,34 @@ def test_independent_stepping_is_deterministic(da):
         assert base["da"] == other["da"]
 
 
-def test_independent_stepping_refuses_coupled_chains():
-    from aspartik_gb300._native import B3GError
+def test_independent_stepping_with_swaps_is_deterministic():
+    """MC3 chains advancing on their own between swap attempts: the same
+    traces, swaps and temperatures on 1 and 4 host threads and over several
+    calls, and the ladder stays a permutation of the temperatures."""
     from aspartik_gb300.mcmc import Mcmc, McmcSettings
 
-    c = dna_case(12, 200, seed=44, model="gtr", alpha=0.5, num_categories=4)
-    s = McmcSettings(model="gtr", precision="f32", num_categories=4, num_chains=4,
-                     heat=0.1, swap_every=10, launch="independent")
-    with pytest.raises(B3GError):
-        Mcmc(c.leaves, c.weights, c.tree.parents, c.tree.heights, s)
+    probs = problems()
+    runs = []
+    for threads, split in ((1, (800,)), (4, (333, 467))):
+        s = McmcSettings(model="gtr", precision="f32", num_categories=4, num_chains=6,
+                         heat=HEAT, swap_every=7, seed=19, sample_every=5, tune_every=100,
+                         launch="independent", host_threads=threads)
+        m = Mcmc.multi(probs, s)
+        m.set_parameters(rates=np.ones(6), frequencies=np.full(4, 0.25), alpha=0.5,
+                         birth_rate=1.0)
+        for k in split:
+            m.run(k)
+        assert m.check() < 1e-12
+        betas = [m.chain_state(i)[3] for i in range(6)]
+        runs.append(dict(traces=[m.trace("lnl", chain=i) for i in range(6)],
+                         swaps=m.swaps(), betas=betas, ops=m.operator_stats()))
+        m.close()
+    a, b = runs
+    assert a["swaps"][0] == 2 * (800 // 7) and a["swaps"][1] > 0
+    assert a["swaps"] == b["swaps"] and a["betas"] == b["betas"] and a["ops"] == b["ops"]
+    for x, y in zip(a["traces"], b["traces"]):
+        np.testing.assert_array_equal(x, y)
+    ladder = sorted(1.0 / (1.0 + HEAT * k) for k in range(3))
+    for g in range(2):
+        np.testing.assert_allclose(sorted(a["betas"][3 * g:3 * g + 3]), ladder, rtol=0,
+                                   atol=1e-15)
