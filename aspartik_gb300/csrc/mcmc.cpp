@@ -1159,6 +1159,8 @@ void Mcmc::run_independent(uint64_t steps)
 			swap_temperatures();
 		if (cfg_.tune_every && step_ % cfg_.tune_every == 0)
 			tune();
+		if (cfg_.sample_every && step_ % cfg_.sample_every == 0)
+			record();
 	}
 }
 
@@ -1191,7 +1193,9 @@ void Mcmc::window(uint32_t w, uint32_t threads, uint64_t first_step, uint64_t co
 			settle(*chains_[i]);
 			tally_own(*chains_[i]);
 		}
-		if (cfg_.sample_every && step % cfg_.sample_every == 0)
+		// a sample at the window's last step is taken at the
+		// synchronisation point, after a swap there (as in lockstep)
+		if (cfg_.sample_every && step % cfg_.sample_every == 0 && s + 1 < count)
 			for (const uint32_t i : mine)
 				record_chain(i, i == cold, step);
 	}

@@ -150,16 +150,19 @@ def test_independent_stepping_is_deterministic(da):
 
 def test_independent_stepping_with_swaps_is_deterministic():
     """MC3 chains advancing on their own between swap attempts: the same
-    traces, swaps and temperatures on 1 and 4 host threads and over several
-    calls, and the ladder stays a permutation of the temperatures."""
+    traces (each chain's and the cold chain's), swaps and temperatures on 1
+    and 4 host threads and over several calls as the lockstep driver's
+    (without delayed acceptance the statistics merge changes nothing), and
+    the ladder stays a permutation of the temperatures."""
     from aspartik_gb300.mcmc import Mcmc, McmcSettings
 
     probs = problems()
     runs = []
-    for threads, split in ((1, (800,)), (4, (333, 467))):
+    for launch, threads, split in (("independent", 1, (800,)), ("independent", 4, (333, 467)),
+                                   ("streams", 2, (800,))):
         s = McmcSettings(model="gtr", precision="f32", num_categories=4, num_chains=6,
                          heat=HEAT, swap_every=7, seed=19, sample_every=5, tune_every=100,
-                         launch="independent", host_threads=threads)
+                         launch=launch, host_threads=threads)
         m = Mcmc.multi(probs, s)
         m.set_parameters(rates=np.ones(6), frequencies=np.full(4, 0.25), alpha=0.5,
                          birth_rate=1.0)
@@ -168,13 +171,16 @@ def test_independent_stepping_with_swaps_is_deterministic():
         assert m.check() < 1e-12
         betas = [m.chain_state(i)[3] for i in range(6)]
         runs.append(dict(traces=[m.trace("lnl", chain=i) for i in range(6)],
-                         swaps=m.swaps(), betas=betas, ops=m.operator_stats()))
+                         cold=m.trace("lnl"), swaps=m.swaps(), betas=betas,
+                         ops=m.operator_stats()))
         m.close()
-    a, b = runs
+    a = runs[0]
     assert a["swaps"][0] == 2 * (800 // 7) and a["swaps"][1] > 0
-    assert a["swaps"] == b["swaps"] and a["betas"] == b["betas"] and a["ops"] == b["ops"]
-    for x, y in zip(a["traces"], b["traces"]):
-        np.testing.assert_array_equal(x, y)
+    for b in runs[1:]:
+        assert a["swaps"] == b["swaps"] and a["betas"] == b["betas"] and a["ops"] == b["ops"]
+        np.testing.assert_array_equal(a["cold"], b["cold"])
+        for x, y in zip(a["traces"], b["traces"]):
+            np.testing.assert_array_equal(x, y)
     ladder = sorted(1.0 / (1.0 + HEAT * k) for k in range(3))
     for g in range(2):
         np.testing.assert_allclose(sorted(a["betas"][3 * g:3 * g + 3]), ladder, rtol=0,
