@@ -684,19 +684,27 @@ __device__ __forceinline__ void direct_walk(const NodeOp *ops, const uint8_t (*s
 					if (sr == kSrcTip) {
 						in[j] = tb[ps[u][j]];
 						sc[j] = 0;
-					} else if (sr == kSrcClean) {
-						in[j] = v4_apply(tb, pv[u][j]);
-						sc[j] = ps[u][j];
-					} else if (sr == kSrcPrev) {
-						in[j] = v4_apply(tb, y0);
-						sc[j] = c0;
-					} else if (sr == kSrcPrev2) {
-						in[j] = v4_apply(tb, y1);
-						sc[j] = c1;
 					} else {
-						const Idx ix = (Idx)ids[j] * stride + col_off;
-						in[j] = v4_apply(tb, part[ix]);
-						sc[j] = scales[ix];
+						// the internal child's vector, then one product
+						// (one copy of the code for every source)
+						float4 x;
+						int32_t s;
+						if (sr == kSrcClean) {
+							x = pv[u][j];
+							s = ps[u][j];
+						} else if (sr == kSrcPrev) {
+							x = y0;
+							s = c0;
+						} else if (sr == kSrcPrev2) {
+							x = y1;
+							s = c1;
+						} else {
+							const Idx ix = (Idx)ids[j] * stride + col_off;
+							x = part[ix];
+							s = scales[ix];
+						}
+						in[j] = v4_apply(tb, x);
+						sc[j] = s;
 					}
 				}
 				// the slot just consumed takes entry i + ahead
