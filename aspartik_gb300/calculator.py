@@ -162,15 +162,13 @@ class GpuCalculator:
         check(lib.b3g_calculator_set_gamma(self._h, float(alpha)))
 
     def propose_lengths(self, internals, children, lengths, clock_rate: float = 1.0) -> None:
-        internals = nat.u32(internals)
-        children = nat.u32(children).reshape(-1)
-        lengths = nat.f64(lengths).reshape(-1)
+        internals, pi = nat.arr_addr(internals, np.uint32)
+        children, pc = nat.arr_addr(children, np.uint32)
+        lengths, pl = nat.arr_addr(lengths, np.float64)
         n = internals.size
         if children.size != 2 * n or lengths.size != 2 * n:
             raise ValueError("children and lengths need two values per internal")
-        check(lib.b3g_calculator_propose_lengths(
-            self._h, nat.addr(internals), nat.addr(children), n, nat.addr(lengths),
-            float(clock_rate)))
+        check(lib.b3g_calculator_propose_lengths(self._h, pi, pc, n, pl, float(clock_rate)))
 
     def autotune(self, internals, children, lengths, clock_rate: float = 1.0) -> int:
         """Time the list with each launch configuration of this form and keep
