@@ -1,6 +1,7 @@
 // calculator.cu -- host orchestration of one device-resident pruning store
 // and the C ABI declared in include/b3g.h.
 #include "calculator.hpp"
+#include "host_fold.hpp"
 #include "host_math.hpp"
 
 #include <cmath>
@@ -1062,22 +1063,9 @@ bool Calculator::wait_host_sums()
 	return true;
 }
 
-// The device fold's order (block_fold): lane l of a warp adds sums l, l +
-// 32, ... in order, then a shuffle-down tree of halving offsets into lane
-// 0, so the result is the one a last block would have computed.
 double Calculator::fold_host_sums() const
 {
-	double lane[32];
-	for (uint32_t l = 0; l < 32; ++l) {
-		double sum = 0.0;
-		for (uint32_t k = l; k < host_fold_blocks_; k += 32)
-			sum += h_bsums_[k];
-		lane[l] = sum;
-	}
-	for (uint32_t off = 16; off > 0; off >>= 1)
-		for (uint32_t l = 0; l + off < 32; ++l)
-			lane[l] += lane[l + off];
-	return lane[0];
+	return fold_block_sums(h_bsums_, host_fold_blocks_);
 }
 
 // Waits for the mapped result word to leave the sentinel; every 64 polls
