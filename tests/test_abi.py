@@ -91,3 +91,27 @@ def test_no_gpu_reports_cuda_error():
                                        ct.byref(handle))
     assert st in (nat.B3G_ERR_CUDA, nat.B3G_ERR_INVALID_ARGUMENT)
     assert nat.lib.b3g_last_error()
+
+
+def test_array_addresses_for_per_call_arguments():
+    """nat.arr_addr: an array already C-contiguous of the asked type comes
+    back as itself (no copy) with its data address; anything else is
+    converted first; read-only and empty arrays take the ctypes path."""
+    from aspartik_gb300 import _native as nat
+
+    a = np.arange(10, dtype=np.uint32)
+    same, p = nat.arr_addr(a, np.uint32)
+    assert same is a and p == a.ctypes.data
+    b = np.arange(20, dtype=np.int64)[::2]
+    conv, q = nat.arr_addr(b, np.uint32)
+    assert conv is not b and conv.dtype == np.uint32 and conv.flags.c_contiguous
+    assert q == conv.ctypes.data and list(conv) == list(range(0, 20, 2))
+    m = np.arange(6, dtype=np.float64).reshape(3, 2)
+    same2, r = nat.arr_addr(m, np.float64)
+    assert same2 is m and r == m.ctypes.data
+    ro = np.arange(4, dtype=np.float64)
+    ro.flags.writeable = False
+    got, s = nat.arr_addr(ro, np.float64)
+    assert got is ro and s == ro.ctypes.data
+    empty, _ = nat.arr_addr([], np.uint32)
+    assert empty.size == 0
