@@ -654,36 +654,10 @@ void Mcmc::features(const Chain &ch, float *out) const
 void Mcmc::screen_all()
 {
 	screen_idx_.clear();
-	for (auto &ch : chains_)
-		if (ch->status == 0 && ch->screenable)
-			screen_idx_.push_back(ch->index);
-	const uint32_t n = (uint32_t)screen_idx_.size();
-	if (n == 0)
-		return;
-	screen_xn_.resize((size_t)n * kDaInputs);
-	screen_xo_.resize((size_t)n * kDaInputs);
-	screen_out_.resize(n);
-	for (uint32_t j = 0; j < n; ++j) {
-		const Chain &ch = *chains_[screen_idx_[j]];
-		for (uint32_t k = 0; k < kDaInputs; ++k) {
-			screen_xn_[j * kDaInputs + k] =
-				(ch.feat_new[k] - in_mean_[k]) * in_scale_[k];
-			screen_xo_[j * kDaInputs + k] =
-				(ch.feat_old[k] - in_mean_[k]) * in_scale_[k];
-		}
-	}
-	surrogate_->deltas(screen_xn_.data(), screen_xo_.data(), n, screen_out_.data());
-	for (uint32_t j = 0; j < n; ++j) {
-		Chain &ch = *chains_[screen_idx_[j]];
-		ch.da_delta = out_scale_ * (double)screen_out_[j];
-		const double log_r1 = ch.beta * (ch.da_delta + ch.prior_new -
-						 ch.prior_cache) +
-				      ch.hastings;
-		if (log_r1 > std::log(ch.rng.uniform()))
-			ch.screened = true;
-		else
-			ch.status = 3;
-	}
+	for (size_t i = 0; i < chains_.size(); ++i)
+		if (chains_[i]->status == 0 && chains_[i]->screenable)
+			screen_idx_.push_back((uint32_t)i);
+	screen_chains(screen_idx_, 0, screen_xn_, screen_xo_, screen_out_);
 }
 
 void Mcmc::screen_chains(const std::vector<uint32_t> &idx, uint32_t ctx,
