@@ -838,40 +838,44 @@ void Mcmc::settle(Chain &ch)
 
 // In chain order, so the counters, the drift window and the surrogate's
 // pilot pairs do not depend on the host threads.
-void Mcmc::tally(const Chain &ch)
+// The step's statistics of one chain into `sink`: the driver's own
+// counters, drift window and pilot pairs (lockstep) or the chain's
+// (independent stepping).
+void Mcmc::tally_into(const Chain &ch, const TallySink &sink)
 {
-	OpStats &st = ops_[ch.op];
+	OpStats &st = sink.ops[ch.op];
+	DaStats &da = *sink.da;
 	if (ch.evaluated)
-		++da_.exact_evaluations;
+		++da.exact_evaluations;
 	if (ch.status == 3)
-		++da_.stage1_rejects;
+		++da.stage1_rejects;
 	if (ch.status == 0 && ch.finite) {
 		if (ch.screened) {
-			++(ch.accepted ? da_.stage2_accepts : da_.stage2_rejects);
+			++(ch.accepted ? da.stage2_accepts : da.stage2_rejects);
 			// drift of the screen: RMS of the last window of errors
+			std::vector<double> &drift = *sink.drift;
 			const double err = ch.dlnl - ch.da_delta;
-			drift_[drift_pos_++ % drift_.size()] = err * err;
-			if (drift_pos_ >= drift_.size()) {
-				double s = 0.0;
-				for (const double e2 : drift_)
-					s += e2;
-				da_.drift_rms = std::sqrt(s / drift_.size());
-				if (cfg_.da_drift_limit > 0.0 &&
-				    da_.drift_rms > cfg_.da_drift_limit) {
-					da_active_ = false; // back to the exact chain
-					da_.fallback = 1;
+			drift[(*sink.drift_pos)++ % drift.size()] = err * err;
+			if (*sink.drift_pos >= drift.size()) {
+				double sum = 0.0;
+				for (const double e2 : drift)
+					sum += e2;
+				da.drift_rms = std::sqrt(sum / drift.size());
+				if (cfg_.da_drift_limit > 0.0 && da.drift_rms > cfg_.da_drift_limit) {
+					*sink.screening = false; // back to the exact chain
+					da.fallback = 1;
 				}
 			}
 		}
 		// pilot pairs for the surrogate
-		if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
-		    da_.fallback == 0 && std::isfinite(ch.dlnl)) {
-			pilot_old_.insert(pilot_old_.end(), ch.feat_old,
-					  ch.feat_old + kDaInputs);
-			pilot_new_.insert(pilot_new_.end(), ch.feat_new,
-					  ch.feat_new + kDaInputs);
-			pilot_delta_.push_back((float)ch.dlnl);
-			++da_.pilot_pairs;
+		if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ && da_.fallback == 0 &&
+		    std::isfinite(ch.dlnl)) {
+			sink.pilot_old->insert(sink.pilot_old->end(), ch.feat_old,
+					       ch.feat_old + kDaInputs);
+			sink.pilot_new->insert(sink.pilot_new->end(), ch.feat_new,
+					       ch.feat_new + kDaInputs);
+			sink.pilot_delta->push_back((float)ch.dlnl);
+			++da.pilot_pairs;
 		}
 	}
 	if (ch.status == 1)
@@ -885,6 +889,12 @@ void Mcmc::tally(const Chain &ch)
 		++st.rejects;
 		++st.window_rejects;
 	}
+}
+
+void Mcmc::tally(const Chain &ch)
+{
+	tally_into(ch, TallySink{ops_, &da_, &drift_, &drift_pos_, &da_active_, &pilot_old_,
+				 &pilot_new_, &pilot_delta_});
 }
 
 // Metropolis coupling: adjacent temperatures exchange with probability
@@ -1178,47 +1188,8 @@ void Mcmc::window(uint32_t w, uint32_t threads, uint64_t first_step, uint64_t co
 // tally() into the chain's own accumulators, with its own drift window.
 void Mcmc::tally_own(Chain &ch)
 {
-	OpStats &st = ch.acc_ops[ch.op];
-	DaStats &da = ch.acc_da;
-	if (ch.evaluated)
-		++da.exact_evaluations;
-	if (ch.status == 3)
-		++da.stage1_rejects;
-	if (ch.status == 0 && ch.finite) {
-		if (ch.screened) {
-			++(ch.accepted ? da.stage2_accepts : da.stage2_rejects);
-			const double err = ch.dlnl - ch.da_delta;
-			ch.drift[ch.drift_pos++ % ch.drift.size()] = err * err;
-			if (ch.drift_pos >= ch.drift.size()) {
-				double sum = 0.0;
-				for (const double e2 : ch.drift)
-					sum += e2;
-				da.drift_rms = std::sqrt(sum / ch.drift.size());
-				if (cfg_.da_drift_limit > 0.0 && da.drift_rms > cfg_.da_drift_limit) {
-					ch.da_on = false; // this chain back to the exact chain
-					da.fallback = 1;
-				}
-			}
-		}
-		if (ch.screenable && cfg_.da_pilot_steps && !surrogate_ &&
-		    da_.fallback == 0 && std::isfinite(ch.dlnl)) {
-			ch.pilot_old.insert(ch.pilot_old.end(), ch.feat_old, ch.feat_old + kDaInputs);
-			ch.pilot_new.insert(ch.pilot_new.end(), ch.feat_new, ch.feat_new + kDaInputs);
-			ch.pilot_delta.push_back((float)ch.dlnl);
-			++da.pilot_pairs;
-		}
-	}
-	if (ch.status == 1)
-		++st.aborts;
-	else if (ch.status == 2)
-		++st.prior_rejects;
-	if (ch.accepted) {
-		++st.accepts;
-		++st.window_accepts;
-	} else if (ch.status == 0 || ch.status == 3) {
-		++st.rejects;
-		++st.window_rejects;
-	}
+	tally_into(ch, TallySink{ch.acc_ops, &ch.acc_da, &ch.drift, &ch.drift_pos, &ch.da_on,
+				 &ch.pilot_old, &ch.pilot_new, &ch.pilot_delta});
 }
 
 void Mcmc::merge_own()

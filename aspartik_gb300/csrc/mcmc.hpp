@@ -335,6 +335,15 @@ class Mcmc {
 	void settle(Chain &ch);
 	// the step's statistics of one chain (calling thread, chain order)
 	void tally(const Chain &ch);
+	struct TallySink {
+		OpStats *ops; // [kOpCount]
+		DaStats *da;
+		std::vector<double> *drift;
+		size_t *drift_pos;
+		bool *screening; // cleared when the drift exceeds its limit
+		std::vector<float> *pilot_old, *pilot_new, *pilot_delta;
+	};
+	void tally_into(const Chain &ch, const TallySink &sink);
 	// independent stepping (kLaunchIndependent): `steps` steps in windows
 	// between synchronisation points; a window's steps of the chains of
 	// host thread w; the same statistics as tally() into the chain's own
