@@ -115,3 +115,26 @@ def test_array_addresses_for_per_call_arguments():
     assert got is ro and s == ro.ctypes.data
     empty, _ = nat.arr_addr([], np.uint32)
     assert empty.size == 0
+
+
+def test_mcmc_settings_fill_the_c_config():
+    """McmcSettings -> b3g_mcmc_config: operator weights by name, the launch
+    mode (independent stepping = 2) and the host thread count land in the
+    struct's fields, and an unknown operator name is refused."""
+    from aspartik_gb300 import _native as nat
+    from aspartik_gb300.mcmc import OPERATORS, McmcSettings, _config
+
+    s = McmcSettings(model="hky", precision="f64", num_categories=1, num_chains=8,
+                     weights={"tree_scale": 3, "scale_kappa": 1, "node_slide": 2},
+                     launch="independent", host_threads=5, da_pilot_steps=100,
+                     clock_categories=4)
+    c = _config(s)
+    assert c.num_chains == 8 and c.num_categories == 1 and c.model == 0
+    assert c.precision == nat.PRECISION_F64
+    assert c.launch == 2 and c.host_threads == 5
+    assert c.da_pilot_steps == 100 and c.clock_categories == 4 and c.da_reserved == 0
+    w = list(c.op_weights)
+    assert w[OPERATORS.index("tree_scale")] == 3 and w[OPERATORS.index("node_slide")] == 2
+    assert sum(w) == 6
+    with pytest.raises(ValueError):
+        _config(McmcSettings(weights={"no_such_move": 1}))
